@@ -1,0 +1,351 @@
+"""Benchmark of the GB300 Signalsmith-FFT transform path.
+
+Default workload (the batched RealFFT<float> configuration): N in {480, 960, 1920, 3840}, 16384
+frames per size, each frame N(0,1) noise plus 3 sinusoids (seeded); one step = forward (real ->
+N/2 bins, DC/Nyquist in bin 0) and inverse of every size.  Metric: GFLOP/s with 2.5 N log2 N
+flops per real transform.
+
+Reported on one JSON line:
+* value        -- device-resident throughput (inputs already in HBM), CUDA events over K steps;
+* e2e          -- the same work through the C ABI's host-buffer entry point ssfft_exec_host
+                  (pinned host input -> device -> pinned host output, copies inside the timing);
+* roofline     -- the dominant kernel's algorithmic bytes / its mean CUDA-event duration,
+                  against the measured HBM copy bandwidth;
+* cpu_baseline -- the reference algorithm (the C restatement in oracle/, one plan per thread) on
+                  all host cores over the same frames.
+`--impl reference` times that CPU implementation alone, as the reference arm.
+
+Multi-GPU: every rank runs an independent replica of the workload (the transforms are
+independent; there is no exchange step), `value` sums all ranks' work over the slowest rank.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "batched+served FFT GFLOP/s, p99 lat vs plain GPU FFT @ relL2≤1e-6 (FP32)"
+SIZES = (480, 960, 1920, 3840)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--frames", type=int, default=16384)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the host-buffer leg (default: steps/10)")
+    return ap.parse_args()
+
+
+def frames_for(n: int, frames: int, seed: int) -> np.ndarray:
+    """Gaussian N(0,1) noise + 3 sinusoids per frame: frequency U(0, n/2), amplitude U[0.1, 2],
+    phase U[0, 2 pi)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    x = rng.standard_normal((frames, n), dtype=np.float32)
+    t = np.arange(n, dtype=np.float32)
+    for _ in range(3):
+        f = rng.uniform(0, n / 2, (frames, 1)).astype(np.float32)
+        a = rng.uniform(0.1, 2, (frames, 1)).astype(np.float32)
+        ph = rng.uniform(0, 2 * np.pi, (frames, 1)).astype(np.float32)
+        x += a * np.sin(2 * np.pi * f * t / n + ph)
+    return x
+
+
+def flops_per_step(frames: int) -> float:
+    return sum(2 * frames * 2.5 * n * math.log2(n) for n in SIZES)
+
+
+class ClockSampler:
+    """nvidia-smi samples every 100 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm() -> tuple[float, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_leg(frames: int, threads: int, kind: str = "port", seed: int = 7) -> dict:
+    """Time the reference algorithm on the host cores: forward + inverse of every size over
+    `frames` frames, one plan instance per thread."""
+    import oracle
+    total_t, total_f = 0.0, 0.0
+    for i, n in enumerate(SIZES):
+        x = frames_for(n, frames, seed + i)
+        spec = np.empty((frames, n // 2), dtype=np.complex64)
+        back = np.empty((frames, n), dtype=np.float32)
+        t0 = time.perf_counter()
+        oracle.batch(x, n, real=True, inverse=False, threads=threads, out=spec, kind=kind)
+        oracle.batch(spec, n, real=True, inverse=True, threads=threads, out=back, kind=kind)
+        total_t += time.perf_counter() - t0
+        total_f += 2 * frames * 2.5 * n * math.log2(n)
+    return {"gflops": total_f / total_t / 1e9, "seconds": total_t}
+
+
+def run_reference(args, rank: int, world: int):
+    """The reference arm: the reference's CPU algorithm on all host threads, rank 0 only."""
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    # frames per step so that warmup + steps stay within ~2 minutes of wall time
+    probe = cpu_leg(256, threads)
+    per_frame = probe["seconds"] / 256
+    budget = 120.0 / max(1, args.steps + args.warmup)
+    frames = int(max(16, min(args.frames, budget / max(per_frame, 1e-9))))
+    for _ in range(args.warmup):
+        cpu_leg(frames, threads)
+    t = 0.0
+    for _ in range(args.steps):
+        t += cpu_leg(frames, threads)["seconds"]
+    value = flops_per_step(frames) * args.steps / t / 1e9
+    sample = f"{frames} frames per size per step (of {args.frames}), forward+inverse of N in {list(SIZES)}"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "RealFFT<float> N in {480,960,1920,3840}, 16384 frames each, fwd+inv",
+                   "frames_per_step": frames, "host": os.uname().machine},
+        "cpu_baseline": {"value": value, "unit": "GFLOP/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank: int, world: int):
+    import torch
+
+    from fft_gb300 import build as fb
+    fb.build()
+    import fft_gb300 as F
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    frames = args.frames
+    stream = torch.cuda.current_stream()
+    sh = int(stream.cuda_stream)
+
+    # buffers and plans (outside the timed region)
+    plans, xs, specs, backs = [], [], [], []
+    for i, n in enumerate(SIZES):
+        x = frames_for(n, frames, 1000 * rank + i)
+        xs.append(torch.from_numpy(x).cuda())
+        specs.append(torch.empty((frames, n // 2), dtype=torch.complex64, device="cuda"))
+        backs.append(torch.empty((frames, n), dtype=torch.float32, device="cuda"))
+        plans.append(F.Plan(n, "f32", "real", frames))
+    nl = len(SIZES) * 2
+
+    def step(evs=None):
+        k = 0
+        for p, x, s, b in zip(plans, xs, specs, backs):
+            if evs is not None:
+                evs[k][0].record(stream)
+            p.exec(False, x.data_ptr(), s.data_ptr(), sh)
+            if evs is not None:
+                evs[k][1].record(stream)
+                evs[k + 1][0].record(stream)
+            p.exec(True, s.data_ptr(), b.data_ptr(), sh)
+            if evs is not None:
+                evs[k + 1][1].record(stream)
+            k += 2
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+
+    # per-launch CUDA events on the launching stream: one set per step, summed afterwards
+    evsets = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nl)]
+              for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.25)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for k in range(args.steps):
+        step(evsets[k])
+    t1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    elapsed = t0.elapsed_time(t1) / 1e3
+    if dist:
+        tt = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        elapsed = float(tt.item())
+    value = flops_per_step(frames) * args.steps * world / elapsed / 1e9
+
+    # per-kernel durations
+    kt = np.zeros(nl)
+    for evs in evsets:
+        for j, (a, b) in enumerate(evs):
+            kt[j] += a.elapsed_time(b) / 1e3
+    kt /= args.steps
+    names, alg = [], []
+    for n in SIZES:
+        for d in ("r2c", "c2r"):
+            names.append(f"realfft_f32_{d}_N{n}")
+            alg.append(frames * 8.0 * n)  # 4N bytes in + 4N bytes out (N/2 complex) per frame
+    top = int(np.argmax(kt))
+    peak, peak_kind = measured_peak_hbm()
+    achieved = alg[top] / kt[top] / 1e9
+    kernels = {names[j]: {"ms": round(kt[j] * 1e3, 4), "GB_s": round(alg[j] / kt[j] / 1e9, 1),
+                          "frac": round(alg[j] / kt[j] / 1e9 / peak, 3)} for j in range(nl)}
+    agg_bytes = sum(alg)
+    agg_gbs = agg_bytes / kt.sum() / 1e9
+
+    # numerics spot check of what was timed
+    import oracle
+    sref = np.stack([oracle.rfft(r.astype(np.float64)) for r in xs[-1][:64].cpu().numpy()])
+    rel = float(np.linalg.norm(specs[-1][:64].cpu().numpy() - sref) / np.linalg.norm(sref))
+
+    # end to end through the C ABI with pinned host buffers
+    e2e_steps = args.e2e_steps or max(3, args.steps // 10)
+    hin = [torch.from_numpy(x.cpu().numpy()).pin_memory() for x in xs]
+    hspec = [torch.empty(s.shape, dtype=s.dtype).pin_memory() for s in specs]
+    hback = [torch.empty(b.shape, dtype=b.dtype).pin_memory() for b in backs]
+    lib = F.lib()
+
+    def e2e_step():
+        for p, a, s, b in zip(plans, hin, hspec, hback):
+            F.check(lib.ssfft_exec_host(p.handle, 0, a.data_ptr(), s.data_ptr()), "exec_host")
+            F.check(lib.ssfft_exec_host(p.handle, 1, s.data_ptr(), b.data_ptr()), "exec_host")
+
+    for _ in range(2):
+        e2e_step()
+    if dist:
+        dist.barrier()
+    te = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    te = time.perf_counter() - te
+    if dist:
+        tt = torch.tensor([te], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        te = float(tt.item())
+    h2d = sum(a.numel() * 4 for a in hin) + sum(s.numel() * 8 for s in hspec)
+    d2h = sum(s.numel() * 8 for s in hspec) + sum(b.numel() * 4 for b in hback)
+    e2e = {"value": flops_per_step(frames) * e2e_steps * world / te / 1e9, "unit": "GFLOP/s",
+           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
+           "path": "ssfft_exec_host (pinned host buffers, 3-stream copy/compute pipeline)"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        sample = min(frames, 4096)
+        c = cpu_leg(sample, threads)
+        cpu = {"value": c["gflops"], "unit": "GFLOP/s", "cores": threads, "kind": "port",
+               "sample": f"{sample} frames per size, forward+inverse of N in {list(SIZES)} "
+                         f"({c['seconds']:.1f} s wall), oracle/ssfft_oracle.c built -O3"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "RealFFT<float> N in {480,960,1920,3840}, 16384 frames each, fwd+inv",
+                       "frames": frames, "parallelism": f"replicas x{world}",
+                       "l2": "each step streams ~1.9 GB (> 129 MB L2), no flush"},
+            "gpu_launches": nl * args.steps,
+            "relL2_vs_fp64_oracle": rel,
+            "roofline": {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": peak,
+                         "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "alg_bytes_per_launch": alg[top], "aggregate_GB_s": agg_gbs},
+            "kernels": kernels,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world if "WORLD_SIZE" in os.environ else 1)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,107 @@
+// ssfft_host.h -- host-side plan objects shared by the translation units of libssfft.so.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/ssfft.h"
+#include "ssfft_codelets.cuh"
+
+namespace ssfft {
+
+constexpr int kElemsPerThread = 16;     // complex values a thread holds in one pass
+constexpr int kMaxCtaThreads = 1024;
+constexpr int kMaxSubTransform = 16384; // longest transform one CTA runs (FP32)
+
+// A size-specialised kernel schedule: the compile-time parameters of one ssfft_cl::batch (or
+// ssfft_cl::strided) instantiation.
+struct Schedule {
+	ssfft_dtype dtype = SSFFT_F32;
+	int n = 0;                // complex points per transform
+	std::vector<int> radices; // pass order
+	int threads = 0;          // threads per transform
+	int per_cta = 0;          // transforms per CTA
+	int smem_stride = 0;      // padded complex slots per transform
+	int kind = 0;             // ssfft_cl::kComplex / kReal / kRealHalfShift
+	bool odd = false;         // real length is odd (scalar loads/stores)
+	size_t smem_bytes = 0;
+	int cta_threads() const { return threads * per_cta; }
+	std::string name(bool inverse) const;
+};
+
+// Device tables of one schedule (all inside the plan's single table allocation).
+struct Tables {
+	const void *tw = nullptr, *roots = nullptr, *rtw = nullptr, *rot = nullptr;
+};
+
+struct SubPlan {
+	Schedule sch;
+	Tables tab;
+	CUfunction fwd = nullptr, inv = nullptr;
+};
+
+// Multi-pass (four-step) schedule for transforms longer than one CTA holds; see ssfft_large.cu.
+struct LargePlan;
+
+// Buffers and streams for ssfft_exec_host's copy/compute pipeline.
+struct HostStage {
+	static constexpr int kStreams = 3;
+	cudaStream_t stream[kStreams] = {};
+	void *d_in[kStreams] = {};
+	void *d_out[kStreams] = {};
+	size_t chunk = 0;   // transforms per chunk
+	int streams = kStreams;
+};
+
+struct Plan {
+	size_t n = 0;
+	ssfft_dtype dtype = SSFFT_F32;
+	ssfft_kind kind = SSFFT_COMPLEX;
+	size_t batch = 1;
+	int device = 0;
+	SubPlan main;
+	void *d_tables = nullptr;
+	size_t table_bytes = 0;
+	size_t scratch_bytes = 0;
+	size_t stage_bytes = 0;
+	int launches_per_exec = 1;
+	LargePlan *large = nullptr;
+	HostStage *stage = nullptr;
+	std::mutex stage_mutex;
+};
+
+// errors
+ssfft_status cuda_fail(cudaError_t e, const char *what);
+
+// roots of unity, schedules and tables
+void unit_root(unsigned long long k, unsigned long long L, double *re, double *im);
+bool choose_radices(int n, std::vector<int> &radices);
+bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, Schedule &s);
+void schedule_twiddles(const Schedule &s, std::vector<double> &tw, std::vector<double> &roots);
+size_t device_smem_limit(int dev);
+
+// JIT (ssfft_jit.cu)
+std::string device_arch(int device);
+ssfft_status jit_kernels(const std::vector<std::string> &names, size_t smem_bytes, std::vector<CUfunction> &fns);
+ssfft_status jit_compile_only(const std::vector<std::string> &names, const std::string &arch, size_t *image_bytes);
+ssfft_status jit_launch(CUfunction f, unsigned grid, unsigned block, size_t smem, cudaStream_t stream, void *args);
+const char *jit_last_log();
+
+// plans
+void plan_dists(const Plan *p, int inverse, long long &in_dist, long long &out_dist);
+size_t plan_in_bytes(const Plan *p, int inverse, size_t batch);
+size_t plan_out_bytes(const Plan *p, int inverse, size_t batch);
+size_t size_minimum(size_t n);
+size_t size_maximum(size_t n);
+ssfft_status plan_build_large(Plan *p);
+void plan_release(Plan *p);
+ssfft_status launch_batch(const Plan *p, int inverse, const void *in, void *out, size_t batch, cudaStream_t s);
+ssfft_status launch_large(Plan *p, int inverse, const void *in, void *out, size_t batch, cudaStream_t s);
+void large_release(LargePlan *lp);
+
+}  // namespace ssfft

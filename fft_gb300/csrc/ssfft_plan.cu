@@ -1,0 +1,535 @@
+// ssfft_plan.cu -- host planner, FP64 twiddle tables, kernel launches and the C ABI of
+// libssfft.so (include/ssfft.h).
+//
+// Replaces the reference's FFT<V>::setPlan / addPlanSteps (signalsmith-fft.h:93-185) and
+// RealFFT<V>::setSize (:416-435) with a GB300 schedule: n is split into Stockham passes of
+// radix 16/8/4/2/3/5 (other primes run a direct O(p^2) pass, as the reference's generic step
+// does), every pass of one transform runs inside one CTA, and every twiddle is computed in FP64
+// on the host and rounded once to the plan's dtype.  The kernel for the schedule is compiled
+// for the device at plan time (ssfft_jit.cu) with all of its sizes as constants.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "ssfft_host.h"
+
+namespace ssfft {
+
+// ------------------------------------------------------------------ error plumbing
+
+static thread_local std::string g_last_error;
+
+ssfft_status cuda_fail(cudaError_t e, const char *what) {
+	char buf[256];
+	std::snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+	g_last_error = buf;
+	return e == cudaErrorMemoryAllocation ? SSFFT_ERR_ALLOC : SSFFT_ERR_CUDA;
+}
+
+// ------------------------------------------------------------------ fast sizes
+
+// FFT::validSize (signalsmith-fft.h:317-325): remainders below 32 that are 0 or 2^a 3^b, b <= 2.
+static bool small_fast(size_t s) {
+	if (s == 0) return true;
+	if (s >= 32) return false;
+	int threes = 0;
+	while (s % 3 == 0) {
+		s /= 3;
+		++threes;
+	}
+	while (s % 2 == 0) s /= 2;
+	return s == 1 && threes <= 2;
+}
+
+// FFT::sizeMinimum (signalsmith-fft.h:327-337)
+size_t size_minimum(size_t size) {
+	size_t p2 = 1;
+	while (size >= 32) {
+		size = (size - 1) / 2 + 1;
+		p2 *= 2;
+	}
+	while (size < 32 && !small_fast(size)) ++size;
+	return p2 * size;
+}
+
+// FFT::sizeMaximum (signalsmith-fft.h:338-348)
+size_t size_maximum(size_t size) {
+	size_t p2 = 1;
+	while (size >= 32) {
+		size /= 2;
+		p2 *= 2;
+	}
+	while (size > 1 && !small_fast(size)) --size;
+	return p2 * size;
+}
+
+// ------------------------------------------------------------------ FP64 roots of unity
+
+// e^{-2 pi i k / L} in double.  The angle is reduced to the first octant by exact integer
+// arithmetic before cos/sin are evaluated, so the error stays near 1 ulp for every k and L.
+void unit_root(unsigned long long k, unsigned long long L, double *re, double *im) {
+	k %= L;
+	// theta = 2 pi k / L = q pi/2 + phi, phi = (pi/2) r / L, 0 <= r < L (exact: 4k < 2^64)
+	const unsigned long long k4 = 4ull * k;
+	const unsigned long long q = k4 / L;
+	const unsigned long long r = k4 - q * L;
+	double c, s;
+	if (2 * r <= L) {
+		const double phi = (M_PI / 2) * (double)r / (double)L;
+		c = std::cos(phi);
+		s = std::sin(phi);
+	} else {
+		const double phi = (M_PI / 2) * (double)(L - r) / (double)L;
+		c = std::sin(phi);
+		s = std::cos(phi);
+	}
+	double x, y;  // e^{i theta} = i^q e^{i phi}
+	switch (q & 3) {
+	case 0: x = c; y = s; break;
+	case 1: x = -s; y = c; break;
+	case 2: x = -c; y = -s; break;
+	default: x = s; y = -c; break;
+	}
+	*re = x;
+	*im = -y;
+}
+
+// ------------------------------------------------------------------ schedules
+
+static bool specialised(int r) { return r == 1 || r == 2 || r == 3 || r == 4 || r == 5 || r == 8 || r == 16; }
+
+// Radix list for an in-CTA transform of n points: powers of two in ceil(a/4) balanced passes of
+// 16/8/4/2, then 3s, then 5s, then the remaining primes (direct passes).
+bool choose_radices(int n, std::vector<int> &radices) {
+	radices.clear();
+	if (n < 1) return false;
+	if (n == 1) {
+		radices.push_back(1);
+		return true;
+	}
+	int m = n, a = 0;
+	while (m % 2 == 0) {
+		m /= 2;
+		++a;
+	}
+	if (a > 0) {
+		const int passes = (a + 3) / 4;
+		for (int p = 0; p < passes; ++p) radices.push_back(1 << (a / passes + (p < a % passes ? 1 : 0)));
+		std::sort(radices.begin(), radices.end(), [](int x, int y) { return x > y; });
+	}
+	while (m % 3 == 0) {
+		m /= 3;
+		radices.push_back(3);
+	}
+	while (m % 5 == 0) {
+		m /= 5;
+		radices.push_back(5);
+	}
+	for (int p = 7; m > 1;) {
+		if ((long long)p * p > m) {
+			radices.push_back(m);
+			break;
+		}
+		if (m % p == 0) {
+			radices.push_back(p);
+			m /= p;
+		} else {
+			p += 2;
+		}
+	}
+	return radices.size() <= 24;
+}
+
+size_t device_smem_limit(int dev) {
+	int v = 0;
+	if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || v <= 0)
+		v = 227 * 1024;
+	return (size_t)v;
+}
+
+// Threads per transform, transforms per CTA and shared memory for n points.
+bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, Schedule &s) {
+	s = Schedule();
+	s.dtype = dtype;
+	s.n = n;
+	s.kind = kind;
+	s.odd = odd;
+	if (!choose_radices(n, s.radices)) return false;
+	int t = 1;
+	for (int r : s.radices) {
+		const int per = r == 1 ? 1 : kElemsPerThread / r;  // butterflies a thread holds
+		const int need = specialised(r) ? (n / r + per - 1) / per : (n + kElemsPerThread - 1) / kElemsPerThread;
+		t = std::max(t, need);
+	}
+	// real transforms also split/merge h/2 pairs; keep at least a warp's worth of threads busy
+	if (t > kMaxCtaThreads) return false;
+	s.threads = t;
+	const size_t eb = dtype == SSFFT_F32 ? 8 : 16;
+	const int shift = dtype == SSFFT_F32 ? 4 : 3;
+	s.smem_stride = (n - 1) + ((n - 1) >> shift) + 1;
+	if (s.smem_stride % 2 == 0) s.smem_stride += 1;  // neighbouring transforms start on other banks
+	const size_t per = (size_t)s.smem_stride * eb;
+	if (per > 227 * 1024) return false;
+	// about 256 threads per CTA, at most 48 KiB of shared memory unless one transform needs more
+	int g = std::max(1, 256 / t);
+	const size_t soft = std::max<size_t>(per, 48 * 1024);
+	while (g > 1 && (size_t)g * per > soft) --g;
+	if (batch > 0 && (size_t)g > batch) g = (int)batch;
+	s.per_cta = std::max(1, g);
+	s.smem_bytes = (size_t)s.per_cta * per;
+	// a single-pass complex transform never touches shared memory
+	if (kind == 0 && s.radices.size() == 1) s.smem_bytes = 0;
+	return true;
+}
+
+std::string Schedule::name(bool inverse) const {
+	std::string r = "ssfft_cl::batch<";
+	r += dtype == SSFFT_F32 ? "float" : "double";
+	r += ", " + std::to_string(n) + ", " + std::to_string(threads) + ", " + std::to_string(per_cta) + ", " +
+	     std::to_string(smem_stride) + ", " + std::to_string(kind) + ", " + (inverse ? "true" : "false") + ", " +
+	     (odd ? "true" : "false") + ", " + std::to_string(kElemsPerThread);
+	for (int x : radices) r += ", " + std::to_string(x);
+	r += ">";
+	return r;
+}
+
+// Per-pass twiddles [pass][r-1][m] = W_{ns R}^{m r} (passes after the first) and the roots
+// W_R^k of direct passes, in the order the kernel's compile-time offsets expect.
+void schedule_twiddles(const Schedule &s, std::vector<double> &tw, std::vector<double> &roots) {
+	long long ns = 1;
+	for (int R : s.radices) {
+		if (ns > 1)
+			for (int r = 1; r < R; ++r)
+				for (long long m = 0; m < ns; ++m) {
+					double re, im;
+					unit_root((unsigned long long)(m * r), (unsigned long long)(ns * R), &re, &im);
+					tw.push_back(re);
+					tw.push_back(im);
+				}
+		if (!specialised(R))
+			for (int k = 0; k < R; ++k) {
+				double re, im;
+				unit_root((unsigned long long)k, (unsigned long long)R, &re, &im);
+				roots.push_back(re);
+				roots.push_back(im);
+			}
+		ns *= R;
+	}
+}
+
+// ------------------------------------------------------------------ plan object
+
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+template <typename T>
+static void put_table(std::vector<unsigned char> &blob, size_t off, const std::vector<double> &src) {
+	T *dst = reinterpret_cast<T *>(blob.data() + off);
+	for (size_t i = 0; i < src.size(); ++i) dst[i] = (T)src[i];
+}
+
+static int kind_code(ssfft_kind kind) {
+	return kind == SSFFT_COMPLEX ? ssfft_cl::kComplex : kind == SSFFT_REAL ? ssfft_cl::kReal : ssfft_cl::kRealHalfShift;
+}
+
+// The single-CTA schedule of (n, dtype, kind, batch), or false if n needs the multi-pass path.
+static bool single_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, Schedule &s) {
+	const bool real = kind != SSFFT_COMPLEX;
+	const size_t cn = real ? n / 2 : n;
+	const int max_n = dtype == SSFFT_F32 ? kMaxSubTransform : kMaxSubTransform / 2;
+	if (cn == 0 || cn > (size_t)max_n) return false;
+	return make_schedule(dtype, (int)cn, kind_code(kind), real && (n & 1), batch, s);
+}
+
+// FP64 tables of a single-CTA schedule: pass twiddles, direct-pass roots, and for real kinds
+// the split twiddles and half-shift rotations.
+static void single_tables(const Schedule &s, size_t n_real, std::vector<double> &tw, std::vector<double> &roots,
+                          std::vector<double> &rtw, std::vector<double> &rot) {
+	schedule_twiddles(s, tw, roots);
+	if (s.kind == ssfft_cl::kComplex) return;
+	const size_t h = (size_t)s.n;
+	// twiddlesMinusI (signalsmith-fft.h:420-425) = -i e^{-2 pi i (k + d)/n}, d = 0 or 1/2
+	for (size_t i = 0; i <= h / 2; ++i) {
+		double re, im;
+		if (s.kind == ssfft_cl::kRealHalfShift) unit_root(2 * i + 1, 2 * (unsigned long long)n_real, &re, &im);
+		else unit_root(i, n_real, &re, &im);
+		rtw.push_back(im);  // -i (re + i im) = im - i re
+		rtw.push_back(-re);
+	}
+	if (s.kind == ssfft_cl::kRealHalfShift)
+		// modifiedRotations (signalsmith-fft.h:426-432) = e^{-2 pi i k / n}
+		for (size_t i = 0; i < h; ++i) {
+			double re, im;
+			unit_root(i, n_real, &re, &im);
+			rot.push_back(re);
+			rot.push_back(im);
+		}
+}
+
+static ssfft_status plan_build_single(Plan *p) {
+	Schedule &s = p->main.sch;
+	if (!single_schedule(p->n, p->dtype, p->kind, p->batch, s)) return SSFFT_ERR_UNSUPPORTED;
+	if (s.smem_bytes > device_smem_limit(p->device)) return SSFFT_ERR_UNSUPPORTED;
+	std::vector<double> tw, roots, rtw, rot;
+	single_tables(s, p->n, tw, roots, rtw, rot);
+	const size_t sb = p->dtype == SSFFT_F32 ? 4 : 8;
+	const size_t off_tw = 0;
+	const size_t off_roots = align_up(off_tw + tw.size() * sb, 256);
+	const size_t off_rtw = align_up(off_roots + roots.size() * sb, 256);
+	const size_t off_rot = align_up(off_rtw + rtw.size() * sb, 256);
+	const size_t total = std::max<size_t>(256, align_up(off_rot + rot.size() * sb, 256));
+	std::vector<unsigned char> blob(total, 0);
+	if (sb == 4) {
+		put_table<float>(blob, off_tw, tw);
+		put_table<float>(blob, off_roots, roots);
+		put_table<float>(blob, off_rtw, rtw);
+		put_table<float>(blob, off_rot, rot);
+	} else {
+		put_table<double>(blob, off_tw, tw);
+		put_table<double>(blob, off_roots, roots);
+		put_table<double>(blob, off_rtw, rtw);
+		put_table<double>(blob, off_rot, rot);
+	}
+	cudaError_t e = cudaMalloc(&p->d_tables, total);
+	if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(tables)");
+	p->table_bytes = total;
+	e = cudaMemcpy(p->d_tables, blob.data(), total, cudaMemcpyHostToDevice);
+	if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(tables)");
+	const unsigned char *base = static_cast<const unsigned char *>(p->d_tables);
+	p->main.tab.tw = base + off_tw;
+	p->main.tab.roots = base + off_roots;
+	p->main.tab.rtw = base + off_rtw;
+	p->main.tab.rot = base + off_rot;
+
+	std::vector<CUfunction> fns;
+	ssfft_status st = jit_kernels({s.name(false), s.name(true)}, s.smem_bytes, fns);
+	if (st != SSFFT_SUCCESS) return st;
+	p->main.fwd = fns[0];
+	p->main.inv = fns[1];
+	p->launches_per_exec = 1;
+	return SSFFT_SUCCESS;
+}
+
+// scalar distances between consecutive transforms
+void plan_dists(const Plan *p, int inverse, long long &in_dist, long long &out_dist) {
+	const long long n = (long long)p->n, h2 = 2 * (long long)(p->n / 2);
+	if (p->kind == SSFFT_COMPLEX) {
+		in_dist = out_dist = 2 * n;
+	} else if (!inverse) {
+		in_dist = n;
+		out_dist = h2;
+	} else {
+		in_dist = h2;
+		out_dist = n;
+	}
+}
+
+size_t plan_in_bytes(const Plan *p, int inverse, size_t batch) {
+	long long di, dout;
+	plan_dists(p, inverse, di, dout);
+	return (size_t)di * batch * (p->dtype == SSFFT_F32 ? 4 : 8);
+}
+
+size_t plan_out_bytes(const Plan *p, int inverse, size_t batch) {
+	long long di, dout;
+	plan_dists(p, inverse, di, dout);
+	return (size_t)dout * batch * (p->dtype == SSFFT_F32 ? 4 : 8);
+}
+
+ssfft_status launch_batch(const Plan *p, int inverse, const void *in, void *out, size_t batch, cudaStream_t s) {
+	if (batch == 0) return SSFFT_SUCCESS;
+	const Schedule &sch = p->main.sch;
+	ssfft_cl::Args a;
+	a.in = in;
+	a.out = out;
+	a.batch = (long long)batch;
+	plan_dists(p, inverse, a.in_dist, a.out_dist);
+	a.tw = p->main.tab.tw;
+	a.rtw = p->main.tab.rtw;
+	a.rot = p->main.tab.rot;
+	a.roots = p->main.tab.roots;
+	const long long grid = ((long long)batch + sch.per_cta - 1) / sch.per_cta;
+	if (grid > 0x7fffffffLL) return SSFFT_ERR_INVALID_SIZE;
+	return jit_launch(inverse ? p->main.inv : p->main.fwd, (unsigned)grid, (unsigned)sch.cta_threads(),
+	                  sch.smem_bytes, s, &a);
+}
+
+}  // namespace ssfft
+
+// ====================================================================== C ABI
+
+using namespace ssfft;
+
+extern "C" {
+
+const char *ssfft_status_string(ssfft_status s) {
+	switch (s) {
+	case SSFFT_SUCCESS: return "success";
+	case SSFFT_ERR_INVALID_SIZE: return "invalid size";
+	case SSFFT_ERR_INVALID_VALUE: return "invalid value";
+	case SSFFT_ERR_CUDA: return "CUDA error";
+	case SSFFT_ERR_ALLOC: return "allocation failed";
+	case SSFFT_ERR_UNSUPPORTED: return "unsupported";
+	case SSFFT_ERR_BUDGET: return "exceeds HBM budget";
+	case SSFFT_ERR_TIMEOUT: return "timed out";
+	case SSFFT_ERR_NOT_READY: return "not ready";
+	case SSFFT_ERR_SHUTDOWN: return "shut down";
+	}
+	return "unknown status";
+}
+
+const char *ssfft_last_cuda_error(void) {
+	const char *j = jit_last_log();
+	return (j && *j) ? j : g_last_error.c_str();
+}
+
+size_t ssfft_size_minimum(size_t n) { return size_minimum(n); }
+size_t ssfft_size_maximum(size_t n) { return size_maximum(n); }
+size_t ssfft_real_size_minimum(size_t n) { return (size_minimum((n - 1) / 2) + 1) * 2; }
+size_t ssfft_real_size_maximum(size_t n) { return size_minimum(n / 2) * 2; }
+
+ssfft_status ssfft_plan_create(ssfft_plan_t *out, size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch) {
+	if (!out) return SSFFT_ERR_INVALID_VALUE;
+	*out = nullptr;
+	if (dtype != SSFFT_F32 && dtype != SSFFT_F64) return SSFFT_ERR_INVALID_VALUE;
+	if (kind != SSFFT_COMPLEX && kind != SSFFT_REAL && kind != SSFFT_REAL_HALFSHIFT) return SSFFT_ERR_INVALID_VALUE;
+	if (n == 0 || (kind != SSFFT_COMPLEX && n < 2)) return SSFFT_ERR_INVALID_SIZE;
+	if (n > (size_t)1 << 31) return SSFFT_ERR_INVALID_SIZE;
+	if (batch == 0) batch = 1;
+	Plan *p = new (std::nothrow) Plan();
+	if (!p) return SSFFT_ERR_ALLOC;
+	p->n = n;
+	p->dtype = dtype;
+	p->kind = kind;
+	p->batch = batch;
+	cudaError_t e = cudaGetDevice(&p->device);
+	ssfft_status st = e == cudaSuccess ? SSFFT_SUCCESS : cuda_fail(e, "cudaGetDevice");
+	if (st == SSFFT_SUCCESS) {
+		st = plan_build_single(p);
+		if (st == SSFFT_ERR_UNSUPPORTED) st = plan_build_large(p);
+	}
+	if (st != SSFFT_SUCCESS) {
+		plan_release(p);
+		delete p;
+		return st;
+	}
+	*out = reinterpret_cast<ssfft_plan_t>(p);
+	return SSFFT_SUCCESS;
+}
+
+ssfft_status ssfft_plan_destroy(ssfft_plan_t plan) {
+	if (!plan) return SSFFT_ERR_INVALID_VALUE;
+	Plan *p = reinterpret_cast<Plan *>(plan);
+	plan_release(p);
+	delete p;
+	return SSFFT_SUCCESS;
+}
+
+size_t ssfft_plan_size(ssfft_plan_t plan) { return plan ? reinterpret_cast<Plan *>(plan)->n : 0; }
+size_t ssfft_plan_batch(ssfft_plan_t plan) { return plan ? reinterpret_cast<Plan *>(plan)->batch : 0; }
+size_t ssfft_plan_device_bytes(ssfft_plan_t plan) {
+	if (!plan) return 0;
+	const Plan *p = reinterpret_cast<Plan *>(plan);
+	return p->table_bytes + p->scratch_bytes + p->stage_bytes;
+}
+
+ssfft_status ssfft_plan_describe(ssfft_plan_t plan, int *npasses, int *radices, int cap, int *threads_per_transform,
+                                 int *transforms_per_cta, int *kernel_launches) {
+	if (!plan) return SSFFT_ERR_INVALID_VALUE;
+	const Plan *p = reinterpret_cast<Plan *>(plan);
+	const Schedule &s = p->main.sch;
+	if (npasses) *npasses = (int)s.radices.size();
+	if (radices)
+		for (int i = 0; i < (int)s.radices.size() && i < cap; ++i) radices[i] = s.radices[i];
+	if (threads_per_transform) *threads_per_transform = s.threads;
+	if (transforms_per_cta) *transforms_per_cta = s.per_cta;
+	if (kernel_launches) *kernel_launches = p->launches_per_exec;
+	return SSFFT_SUCCESS;
+}
+
+static ssfft_status check_exec(const Plan *p, const void *in, void *out) {
+	if (!p || !in || !out) return SSFFT_ERR_INVALID_VALUE;
+	const size_t align = p->dtype == SSFFT_F32 ? 8 : 16;
+	// real data are read/written as {x[2k], x[2k+1]} pairs unless the real length is odd
+	const size_t need = p->kind != SSFFT_COMPLEX && (p->n & 1) ? align / 2 : align;
+	if ((uintptr_t)in % need || (uintptr_t)out % need) return SSFFT_ERR_INVALID_VALUE;
+	return SSFFT_SUCCESS;
+}
+
+ssfft_status ssfft_exec_batch(ssfft_plan_t plan, int inverse, const void *d_in, void *d_out, size_t batch,
+                              void *stream) {
+	Plan *p = reinterpret_cast<Plan *>(plan);
+	ssfft_status st = check_exec(p, d_in, d_out);
+	if (st != SSFFT_SUCCESS) return st;
+	if (batch > p->batch) return SSFFT_ERR_INVALID_SIZE;
+	cudaStream_t s = static_cast<cudaStream_t>(stream);
+	if (p->large) return launch_large(p, inverse, d_in, d_out, batch, s);
+	return launch_batch(p, inverse, d_in, d_out, batch, s);
+}
+
+ssfft_status ssfft_exec(ssfft_plan_t plan, int inverse, const void *d_in, void *d_out, void *stream) {
+	if (!plan) return SSFFT_ERR_INVALID_VALUE;
+	return ssfft_exec_batch(plan, inverse, d_in, d_out, reinterpret_cast<Plan *>(plan)->batch, stream);
+}
+
+// ---------------------------------------------------------------- diagnostics (no GPU needed)
+
+// Compile the kernels a plan of this shape would use (build-time check).
+ssfft_status ssfft_jit_check(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, const char *arch,
+                             size_t *image_bytes) {
+	Schedule s;
+	if (!single_schedule(n, dtype, kind, batch, s)) return SSFFT_ERR_UNSUPPORTED;
+	return jit_compile_only({s.name(false), s.name(true)}, arch ? arch : "sm_103a", image_bytes);
+}
+
+ssfft_status ssfft_schedule_info(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, int *radices, int cap,
+                                 int *npasses, int *threads, int *per_cta, size_t *smem_bytes) {
+	Schedule s;
+	if (!single_schedule(n, dtype, kind, batch, s)) return SSFFT_ERR_UNSUPPORTED;
+	if (npasses) *npasses = (int)s.radices.size();
+	if (radices)
+		for (int i = 0; i < (int)s.radices.size() && i < cap; ++i) radices[i] = s.radices[i];
+	if (threads) *threads = s.threads;
+	if (per_cta) *per_cta = s.per_cta;
+	if (smem_bytes) *smem_bytes = s.smem_bytes;
+	return SSFFT_SUCCESS;
+}
+
+ssfft_status ssfft_schedule_name(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, int inverse, char *buf,
+                                 size_t cap) {
+	Schedule s;
+	if (!single_schedule(n, dtype, kind, batch, s)) return SSFFT_ERR_UNSUPPORTED;
+	const std::string name = s.name(inverse != 0);
+	if (!buf || cap < name.size() + 1) return SSFFT_ERR_INVALID_VALUE;
+	std::memcpy(buf, name.c_str(), name.size() + 1);
+	return SSFFT_SUCCESS;
+}
+
+ssfft_status ssfft_schedule_tables(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, double *tw,
+                                   size_t *ntw, double *roots, size_t *nroots, double *rtw, size_t *nrtw, double *rot,
+                                   size_t *nrot) {
+	Schedule s;
+	if (!single_schedule(n, dtype, kind, batch, s)) return SSFFT_ERR_UNSUPPORTED;
+	std::vector<double> vtw, vroots, vrtw, vrot;
+	single_tables(s, n, vtw, vroots, vrtw, vrot);
+	const std::vector<double> *src[4] = {&vtw, &vroots, &vrtw, &vrot};
+	double *dst[4] = {tw, roots, rtw, rot};
+	size_t *cnt[4] = {ntw, nroots, nrtw, nrot};
+	for (int i = 0; i < 4; ++i) {
+		if (!cnt[i]) return SSFFT_ERR_INVALID_VALUE;
+		if (dst[i]) {
+			if (*cnt[i] < src[i]->size()) return SSFFT_ERR_INVALID_VALUE;
+			std::memcpy(dst[i], src[i]->data(), src[i]->size() * sizeof(double));
+		}
+		*cnt[i] = src[i]->size();
+	}
+	return SSFFT_SUCCESS;
+}
+
+}  // extern "C"

@@ -1,0 +1,111 @@
+// ssfft_stage.cu -- host-memory execution (ssfft_exec_host) and plan teardown.
+//
+// ssfft_exec_host is the GB300 form of the reference's host-iterator fft/ifft
+// (signalsmith-fft.h:374-386): the caller's host buffers stream through the device in chunks,
+// each chunk's host->device copy, transform and device->host copy issued on one of three
+// streams so that the two copy directions and the kernels of neighbouring chunks overlap.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "ssfft_host.h"
+
+namespace ssfft {
+
+void plan_release(Plan *p) {
+	if (!p) return;
+	int prev = -1;
+	cudaGetDevice(&prev);
+	cudaSetDevice(p->device);
+	if (p->stage) {
+		HostStage *st = p->stage;
+		for (int i = 0; i < HostStage::kStreams; ++i) {
+			if (st->stream[i]) cudaStreamSynchronize(st->stream[i]);
+			if (st->d_in[i]) cudaFree(st->d_in[i]);
+			if (st->d_out[i]) cudaFree(st->d_out[i]);
+			if (st->stream[i]) cudaStreamDestroy(st->stream[i]);
+		}
+		delete st;
+		p->stage = nullptr;
+	}
+	if (p->large) {
+		large_release(p->large);
+		p->large = nullptr;
+	}
+	if (p->d_tables) cudaFree(p->d_tables);
+	p->d_tables = nullptr;
+	if (prev >= 0) cudaSetDevice(prev);
+}
+
+// Chunk of ~16 MiB of input per stream (at least one transform).
+static ssfft_status stage_init(Plan *p) {
+	if (p->stage) return SSFFT_SUCCESS;
+	HostStage *st = new HostStage();
+	const size_t per_in = std::max(plan_in_bytes(p, 0, 1), plan_in_bytes(p, 1, 1));
+	const size_t per_out = std::max(plan_out_bytes(p, 0, 1), plan_out_bytes(p, 1, 1));
+	size_t chunk = std::max<size_t>(1, (16u << 20) / std::max<size_t>(per_in, 1));
+	chunk = std::min(chunk, p->batch);
+	st->chunk = chunk;
+	// multi-pass plans share one scratch buffer, so their chunks run on a single stream
+	st->streams = p->large ? 1 : HostStage::kStreams;
+	for (int i = 0; i < st->streams; ++i) {
+		cudaError_t e = cudaStreamCreateWithFlags(&st->stream[i], cudaStreamNonBlocking);
+		if (e == cudaSuccess) e = cudaMalloc(&st->d_in[i], per_in * chunk);
+		if (e == cudaSuccess) e = cudaMalloc(&st->d_out[i], per_out * chunk);
+		if (e != cudaSuccess) {
+			p->stage = st;  // released with the plan
+			return cuda_fail(e, "exec_host staging");
+		}
+	}
+	p->stage_bytes = (size_t)st->streams * (per_in + per_out) * chunk;
+	p->stage = st;
+	return SSFFT_SUCCESS;
+}
+
+}  // namespace ssfft
+
+using namespace ssfft;
+
+extern "C" ssfft_status ssfft_exec_host(ssfft_plan_t plan, int inverse, const void *h_in, void *h_out) {
+	Plan *p = reinterpret_cast<Plan *>(plan);
+	if (!p || !h_in || !h_out) return SSFFT_ERR_INVALID_VALUE;
+	std::lock_guard<std::mutex> lock(p->stage_mutex);
+	int prev = -1;
+	cudaGetDevice(&prev);
+	if (prev != p->device) cudaSetDevice(p->device);
+	ssfft_status st = stage_init(p);
+	if (st != SSFFT_SUCCESS) return st;
+	HostStage *sg = p->stage;
+	const size_t per_in = plan_in_bytes(p, inverse, 1), per_out = plan_out_bytes(p, inverse, 1);
+	const unsigned char *src = static_cast<const unsigned char *>(h_in);
+	unsigned char *dst = static_cast<unsigned char *>(h_out);
+	size_t done = 0;
+	int k = 0;
+	while (done < p->batch && st == SSFFT_SUCCESS) {
+		const size_t b = std::min(sg->chunk, p->batch - done);
+		const int i = k % sg->streams;
+		cudaStream_t s = sg->stream[i];
+		cudaError_t e = cudaMemcpyAsync(sg->d_in[i], src + done * per_in, b * per_in, cudaMemcpyHostToDevice, s);
+		if (e != cudaSuccess) {
+			st = cuda_fail(e, "exec_host H2D");
+			break;
+		}
+		st = p->large ? launch_large(p, inverse, sg->d_in[i], sg->d_out[i], b, s)
+		              : launch_batch(p, inverse, sg->d_in[i], sg->d_out[i], b, s);
+		if (st != SSFFT_SUCCESS) break;
+		e = cudaMemcpyAsync(dst + done * per_out, sg->d_out[i], b * per_out, cudaMemcpyDeviceToHost, s);
+		if (e != cudaSuccess) {
+			st = cuda_fail(e, "exec_host D2H");
+			break;
+		}
+		done += b;
+		++k;
+	}
+	for (int i = 0; i < sg->streams; ++i) {
+		cudaError_t e = cudaStreamSynchronize(sg->stream[i]);
+		if (e != cudaSuccess && st == SSFFT_SUCCESS) st = cuda_fail(e, "exec_host sync");
+	}
+	if (prev >= 0 && prev != p->device) cudaSetDevice(prev);
+	return st;
+}

@@ -1,0 +1,72 @@
+// tests/emu/emu_main.cpp -- runs one emulated kernel launch.  Compiled together with a generated
+// case table (emu_cases.inc: `{name, &ssfft_cl::batch<...>, cta_threads, smem_bytes},` lines).
+// argv: case index, grid, raw input file, raw output file (pre-filled), table file, batch,
+//       in_dist, out_dist (scalars), scalar bytes.
+// The table file holds tw, roots, rtw, rot back to back in the kernel's dtype, preceded by four
+// uint64 element counts (scalars).
+#include "cuda_emu.h"
+#include "ssfft_codelets.cuh"
+
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iterator>
+#include <thread>
+#include <vector>
+
+thread_local EmuIdx threadIdx, blockIdx;
+thread_local std::barrier<> *emu_barrier;
+namespace ssfft_cl {
+alignas(16) unsigned char smem_raw[232 * 1024];
+}
+
+struct Case {
+	const char *name;
+	void (*fn)(const ssfft_cl::Args);
+	int cta_threads;
+	size_t smem;
+};
+static const Case kCases[] = {
+#include "emu_cases.inc"
+};
+
+static std::vector<char> slurp(const char *path) {
+	std::ifstream f(path, std::ios::binary);
+	return std::vector<char>((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+}
+
+int main(int argc, char **argv) {
+	if (argc != 10) return 2;
+	const Case &c = kCases[std::atoi(argv[1])];
+	const int grid = std::atoi(argv[2]);
+	std::vector<char> in = slurp(argv[3]), out = slurp(argv[4]), tab = slurp(argv[5]);
+	const size_t sb = (size_t)std::atoi(argv[9]);
+	const uint64_t *cnt = reinterpret_cast<const uint64_t *>(tab.data());
+	const char *base = tab.data() + 4 * sizeof(uint64_t);
+	ssfft_cl::Args a;
+	a.in = in.data();
+	a.out = out.data();
+	a.batch = std::atoll(argv[6]);
+	a.in_dist = std::atoll(argv[7]);
+	a.out_dist = std::atoll(argv[8]);
+	a.tw = base;
+	a.roots = base + cnt[0] * sb;
+	a.rtw = base + (cnt[0] + cnt[1]) * sb;
+	a.rot = base + (cnt[0] + cnt[1] + cnt[2]) * sb;
+	for (int b = 0; b < grid; ++b) {
+		std::barrier<> bar(c.cta_threads);
+		std::vector<std::thread> th;
+		th.reserve(c.cta_threads);
+		for (int t = 0; t < c.cta_threads; ++t)
+			th.emplace_back([&, t, b] {
+				threadIdx.x = (unsigned)t;
+				blockIdx.x = (unsigned)b;
+				emu_barrier = &bar;
+				c.fn(a);
+			});
+		for (auto &x : th) x.join();
+	}
+	std::ofstream f(argv[4], std::ios::binary);
+	f.write(out.data(), (std::streamsize)out.size());
+	return 0;
+}

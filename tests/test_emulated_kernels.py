@@ -1,0 +1,107 @@
+"""Run the exact kernel source (fft_gb300/csrc/ssfft_codelets.cuh) on the CPU through the CUDA
+emulation shim in tests/emu/, with the schedules and FP64 tables libssfft.so's planner picks, and
+compare with the oracle.  This checks the kernels' index arithmetic, butterflies, twiddle layout,
+real split/merge (including the reference's pair-overwrite order) and partial CTAs without a GPU.
+The GPU parity tests (test_gpu_parity.py) repeat the comparison on the device."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import fft_gb300 as F
+import oracle
+from conftest import ROOT, rel_l2
+
+# (n, dtype, kind, plan batch, exec batch)
+CASES = [
+    (1, "f64", "complex", 1, 1), (2, "f64", "complex", 3, 3), (3, "f32", "complex", 2, 2),
+    (8, "f64", "complex", 1, 1), (16, "f32", "complex", 5, 5), (23, "f64", "complex", 1, 1),
+    (49, "f64", "complex", 2, 2), (60, "f32", "complex", 100, 100), (96, "f64", "complex", 3, 3),
+    (240, "f32", "complex", 2, 2), (1024, "f64", "complex", 2, 2), (1920, "f32", "complex", 1, 1),
+    (4096, "f32", "complex", 1, 1),
+    (2, "f64", "real", 1, 1), (3, "f64", "real", 2, 2), (7, "f32", "real", 1, 1), (10, "f64", "real", 4, 4),
+    (98, "f32", "real", 3, 3), (480, "f32", "real", 5, 5), (3840, "f32", "real", 2, 2),
+    (2, "f64", "real_halfshift", 1, 1), (4, "f64", "real_halfshift", 2, 2), (9, "f64", "real_halfshift", 1, 1),
+    (12, "f32", "real_halfshift", 2, 2), (98, "f64", "real_halfshift", 1, 1), (960, "f32", "real_halfshift", 2, 2),
+]
+
+
+@pytest.fixture(scope="session")
+def emulator(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    d = tmp_path_factory.mktemp("emu")
+    lines = []
+    index = {}
+    for (n, dt, kind, pb, _) in CASES:
+        info = F.schedule_info(n, dt, kind, pb)
+        for inv in (False, True):
+            name = F.schedule_name(n, dt, kind, pb, inv)
+            index[(n, dt, kind, pb, inv)] = (len(lines), info)
+            lines.append(f'{{"{n}-{dt}-{kind}-{int(inv)}", &{name}, {info["threads"] * info["per_cta"]}, '
+                         f'{info["smem_bytes"]}}},')
+    (d / "emu_cases.inc").write_text("\n".join(lines) + "\n")
+    exe = d / "emu"
+    cmd = ["g++", "-std=c++20", "-O1", "-pthread", "-w", "-I", str(d), "-I", os.path.join(ROOT, "tests", "emu"),
+           "-I", os.path.join(ROOT, "fft_gb300", "csrc"), os.path.join(ROOT, "tests", "emu", "emu_main.cpp"),
+           "-o", str(exe)]
+    subprocess.run(cmd, check=True)
+    return exe, index, d
+
+
+def _run(emulator, n, dt, kind, pb, eb, inv, x):
+    exe, index, d = emulator
+    ci, info = index[(n, dt, kind, pb, inv)]
+    sdt = np.float32 if dt == "f32" else np.float64
+    real = kind != "complex"
+    h2 = 2 * (n // 2)
+    if not real:
+        in_dist = out_dist = 2 * n
+    elif not inv:
+        in_dist, out_dist = n, h2
+    else:
+        in_dist, out_dist = h2, n
+    xin = np.ascontiguousarray(x).view(sdt).reshape(eb, in_dist)
+    out = np.full((eb, out_dist), np.nan, dtype=sdt)
+    tabs = F.schedule_tables(n, dt, kind, pb)
+    blob = np.array([tabs[k].size for k in ("tw", "roots", "rtw", "rot")], dtype=np.uint64).tobytes()
+    blob += b"".join(tabs[k].astype(sdt).tobytes() for k in ("tw", "roots", "rtw", "rot"))
+    fi, fo, ft = d / f"in{ci}", d / f"out{ci}", d / f"tab{ci}"
+    fi.write_bytes(xin.tobytes())
+    fo.write_bytes(out.tobytes())
+    ft.write_bytes(blob)
+    grid = -(-eb // info["per_cta"])
+    subprocess.run([str(exe), str(ci), str(grid), str(fi), str(fo), str(ft), str(eb), str(in_dist), str(out_dist),
+                    str(np.dtype(sdt).itemsize)], check=True, timeout=300)
+    return np.frombuffer(fo.read_bytes(), dtype=sdt).reshape(eb, out_dist)
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}-{c[1]}-{c[2]}")
+def test_emulated_kernel_matches_oracle(emulator, case):
+    n, dt, kind, pb, eb = case
+    rng = np.random.default_rng(n * 7 + len(kind))
+    tol = 1e-6 if dt == "f32" else 1e-13
+    cdt = np.complex64 if dt == "f32" else np.complex128
+    rdt = np.float32 if dt == "f32" else np.float64
+    if kind == "complex":
+        x = (rng.uniform(-1, 1, (eb, n)) + 1j * rng.uniform(-1, 1, (eb, n))).astype(cdt)
+        for inv in (False, True):
+            got = _run(emulator, n, dt, kind, pb, eb, inv, x).view(cdt)
+            ref = np.stack([oracle.fft(r.astype(np.complex128), inv) for r in x])
+            assert rel_l2(got, ref) <= tol, (inv, rel_l2(got, ref))
+    else:
+        mod = kind == "real_halfshift"
+        h = n // 2
+        x = rng.standard_normal((eb, n)).astype(rdt)
+        got = _run(emulator, n, dt, kind, pb, eb, False, x).view(cdt)
+        ref = np.stack([oracle.rfft(r.astype(np.float64), mod) for r in x])
+        assert got.shape == ref.shape
+        assert rel_l2(got, ref) <= tol, rel_l2(got, ref)
+        s = (rng.standard_normal((eb, h)) + 1j * rng.standard_normal((eb, h))).astype(cdt)
+        got = _run(emulator, n, dt, kind, pb, eb, True, s)
+        ref = np.stack([oracle.irfft(r.astype(np.complex128), n, mod) for r in s])
+        assert rel_l2(got[:, :2 * h], ref) <= tol, rel_l2(got[:, :2 * h], ref)
+        if n % 2:
+            assert np.all(np.isnan(got[:, 2 * h:])), "odd real length: last sample must be left alone"

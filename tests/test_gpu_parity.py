@@ -1,0 +1,248 @@
+"""GPU parity tests: the sm_103a kernels, called through the C ABI (libssfft.so via ctypes, device
+buffers from torch), against the reference's golden vectors and the CPU oracle, plus the
+reference test suite's own checks (tests/00-fft.cpp, tests/01-real.cpp) restated on the device.
+
+Tolerances (relative L2 error against the FP64 oracle): 1e-14 for FP64 (1e-13 for the direct
+O(p^2) prime passes), 1e-6 for FP32."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+F32_TOL = 1e-6
+F64_TOL = 1e-14
+
+
+def f64_tol(n):
+    m = n
+    for p in (2, 3, 5):
+        while m % p == 0:
+            m //= p
+    return F64_TOL if m == 1 else 1e-13
+
+
+@pytest.fixture(scope="module")
+def F():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import fft_gb300
+    fft_gb300.lib()
+    _prewarm(fft_gb300)
+    return fft_gb300
+
+
+def _prewarm(F):
+    """Compile the many single-transform plans of the golden tests concurrently (NVRTC runs
+    outside the library's lock; ctypes releases the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+    keys = [(n, dt, "complex", 1) for n in COMPLEX_SIZES for dt in ("f32", "f64")]
+    keys += [(n, dt, k, 1) for n in range(2, 100) for dt in ("f32", "f64") for k in ("real", "real_halfshift")]
+    torch.cuda.init()
+    dev = torch.cuda.current_device()
+
+    def make(k):
+        torch.cuda.set_device(dev)
+        F.Plan(*k).destroy()
+
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        list(ex.map(make, keys))
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def run_complex(F, x, inverse, batch=None):
+    """x: (b, n) complex numpy -> numpy result through ssfft_exec."""
+    b, n = x.shape
+    dt = "f32" if x.dtype == np.complex64 else "f64"
+    p = F.Plan(n, dt, "complex", b)
+    xi = dev(x)
+    xo = torch.empty_like(xi)
+    p.exec(inverse, xi.data_ptr(), xo.data_ptr(), torch.cuda.current_stream().cuda_stream, batch)
+    torch.cuda.synchronize()
+    return xo.cpu().numpy(), xi.cpu().numpy()
+
+
+COMPLEX_SIZES = [1, 2, 4, 8, 16, 32, 64, 128, 256, 3, 6, 9, 12, 18, 24, 5, 10, 15, 20, 25,
+                 7, 14, 21, 28, 49, 11, 13, 17, 19, 22, 23, 480, 1024]
+
+
+@pytest.mark.parametrize("dt", ["f64", "f32"])
+def test_complex_golden(F, golden, dt):
+    for n in COMPLEX_SIZES:
+        x = golden[f"c2c_{dt}_{n}_in"][None, :]
+        for d, inv in (("fwd", False), ("inv", True)):
+            got, xin = run_complex(F, x, inv)
+            ref = golden[f"c2c_{dt}_{n}_{d}"]
+            tol = f64_tol(n) if dt == "f64" else F32_TOL
+            assert rel_l2(got[0], ref) <= tol, (n, d, rel_l2(got[0], ref))
+            assert np.array_equal(xin, x), "input was changed"
+
+
+@pytest.mark.parametrize("dt", ["f64", "f32"])
+@pytest.mark.parametrize("kind", ["real", "real_halfshift"])
+def test_real_golden(F, golden, dt, kind):
+    mod = kind == "real_halfshift"
+    for n in list(range(2, 100)) + [480, 960, 1920, 3840]:
+        key = f"r_{dt}_m{int(mod)}_{n}"
+        if key + "_in" not in golden:
+            continue
+        tol = f64_tol(n // 2) if dt == "f64" else F32_TOL
+        x = golden[key + "_in"]
+        p = F.Plan(n, dt, kind, 1)
+        h = n // 2
+        cdt = torch.complex64 if dt == "f32" else torch.complex128
+        xi = dev(x)
+        # the output buffer has n complex slots; the second half must stay untouched
+        # (tests/01-real.cpp:49-52, :70-73)
+        out = torch.full((n,), complex(52, 21), dtype=cdt, device="cuda")
+        p.exec(False, xi.data_ptr(), out.data_ptr(), 0)
+        torch.cuda.synchronize()
+        o = out.cpu().numpy()
+        assert rel_l2(o[:h], golden[key + "_fwd"]) <= tol, (n, "fwd", rel_l2(o[:h], golden[key + "_fwd"]))
+        assert np.all(o[h:] == complex(52, 21))
+        s = golden[key + "_spec"]
+        si = dev(s)
+        ro = torch.full((n + 1,), 7.0, dtype=xi.dtype, device="cuda")
+        p.exec(True, si.data_ptr(), ro.data_ptr(), 0)
+        torch.cuda.synchronize()
+        r = ro.cpu().numpy()
+        assert rel_l2(r[:2 * h], golden[key + "_inv"]) <= tol, (n, "inv")
+        assert np.all(r[2 * h:] == 7.0)
+
+
+def test_individual_bins_and_linearity(F):
+    """tests/00-fft.cpp:19-99 on the device, FP64 and FP32, all bins of each size at once."""
+    for dt, cdt in (("f64", np.complex128), ("f32", np.complex64)):
+        for n in COMPLEX_SIZES:
+            i = np.arange(n)
+            x = np.exp(2j * np.pi * np.outer(np.arange(n), i) / n).astype(cdt)  # row b = bin b
+            got, _ = run_complex(F, x, False)
+            exp = n * np.eye(n)
+            for b in range(n):
+                assert oracle.close_enough(got[b], exp[b]), (dt, n, b)
+            rng = np.random.default_rng(n)
+            a = (rng.uniform(-0.5, 0.5, (1, n)) + 1j * rng.uniform(-0.5, 0.5, (1, n))).astype(cdt)
+            c = (rng.uniform(-0.5, 0.5, (1, n)) + 1j * rng.uniform(-0.5, 0.5, (1, n))).astype(cdt)
+            fa, fc, fac = run_complex(F, a, False)[0], run_complex(F, c, False)[0], run_complex(F, a + c, False)[0]
+            assert oracle.close_enough(fac, fa + fc)
+
+
+def test_round_trip_is_n_times_input(F):
+    """ifft(fft(x)) == N x (tests/00-fft.cpp:101-145)."""
+    rng = np.random.default_rng(3)
+    for n in COMPLEX_SIZES + [4096, 8192]:
+        x = (rng.uniform(-0.5, 0.5, (2, n)) + 1j * rng.uniform(-0.5, 0.5, (2, n))).astype(np.complex128)
+        spec, _ = run_complex(F, x, False)
+        back, _ = run_complex(F, spec, True)
+        assert rel_l2(back, n * x) <= 1e-13, n
+
+
+@pytest.mark.parametrize("n", [256, 768, 1000, 1024, 2048, 3072, 4096, 4800, 8192, 9216, 15360, 16384])
+def test_complex_f32_vs_oracle(F, n):
+    rng = np.random.default_rng(n)
+    b = 6
+    x = (rng.uniform(-1, 1, (b, n)) + 1j * rng.uniform(-1, 1, (b, n))).astype(np.complex64)
+    for inv in (False, True):
+        got, _ = run_complex(F, x, inv)
+        ref = np.stack([oracle.fft(r.astype(np.complex128), inv) for r in x])
+        assert rel_l2(got, ref) <= F32_TOL, (n, inv, rel_l2(got, ref))
+
+
+def test_config_fp64_1024_x256(F):
+    """FFT<double> N=1024, 256 transforms, forward then inverse, U[-1,1) (relL2 <= 1e-14)."""
+    rng = np.random.default_rng(1)
+    x = rng.uniform(-1, 1, (256, 1024)) + 1j * rng.uniform(-1, 1, (256, 1024))
+    got, _ = run_complex(F, x, False)
+    ref = np.stack([oracle.fft(r) for r in x])
+    assert rel_l2(got, ref) <= F64_TOL
+    back, _ = run_complex(F, got, True)
+    refb = np.stack([oracle.fft(r, True) for r in ref])
+    assert rel_l2(back, refb) <= F64_TOL
+    assert rel_l2(back, 1024 * x) <= F64_TOL
+
+
+@pytest.mark.parametrize("n", [480, 960, 1920, 3840])
+@pytest.mark.parametrize("kind", ["real", "real_halfshift"])
+def test_config_realfft_f32_frames(F, n, kind):
+    """RealFFT<float> frames: N(0,1) noise + 3 sinusoids, forward and inverse vs the oracle."""
+    rng = np.random.default_rng(n)
+    frames = 512
+    t = np.arange(n)
+    x = rng.standard_normal((frames, n))
+    for _ in range(3):
+        f = rng.uniform(0, n / 2, (frames, 1))
+        a = rng.uniform(0.1, 2, (frames, 1))
+        ph = rng.uniform(0, 2 * np.pi, (frames, 1))
+        x += a * np.sin(2 * np.pi * f * t / n + ph)
+    x32 = x.astype(np.float32)
+    mod = kind == "real_halfshift"
+    p = F.Plan(n, "f32", kind, frames)
+    xi = dev(x32)
+    spec = torch.empty((frames, n // 2), dtype=torch.complex64, device="cuda")
+    p.exec(False, xi.data_ptr(), spec.data_ptr(), 0)
+    back = torch.empty_like(xi)
+    p.exec(True, spec.data_ptr(), back.data_ptr(), 0)
+    torch.cuda.synchronize()
+    ref = np.stack([oracle.rfft(r.astype(np.float64), mod) for r in x32])
+    s = spec.cpu().numpy()
+    assert rel_l2(s, ref) <= F32_TOL, rel_l2(s, ref)
+    refb = np.stack([oracle.irfft(r.astype(np.complex128), n, mod) for r in s])
+    assert rel_l2(back.cpu().numpy(), refb) <= F32_TOL
+    assert rel_l2(back.cpu().numpy(), n * x32.astype(np.float64)) <= 2e-6
+
+
+def test_partial_batch_and_host_path(F):
+    rng = np.random.default_rng(9)
+    n, b = 240, 37
+    x = (rng.uniform(-1, 1, (b, n)) + 1j * rng.uniform(-1, 1, (b, n))).astype(np.complex64)
+    p = F.Plan(n, "f32", "complex", b)
+    xi = dev(x)
+    xo = torch.zeros_like(xi)
+    p.exec(False, xi.data_ptr(), xo.data_ptr(), 0, batch=20)
+    torch.cuda.synchronize()
+    o = xo.cpu().numpy()
+    ref = np.stack([oracle.fft(r.astype(np.complex128)) for r in x])
+    assert rel_l2(o[:20], ref[:20]) <= F32_TOL
+    assert np.all(o[20:] == 0)
+    host_out = np.empty_like(x)
+    p.exec_host(False, x, host_out)
+    assert rel_l2(host_out, ref) <= F32_TOL
+
+
+def test_in_place_single_kernel(F):
+    rng = np.random.default_rng(4)
+    x = (rng.uniform(-1, 1, (8, 1024)) + 1j * rng.uniform(-1, 1, (8, 1024))).astype(np.complex64)
+    p = F.Plan(1024, "f32", "complex", 8)
+    xi = dev(x)
+    p.exec(False, xi.data_ptr(), xi.data_ptr(), 0)
+    torch.cuda.synchronize()
+    ref = np.stack([oracle.fft(r.astype(np.complex128)) for r in x])
+    assert rel_l2(xi.cpu().numpy(), ref) <= F32_TOL
+
+
+def test_reference_shaped_api(F):
+    """FFT / RealFFT / ModifiedRealFFT objects: host arrays and device tensors."""
+    rng = np.random.default_rng(2)
+    f = F.FFT(1000, 1, dtype="f64")
+    assert f.size() == 1024
+    x = rng.standard_normal(1024) + 1j * rng.standard_normal(1024)
+    assert rel_l2(f.fft(x), oracle.fft(x)) <= F64_TOL
+    assert rel_l2(f.ifft(x), oracle.fft(x, True)) <= F64_TOL
+    r = F.RealFFT(480, dtype="f64")
+    xr = rng.standard_normal(480)
+    assert rel_l2(r.fft(xr), oracle.rfft(xr)) <= F64_TOL
+    m = F.ModifiedRealFFT(480, dtype="f64")
+    assert rel_l2(m.fft(xr), oracle.rfft(xr, True)) <= F64_TOL
+    s = m.fft(xr)
+    assert rel_l2(m.ifft(s), oracle.irfft(s, 480, True)) <= F64_TOL
+    t = torch.from_numpy(xr).cuda()
+    assert rel_l2(F.rfft(t).cpu().numpy(), oracle.rfft(xr)) <= F64_TOL

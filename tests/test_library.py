@@ -1,0 +1,71 @@
+"""Host-side checks of libssfft.so that need no GPU: it loads, exports every entry point that
+include/ssfft.h declares, reproduces the reference's size helpers bit for bit, rejects invalid
+arguments with status codes, and its planner's kernels compile for sm_103a."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import fft_gb300 as F
+from conftest import ROOT
+
+
+def declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "ssfft.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(ssfft_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ctypes.CDLL(F.LIB_PATH)
+    syms = declared_symbols()
+    assert len(syms) >= 15
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_size_helpers_bit_exact(golden):
+    idx = golden["size_index"]
+    for name in ("size_minimum", "size_maximum", "real_size_minimum", "real_size_maximum"):
+        got = np.array([getattr(F, name)(int(i)) for i in idx])
+        assert np.array_equal(got, golden[name]), name
+    # documented quirks of RealFFT (signalsmith-fft.h:403-408)
+    assert F.real_size_maximum(480) == 512 and F.real_size_minimum(480) == 514
+
+
+def test_status_strings():
+    lib = F.lib()
+    for code in range(10):
+        assert lib.ssfft_status_string(code)
+
+
+def test_invalid_arguments_rejected_without_gpu():
+    lib = F.lib()
+    h = ctypes.c_void_p()
+    assert lib.ssfft_plan_create(ctypes.byref(h), 0, 0, 0, 1) == 1          # n == 0
+    assert lib.ssfft_plan_create(ctypes.byref(h), 1, 0, 1, 1) == 1          # real n < 2
+    assert lib.ssfft_plan_create(ctypes.byref(h), 64, 7, 0, 1) == 2         # bad dtype
+    assert lib.ssfft_plan_create(ctypes.byref(h), 64, 0, 9, 1) == 2         # bad kind
+    assert lib.ssfft_plan_create(None, 64, 0, 0, 1) == 2
+    assert lib.ssfft_exec(None, 0, None, None, None) == 2
+    assert lib.ssfft_plan_destroy(None) == 2
+
+
+@pytest.mark.parametrize("n,dt,kind,batch", [
+    (480, "f32", "real", 16384), (960, "f32", "real", 16384), (1920, "f32", "real", 16384),
+    (3840, "f32", "real", 16384), (1024, "f64", "complex", 256), (16384, "f32", "complex", 4),
+    (8192, "f64", "complex", 2), (97, "f32", "complex", 1), (3840, "f32", "real_halfshift", 8),
+])
+def test_plan_kernels_compile_for_sm103a(n, dt, kind, batch):
+    assert F.jit_check(n, dt, kind, batch, "sm_103a") > 0
+
+
+def test_schedules_respect_register_and_thread_budget():
+    for n in list(range(1, 300)) + [480, 960, 1920, 3840, 4096, 8192, 16384, 15360, 3 ** 8]:
+        info = F.schedule_info(n, "f32", "complex", 1000)
+        assert info["threads"] * info["per_cta"] <= 1024
+        assert info["smem_bytes"] <= 227 * 1024
+        r = info["radices"]
+        assert int(np.prod(r)) == n
