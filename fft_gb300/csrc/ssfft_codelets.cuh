@@ -189,7 +189,9 @@ __device__ __forceinline__ void dft(C *v) {
 
 // ------------------------------------------------------------------ per-thread context
 
-template <typename T, int KIND, bool INV>
+// CIN / COUT: conjugate complex data on global load / store (the inverse runs forward passes on
+// conjugated data; a multi-pass inverse conjugates at its first load and its last store).
+template <typename T, int KIND, bool CIN, bool COUT>
 struct Ctx {
 	using C = typename Cx<T>::C;
 	C *sm;         // this transform's shared-memory slots (padded)
@@ -202,12 +204,12 @@ struct Ctx {
 
 // Global element e of the pass input / output, with the conjugation of the inverse and the
 // real packing folded in.
-template <typename T, int KIND, bool INV, bool ODD>
-__device__ __forceinline__ typename Cx<T>::C gload(const Ctx<T, KIND, INV> &c, int e) {
+template <typename T, int KIND, bool CIN, bool COUT, bool ODD>
+__device__ __forceinline__ typename Cx<T>::C gload(const Ctx<T, KIND, CIN, COUT> &c, int e) {
 	using C = typename Cx<T>::C;
 	if constexpr (KIND == kComplex) {
 		const C v = __ldcs(reinterpret_cast<const C *>(c.gin) + e);
-		return INV ? conj(v) : v;
+		return CIN ? conj(v) : v;
 	} else {
 		// forward real input z[e] = {x[2e], x[2e+1]} (signalsmith-fft.h:449-454)
 		C v;
@@ -218,11 +220,11 @@ __device__ __forceinline__ typename Cx<T>::C gload(const Ctx<T, KIND, INV> &c, i
 	}
 }
 
-template <typename T, int KIND, bool INV, bool ODD>
-__device__ __forceinline__ void gstore(const Ctx<T, KIND, INV> &c, int e, typename Cx<T>::C v) {
+template <typename T, int KIND, bool CIN, bool COUT, bool ODD>
+__device__ __forceinline__ void gstore(const Ctx<T, KIND, CIN, COUT> &c, int e, typename Cx<T>::C v) {
 	using C = typename Cx<T>::C;
 	if constexpr (KIND == kComplex) {
-		__stcs(reinterpret_cast<C *>(c.gout) + e, INV ? conj(v) : v);
+		__stcs(reinterpret_cast<C *>(c.gout) + e, COUT ? conj(v) : v);
 	} else {
 		// inverse real output: the data carry conj(ifft); x[2e], x[2e+1] = ifft value, un-rotated
 		// for the half-shift variant (signalsmith-fft.h:496-501)
@@ -239,9 +241,9 @@ __device__ __forceinline__ void gstore(const Ctx<T, KIND, INV> &c, int e, typena
 
 // ------------------------------------------------------------------ one pass
 
-template <typename T, int N, int THREADS, int R, int NS, int TWO, int ROOTS, int SRC, int DST, int KIND, bool INV,
-          bool ODD, int EMAX>
-__device__ __forceinline__ void pass(const Ctx<T, KIND, INV> &c, const typename Cx<T>::C *tw,
+template <typename T, int N, int THREADS, int R, int NS, int TWO, int ROOTS, int SRC, int DST, int KIND, bool CIN,
+          bool COUT, bool ODD, int EMAX>
+__device__ __forceinline__ void pass(const Ctx<T, KIND, CIN, COUT> &c, const typename Cx<T>::C *tw,
                                      const typename Cx<T>::C *roots) {
 	using C = typename Cx<T>::C;
 	constexpr int PS = Cx<T>::kPadShift;
@@ -257,7 +259,7 @@ __device__ __forceinline__ void pass(const Ctx<T, KIND, INV> &c, const typename 
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
 					if constexpr (SRC == kSmem) v[i][r] = c.sm[pidx<PS>(j + r * NB)];
-					else v[i][r] = gload<T, KIND, INV, ODD>(c, j + r * NB);
+					else v[i][r] = gload<T, KIND, CIN, COUT, ODD>(c, j + r * NB);
 				}
 			}
 		}
@@ -282,7 +284,7 @@ __device__ __forceinline__ void pass(const Ctx<T, KIND, INV> &c, const typename 
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
 					if constexpr (DST == kSmem) c.sm[pidx<PS>(base + r * NS)] = v[i][r];
-					else gstore<T, KIND, INV, ODD>(c, base + r * NS, v[i][r]);
+					else gstore<T, KIND, CIN, COUT, ODD>(c, base + r * NS, v[i][r]);
 				}
 			}
 		}
@@ -300,12 +302,12 @@ __device__ __forceinline__ void pass(const Ctx<T, KIND, INV> &c, const typename 
 				const int k = e / NB, j = e - (e / NB) * NB, m = j % NS;
 				C s;
 				if constexpr (SRC == kSmem) s = c.sm[pidx<PS>(j)];
-				else s = gload<T, KIND, INV, ODD>(c, j);
+				else s = gload<T, KIND, CIN, COUT, ODD>(c, j);
 				int w = 0;
 				for (int r = 1; r < R; ++r) {
 					C x;
 					if constexpr (SRC == kSmem) x = c.sm[pidx<PS>(j + r * NB)];
-					else x = gload<T, KIND, INV, ODD>(c, j + r * NB);
+					else x = gload<T, KIND, CIN, COUT, ODD>(c, j + r * NB);
 					if constexpr (NS > 1) x = mul(x, __ldg(tw + TWO + (r - 1) * NS + m));
 					w += k;
 					if (w >= R) w -= R;
@@ -322,7 +324,7 @@ __device__ __forceinline__ void pass(const Ctx<T, KIND, INV> &c, const typename 
 				const int k = e / NB, j = e - (e / NB) * NB, m = j % NS;
 				const int d = (j - m) * R + m + k * NS;
 				if constexpr (DST == kSmem) c.sm[pidx<PS>(d)] = acc[i];
-				else gstore<T, KIND, INV, ODD>(c, d, acc[i]);
+				else gstore<T, KIND, CIN, COUT, ODD>(c, d, acc[i]);
 			}
 		}
 	}
@@ -339,17 +341,17 @@ struct RootCount {
 	static constexpr int value = Specialised<R>::value ? 0 : R;
 };
 
-template <typename T, int N, int THREADS, int NS, int TWO, int ROOTS, int FIRST_SRC, int LAST_DST, int KIND, bool INV,
-          bool ODD, int EMAX, int R, int... Rest>
-__device__ __forceinline__ void passes(const Ctx<T, KIND, INV> &c, const typename Cx<T>::C *tw,
+template <typename T, int N, int THREADS, int NS, int TWO, int ROOTS, int FIRST_SRC, int LAST_DST, int KIND, bool CIN,
+          bool COUT, bool ODD, int EMAX, int R, int... Rest>
+__device__ __forceinline__ void passes(const Ctx<T, KIND, CIN, COUT> &c, const typename Cx<T>::C *tw,
                                        const typename Cx<T>::C *roots) {
 	constexpr bool last = sizeof...(Rest) == 0;
 	constexpr int SRC = NS == 1 ? FIRST_SRC : kSmem;
 	constexpr int DST = last ? LAST_DST : kSmem;
-	pass<T, N, THREADS, R, NS, TWO, ROOTS, SRC, DST, KIND, INV, ODD, EMAX>(c, tw, roots);
+	pass<T, N, THREADS, R, NS, TWO, ROOTS, SRC, DST, KIND, CIN, COUT, ODD, EMAX>(c, tw, roots);
 	if constexpr (!last)
 		passes<T, N, THREADS, NS * R, TWO + TwCount<R, NS>::value, ROOTS + RootCount<R>::value, FIRST_SRC, LAST_DST,
-		       KIND, INV, ODD, EMAX, Rest...>(c, tw, roots);
+		       KIND, CIN, COUT, ODD, EMAX, Rest...>(c, tw, roots);
 }
 
 // ------------------------------------------------------------------ real split / merge
@@ -363,8 +365,8 @@ __device__ __forceinline__ void pair_writes(int i, int ci, int s, int last, bool
 }
 
 // Forward split: Z (H points) in shared memory -> H bins in HBM (signalsmith-fft.h:459-472).
-template <typename T, int H, int THREADS, int KIND, bool INV>
-__device__ __forceinline__ void real_post(const Ctx<T, KIND, INV> &c, const typename Cx<T>::C *rtw) {
+template <typename T, int H, int THREADS, int KIND, bool CIN, bool COUT>
+__device__ __forceinline__ void real_post(const Ctx<T, KIND, CIN, COUT> &c, const typename Cx<T>::C *rtw) {
 	using C = typename Cx<T>::C;
 	constexpr int PS = Cx<T>::kPadShift;
 	constexpr bool MOD = KIND == kRealHalfShift;
@@ -393,8 +395,8 @@ __device__ __forceinline__ void real_post(const Ctx<T, KIND, INV> &c, const type
 
 // Inverse pre-twiddle: H bins in HBM -> conj(first-pass input) in shared memory
 // (signalsmith-fft.h:477-492).
-template <typename T, int H, int THREADS, int KIND, bool INV>
-__device__ __forceinline__ void real_pre(const Ctx<T, KIND, INV> &c, const typename Cx<T>::C *rtw) {
+template <typename T, int H, int THREADS, int KIND, bool CIN, bool COUT>
+__device__ __forceinline__ void real_pre(const Ctx<T, KIND, CIN, COUT> &c, const typename Cx<T>::C *rtw) {
 	using C = typename Cx<T>::C;
 	constexpr int PS = Cx<T>::kPadShift;
 	constexpr bool MOD = KIND == kRealHalfShift;
@@ -435,7 +437,7 @@ __global__ void __launch_bounds__(THREADS *PER_CTA) batch(const Args a) {
 	constexpr bool R2C = REAL && !INV, C2R = REAL && INV;
 	const int g = threadIdx.x / THREADS;
 	const long long gi = (long long)blockIdx.x * PER_CTA + g;
-	Ctx<T, KIND, INV> c;
+	Ctx<T, KIND, INV, INV> c;
 	c.t = threadIdx.x - g * THREADS;
 	c.valid = gi < a.batch;
 	c.sm = reinterpret_cast<C *>(smem_raw) + g * SMEM_STRIDE;
@@ -445,10 +447,154 @@ __global__ void __launch_bounds__(THREADS *PER_CTA) batch(const Args a) {
 	const C *tw = reinterpret_cast<const C *>(a.tw);
 	const C *roots = reinterpret_cast<const C *>(a.roots);
 	const C *rtw = reinterpret_cast<const C *>(a.rtw);
-	if constexpr (C2R) real_pre<T, N, THREADS, KIND, INV>(c, rtw);
-	passes<T, N, THREADS, 1, 0, 0, C2R ? kSmem : kGlobal, R2C ? kSmem : kGlobal, KIND, INV, ODD, EMAX, Rs...>(c, tw,
-	                                                                                                         roots);
-	if constexpr (R2C) real_post<T, N, THREADS, KIND, INV>(c, rtw);
+	if constexpr (C2R) real_pre<T, N, THREADS, KIND, INV, INV>(c, rtw);
+	passes<T, N, THREADS, 1, 0, 0, C2R ? kSmem : kGlobal, R2C ? kSmem : kGlobal, KIND, INV, INV, ODD, EMAX, Rs...>(
+	    c, tw, roots);
+	if constexpr (R2C) real_post<T, N, THREADS, KIND, INV, INV>(c, rtw);
+}
+
+// ------------------------------------------------------------------ multi-pass (four-step) kernel
+
+// One pass of a multi-pass transform: U = U2*U1*U0 sub-transforms of N points.  Sub-transform
+// u = (u2, u1, u0) reads element e at in + u2*is2 + u1*is1 + u0*is0 + e*in_es and writes element
+// k at out + u2*os2 + u1*os1 + u0*os0 + k*out_es (complex elements).  A CTA takes G consecutive
+// u0 (adjacent in memory when is0 / os0 == 1), so a strided load (SLOAD) or store (SSTORE)
+// through shared memory moves G-element contiguous segments.  TW multiplies output element k of
+// sub-transform u0 by W_TWN^{u0 k} (the four-step inter-pass twiddle), from a two-level table:
+// W^t = twhi[t >> LB] * twlo[t & (2^LB - 1)].  ROT (first pass of a half-shift real forward /
+// last pass of its inverse) applies e^{-+2 pi i j / n_real} by the element's index j in the
+// whole transform.
+struct StridedArgs {
+	const void *in;
+	void *out;
+	long long U0, U1, U2;
+	long long is0, is1, is2, in_es;
+	long long os0, os1, os2, out_es;
+	const void *tw;     // pass twiddles of the N-point sub-transform
+	const void *roots;
+	const void *twlo;   // inter-pass twiddles, two-level table
+	const void *twhi;
+	const void *rot;    // half-shift rotations (ROT)
+	long long rot_in_stride2, rot_out_stride2;  // u2 stride of the index j inside the whole transform
+};
+
+template <typename T, int N, int THREADS, int G, int STRIDE, bool CIN, bool COUT, int EMAX, bool SLOAD, bool SSTORE,
+          long long TWN, int LB, int ROT, int... Rs>
+__global__ void __launch_bounds__(THREADS *G) strided(const StridedArgs a) {
+	using C = typename Cx<T>::C;
+	constexpr int PS = Cx<T>::kPadShift;
+	constexpr int CTA = THREADS * G;
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	C *sm_all = reinterpret_cast<C *>(smem_raw);
+	const long long blocks0 = (a.U0 + G - 1) / G;
+	long long cta = blockIdx.x;
+	const long long u0b = cta % blocks0;
+	cta /= blocks0;
+	const long long u1 = cta % a.U1, u2 = cta / a.U1;
+	const long long u00 = u0b * G;
+	const long long ib = u2 * a.is2 + u1 * a.is1, ob = u2 * a.os2 + u1 * a.os1;
+	const C *in = reinterpret_cast<const C *>(a.in);
+	C *out = reinterpret_cast<C *>(a.out);
+	const int g = threadIdx.x / THREADS;
+	Ctx<T, kComplex, CIN, COUT> c;
+	c.t = threadIdx.x - g * THREADS;
+	c.valid = u00 + g < a.U0;
+	c.sm = sm_all + g * STRIDE;
+	c.gin = reinterpret_cast<const T *>(in + (c.valid ? ib + (u00 + g) * a.is0 : 0));
+	c.gout = reinterpret_cast<T *>(out + (c.valid ? ob + (u00 + g) * a.os0 : 0));
+	c.rot = reinterpret_cast<const C *>(a.rot);
+	if constexpr (SLOAD) {
+		// G-element segments: consecutive threads take consecutive u0 of the same element
+#pragma unroll 4
+		for (int idx = threadIdx.x; idx < G * N; idx += CTA) {
+			const int gg = idx % G, e = idx / G;
+			if (u00 + gg < a.U0) {
+				const long long off = ib + (u00 + gg) * a.is0 + (long long)e * a.in_es;
+				C v = __ldcs(in + off);
+				if constexpr (CIN) v = conj(v);
+				if constexpr (ROT == 1) v = mul(v, __ldg(c.rot + (off - u2 * a.rot_in_stride2)));
+				sm_all[gg * STRIDE + pidx<PS>(e)] = v;
+			}
+		}
+		__syncthreads();
+	}
+	passes<T, N, THREADS, 1, 0, 0, SLOAD ? kSmem : kGlobal, SSTORE ? kSmem : kGlobal, kComplex, CIN, COUT, false, EMAX,
+	       Rs...>(c, reinterpret_cast<const C *>(a.tw), reinterpret_cast<const C *>(a.roots));
+	if constexpr (SSTORE) {
+		const C *twlo = reinterpret_cast<const C *>(a.twlo);
+		const C *twhi = reinterpret_cast<const C *>(a.twhi);
+#pragma unroll 4
+		for (int idx = threadIdx.x; idx < G * N; idx += CTA) {
+			const int gg = idx % G, k = idx / G;
+			const long long u0 = u00 + gg;
+			if (u0 < a.U0) {
+				C v = sm_all[gg * STRIDE + pidx<PS>(k)];
+				if constexpr (TWN > 1) {
+					const unsigned long long t = ((unsigned long long)u0 * (unsigned long long)k) % (unsigned long long)TWN;
+					v = mul(v, mul(__ldg(twhi + (t >> LB)), __ldg(twlo + (t & ((1ull << LB) - 1)))));
+				}
+				const long long off = ob + u0 * a.os0 + (long long)k * a.out_es;
+				if constexpr (ROT == 2) {
+					// inverse half-shift real output: data carry conj(ifft), un-rotate by e^{-2 pi i j/n}
+					C y = conj(v);
+					y = mulc(y, __ldg(c.rot + (off - u2 * a.rot_out_stride2)));
+					__stcs(out + off, y);
+				} else {
+					__stcs(out + off, COUT ? conj(v) : v);
+				}
+			}
+		}
+	}
+}
+
+// Real split / merge over global memory for real transforms longer than one CTA holds
+// (signalsmith-fft.h:459-472 forward, :477-492 inverse).  One thread per pair (i, conj(i)),
+// in place on `buf` (H complex per transform, batch transforms `dist` complex apart).
+// Forward: buf holds Z = FFT(z) and receives the H bins.  Inverse: buf holds the H bins and
+// receives conj(pre-twiddled input) for the forward passes that follow.
+struct SplitArgs {
+	void *buf;
+	const void *src;   // inverse only: the caller's bins (buf may differ so the input is kept)
+	long long batch, dist;
+	const void *rtw;
+};
+
+template <typename T, long long H, bool MOD, bool INVERSE>
+__global__ void __launch_bounds__(256) real_split(const SplitArgs a) {
+	using C = typename Cx<T>::C;
+	constexpr long long S = MOD ? 0 : 1, LAST = H / 2, NPAIRS = LAST - S + 1;
+	const long long gid = (long long)blockIdx.x * 256 + threadIdx.x;
+	const long long b = blockIdx.y;
+	if (b >= a.batch) return;
+	C *buf = reinterpret_cast<C *>(a.buf) + b * a.dist;
+	const C *src = reinterpret_cast<const C *>(INVERSE ? a.src : a.buf) + b * a.dist;
+	const C *rtw = reinterpret_cast<const C *>(a.rtw);
+	if (!MOD && gid == 0) {
+		const C v = src[0];
+		if (INVERSE) buf[0] = conj(mkc(v.x + v.y, v.x - v.y));
+		else buf[0] = mkc(v.x + v.y, v.x - v.y);
+	}
+	if (gid >= NPAIRS) return;
+	const long long i = S + gid;
+	const long long ci = MOD ? H - 1 - i : H - i;
+	const bool ci_in = ci >= S && ci <= LAST;
+	const bool wi = !ci_in || ci < i, wci = !ci_in || i >= ci;
+	if (!INVERSE) {
+		const C zi = src[i];
+		const C zc = conj(src[ci]);
+		const C odd = scale(add(zi, zc), T(0.5));
+		const C even = scale(sub(zi, zc), T(0.5));
+		const C e = mul(even, __ldg(rtw + i));
+		if (wi) buf[i] = add(odd, e);
+		if (wci) buf[ci] = conj(sub(odd, e));
+	} else {
+		const C v = src[i];
+		const C v2c = conj(src[ci]);
+		const C odd = add(v, v2c);
+		const C even = mulc(sub(v, v2c), __ldg(rtw + i));
+		if (wi) buf[i] = conj(add(odd, even));
+		if (wci) buf[ci] = sub(odd, even);
+	}
 }
 
 }  // namespace ssfft_cl

@@ -90,6 +90,8 @@ std::string device_arch(int device);
 ssfft_status jit_kernels(const std::vector<std::string> &names, size_t smem_bytes, std::vector<CUfunction> &fns);
 ssfft_status jit_compile_only(const std::vector<std::string> &names, const std::string &arch, size_t *image_bytes);
 ssfft_status jit_launch(CUfunction f, unsigned grid, unsigned block, size_t smem, cudaStream_t stream, void *args);
+ssfft_status jit_launch_grid(CUfunction f, unsigned grid_x, unsigned grid_y, unsigned block, size_t smem,
+                             cudaStream_t stream, void *args);
 const char *jit_last_log();
 
 // plans
@@ -103,5 +105,7 @@ void plan_release(Plan *p);
 ssfft_status launch_batch(const Plan *p, int inverse, const void *in, void *out, size_t batch, cudaStream_t s);
 ssfft_status launch_large(Plan *p, int inverse, const void *in, void *out, size_t batch, cudaStream_t s);
 void large_release(LargePlan *lp);
+ssfft_status large_jit_check(size_t n, ssfft_dtype dtype, ssfft_kind kind, const char *arch, size_t *image_bytes);
+bool large_describe(size_t n, ssfft_dtype dtype, ssfft_kind kind, std::vector<long long> &F);
 
 }  // namespace ssfft

@@ -292,11 +292,17 @@ ssfft_status jit_compile_only(const std::vector<std::string> &names, const std::
 	return st;
 }
 
-ssfft_status jit_launch(CUfunction f, unsigned grid, unsigned block, size_t smem, cudaStream_t stream, void *args) {
+ssfft_status jit_launch_grid(CUfunction f, unsigned grid_x, unsigned grid_y, unsigned block, size_t smem,
+                             cudaStream_t stream, void *args) {
 	void *params[] = {args};
-	CUresult r = driver().launchKernel(f, grid, 1, 1, block, 1, 1, (unsigned)smem, (CUstream)stream, params, nullptr);
+	CUresult r =
+	    driver().launchKernel(f, grid_x, grid_y, 1, block, 1, 1, (unsigned)smem, (CUstream)stream, params, nullptr);
 	if (r != CUDA_SUCCESS) return cu_fail(r, "cuLaunchKernel");
 	return SSFFT_SUCCESS;
+}
+
+ssfft_status jit_launch(CUfunction f, unsigned grid, unsigned block, size_t smem, cudaStream_t stream, void *args) {
+	return jit_launch_grid(f, grid, 1, block, smem, stream, args);
 }
 
 }  // namespace ssfft

@@ -1,16 +1,406 @@
 // ssfft_large.cu -- multi-pass (four-step) transforms for sizes beyond one CTA.
+//
+// The reference runs large sizes depth-first with the same radix steps (cache blocking when a
+// sub-block exceeds 64 KiB, signalsmith-fft.h:130-136).  Here a transform of N complex points
+// (N = F1 * F2 [* F3], each factor <= 1024) runs as 2 or 3 kernel passes over HBM:
+//
+//   n = n1 F2 F3 + n2 F3 + n3,  k = k1 + F1 k2 + F1 F2 k3
+//   pass 1: Y1[k1][n2][n3] = DFT_F1 over n1, times W_N^{(n2 F3 + n3) k1}        (in -> scratch)
+//   pass 2: Y2[k1][k2][n3] = DFT_F2 over n2, times W_{F2 F3}^{n3 k2}            (scratch, in place)
+//   pass 3: X[k1 + F1 k2 + F1 F2 k3] = DFT_F3 over n3                          (scratch -> out)
+//
+// Each pass is one launch of ssfft_cl::strided: a CTA takes G sub-transforms that are adjacent
+// in memory, so strided loads and stores move G-element contiguous segments through shared
+// memory, and the inter-pass twiddle is applied in the pass's store.  Real transforms of
+// h = n/2 > 16384 points add the even/odd split (forward) or pre-twiddle (inverse) as one
+// element-wise kernel (ssfft_cl::real_split).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
 #include "ssfft_host.h"
 
 namespace ssfft {
 
-struct LargePlan {
-	int unused = 0;
+constexpr long long kMaxFactor = 1024;
+constexpr int kGroup = 16;  // sub-transforms per CTA in the strided passes
+
+struct LargePass {
+	Schedule sub;              // N-point sub-transform (sub.per_cta = G)
+	bool sload = false, sstore = false;
+	long long twn = 1;
+	int lb = 0;
+	long long U0 = 1, U1 = 1;
+	long long is0 = 0, is1 = 0, in_es = 1, os0 = 0, os1 = 0, out_es = 1;
+	size_t off_tw = 0, off_roots = 0, off_twlo = 0, off_twhi = 0;
+	CUfunction fwd = nullptr, inv = nullptr;
+	std::string name(bool inverse, bool first, bool last, int rot) const;
 };
 
-ssfft_status plan_build_large(Plan *) { return SSFFT_ERR_UNSUPPORTED; }
+struct LargePlan {
+	long long N = 0;            // complex points
+	std::vector<long long> F;   // pass factors
+	std::vector<LargePass> pass;
+	bool real = false, modified = false;
+	size_t off_rtw = 0, off_rot = 0;
+	CUfunction split_fwd = nullptr, split_inv = nullptr;
+	void *d_tables = nullptr;
+	void *d_scratch = nullptr;
+	size_t scratch_batch = 0;
+};
 
-ssfft_status launch_large(Plan *, int, const void *, void *, size_t, cudaStream_t) { return SSFFT_ERR_UNSUPPORTED; }
+std::string LargePass::name(bool inverse, bool first, bool last, int rot) const {
+	const bool cin = inverse && first, cout = inverse && last;
+	std::string r = "ssfft_cl::strided<";
+	r += sub.dtype == SSFFT_F32 ? "float" : "double";
+	r += ", " + std::to_string(sub.n) + ", " + std::to_string(sub.threads) + ", " + std::to_string(sub.per_cta) + ", " +
+	     std::to_string(sub.smem_stride) + ", " + (cin ? "true" : "false") + ", " + (cout ? "true" : "false") + ", " +
+	     std::to_string(kElemsPerThread) + ", " + (sload ? "true" : "false") + ", " + (sstore ? "true" : "false") +
+	     ", " + std::to_string(twn) + "LL, " + std::to_string(lb) + ", " + std::to_string(rot);
+	for (int x : sub.radices) r += ", " + std::to_string(x);
+	r += ">";
+	return r;
+}
 
-void large_release(LargePlan *lp) { delete lp; }
+static std::string split_name(ssfft_dtype dt, long long h, bool mod, bool inverse) {
+	return std::string("ssfft_cl::real_split<") + (dt == SSFFT_F32 ? "float" : "double") + ", " + std::to_string(h) +
+	       "LL, " + (mod ? "true" : "false") + ", " + (inverse ? "true" : "false") + ">";
+}
+
+// Split N into 2 (N <= kMaxFactor^2) or 3 balanced factors, each <= kMaxFactor.
+static bool large_factors(long long N, std::vector<long long> &F) {
+	std::vector<long long> primes;
+	long long m = N;
+	for (long long p = 2; p * p <= m; ++p)
+		while (m % p == 0) {
+			primes.push_back(p);
+			m /= p;
+		}
+	if (m > 1) primes.push_back(m);
+	for (long long p : primes)
+		if (p > kMaxFactor) return false;
+	const int P = N <= kMaxFactor * kMaxFactor ? 2 : 3;
+	if (N > kMaxFactor * kMaxFactor * kMaxFactor) return false;
+	std::sort(primes.begin(), primes.end(), [](long long a, long long b) { return a > b; });
+	F.assign(P, 1);
+	for (long long p : primes) {
+		// give p to the smallest group that can take it
+		int best = -1;
+		for (int i = 0; i < P; ++i)
+			if (F[i] * p <= kMaxFactor && (best < 0 || F[i] < F[best])) best = i;
+		if (best < 0) return false;
+		F[best] *= p;
+	}
+	for (long long f : F)
+		if (f < 2) return false;
+	return true;
+}
+
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+template <typename T>
+static void put(std::vector<unsigned char> &blob, size_t off, const std::vector<double> &src) {
+	T *dst = reinterpret_cast<T *>(blob.data() + off);
+	for (size_t i = 0; i < src.size(); ++i) dst[i] = (T)src[i];
+}
+
+void large_release(LargePlan *lp) {
+	if (!lp) return;
+	if (lp->d_scratch) cudaFree(lp->d_scratch);
+	if (lp->d_tables) cudaFree(lp->d_tables);
+	delete lp;
+}
+
+// Schedule, strides and FP64 tables of a multi-pass plan (no GPU needed).
+struct LargeTables {
+	std::vector<std::vector<double>> tw, roots, twlo, twhi;
+};
+
+static ssfft_status large_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t smem_limit, LargePlan *lp,
+                                   LargeTables &t) {
+	const bool real = kind != SSFFT_COMPLEX;
+	if (real && (n & 1)) return SSFFT_ERR_UNSUPPORTED;  // long odd real lengths
+	const long long N = (long long)(real ? n / 2 : n);
+	std::vector<long long> F;
+	if (!large_factors(N, F)) return SSFFT_ERR_UNSUPPORTED;
+	lp->N = N;
+	lp->F = F;
+	lp->real = real;
+	lp->modified = kind == SSFFT_REAL_HALFSHIFT;
+	const int P = (int)F.size();
+	const size_t eb = dtype == SSFFT_F32 ? 8 : 16;
+	t.tw.assign(P, {});
+	t.roots.assign(P, {});
+	t.twlo.assign(P, {});
+	t.twhi.assign(P, {});
+	auto &tw = t.tw, &roots = t.roots, &twlo = t.twlo, &twhi = t.twhi;
+	lp->pass.clear();
+	lp->pass.reserve(P);
+	long long L = N;  // length of the dimensions not yet transformed
+	for (int i = 0; i < P; ++i) {
+		LargePass &ps = *lp->pass.emplace(lp->pass.end());
+		const long long Fi = F[i], R = L / Fi, Q = N / L;
+		const bool last = i == P - 1;
+		Schedule s;
+		if (!make_schedule(dtype, (int)Fi, 0, false, 1, s)) return SSFFT_ERR_UNSUPPORTED;
+		// G sub-transforms per CTA: 128-256 B segments, <= 1024 threads, <= ~100 KiB smem
+		const long long U0 = last ? F[0] : R;
+		int G = (int)std::min<long long>(kGroup, U0);
+		while (G > 1 && (G * s.threads > kMaxCtaThreads || (size_t)G * s.smem_stride * eb > 100 * 1024)) --G;
+		s.per_cta = G;
+		s.smem_bytes = (size_t)G * s.smem_stride * eb;
+		if (s.smem_bytes > smem_limit) return SSFFT_ERR_UNSUPPORTED;
+		ps.sub = s;
+		if (!last) {
+			ps.sload = ps.sstore = true;
+			ps.U0 = R;
+			ps.U1 = Q;
+			ps.is0 = ps.os0 = 1;
+			ps.is1 = ps.os1 = L;
+			ps.in_es = ps.out_es = R;
+			ps.twn = L;
+		} else {
+			// rows of F_P contiguous; output index k1 + F1 k2 (+ F1 F2 k3)
+			ps.sload = false;
+			ps.sstore = true;
+			ps.U0 = F[0];
+			ps.U1 = P == 2 ? 1 : Q / F[0];
+			ps.is0 = N / F[0];
+			ps.os0 = 1;
+			ps.is1 = Fi;           // P == 3: u1 = k2, row offset k2 F3
+			ps.os1 = F[0];         // P == 3: output offset F1 k2
+			ps.in_es = 1;
+			ps.out_es = N / Fi;    // F1 F2 (or F1 for P == 2)
+			ps.twn = 1;
+		}
+		schedule_twiddles(s, tw[i], roots[i]);
+		if (ps.twn > 1) {
+			int lb = 0;
+			while ((1ll << (2 * lb)) < ps.twn) ++lb;  // 2^lb >= sqrt(twn)
+			ps.lb = lb;
+			const long long lo = 1ll << lb, hi = (ps.twn + lo - 1) / lo;
+			for (long long k = 0; k < lo; ++k) {
+				double re, im;
+				unit_root((unsigned long long)k, (unsigned long long)ps.twn, &re, &im);
+				twlo[i].push_back(re);
+				twlo[i].push_back(im);
+			}
+			for (long long k = 0; k < hi; ++k) {
+				double re, im;
+				unit_root((unsigned long long)(k * lo), (unsigned long long)ps.twn, &re, &im);
+				twhi[i].push_back(re);
+				twhi[i].push_back(im);
+			}
+		}
+		L = R;
+	}
+	return SSFFT_SUCCESS;
+}
+
+// Kernel names of a multi-pass plan: per pass forward then inverse, then the real split/merge.
+static std::vector<std::string> large_kernel_names(const LargePlan *lp, ssfft_dtype dtype) {
+	std::vector<std::string> names;
+	const int P = (int)lp->pass.size();
+	for (int i = 0; i < P; ++i) {
+		const LargePass &ps = lp->pass[i];
+		const bool first = i == 0, last = i == P - 1;
+		const int rot_f = lp->modified && first ? 1 : 0, rot_i = lp->modified && last ? 2 : 0;
+		names.push_back(ps.name(false, first, last, rot_f));
+		// a real inverse arrives pre-twiddled and conjugated, so its first pass does not conjugate
+		names.push_back(lp->real ? ps.name(true, false, last, rot_i) : ps.name(true, first, last, 0));
+	}
+	if (lp->real) {
+		names.push_back(split_name(dtype, lp->N, lp->modified, false));
+		names.push_back(split_name(dtype, lp->N, lp->modified, true));
+	}
+	return names;
+}
+
+ssfft_status large_jit_check(size_t n, ssfft_dtype dtype, ssfft_kind kind, const char *arch, size_t *image_bytes) {
+	LargePlan lp;
+	LargeTables t;
+	ssfft_status st = large_schedule(n, dtype, kind, 227 * 1024, &lp, t);
+	if (st != SSFFT_SUCCESS) return st;
+	return jit_compile_only(large_kernel_names(&lp, dtype), arch, image_bytes);
+}
+
+ssfft_status plan_build_large(Plan *p) {
+	LargePlan *lp = new LargePlan();
+	p->large = lp;
+	LargeTables tabs;
+	ssfft_status st0 = large_schedule(p->n, p->dtype, p->kind, device_smem_limit(p->device), lp, tabs);
+	if (st0 != SSFFT_SUCCESS) return st0;
+	const bool real = lp->real;
+	const long long N = lp->N;
+	const int P = (int)lp->pass.size();
+	const size_t eb = p->dtype == SSFFT_F32 ? 8 : 16, sb = eb / 2;
+	auto &tw = tabs.tw, &roots = tabs.roots, &twlo = tabs.twlo, &twhi = tabs.twhi;
+	std::vector<double> rtw, rot;
+	if (real) {
+		for (long long i = 0; i <= N / 2; ++i) {
+			double re, im;
+			if (lp->modified) unit_root(2 * i + 1, 2 * (unsigned long long)p->n, &re, &im);
+			else unit_root(i, p->n, &re, &im);
+			rtw.push_back(im);
+			rtw.push_back(-re);
+		}
+		if (lp->modified)
+			for (long long i = 0; i < N; ++i) {
+				double re, im;
+				unit_root(i, p->n, &re, &im);
+				rot.push_back(re);
+				rot.push_back(im);
+			}
+	}
+	// one table allocation
+	size_t off = 0;
+	for (int i = 0; i < P; ++i) {
+		LargePass &ps = lp->pass[i];
+		ps.off_tw = off;
+		off = align_up(off + tw[i].size() * sb, 256);
+		ps.off_roots = off;
+		off = align_up(off + roots[i].size() * sb, 256);
+		ps.off_twlo = off;
+		off = align_up(off + twlo[i].size() * sb, 256);
+		ps.off_twhi = off;
+		off = align_up(off + twhi[i].size() * sb, 256);
+	}
+	lp->off_rtw = off;
+	off = align_up(off + rtw.size() * sb, 256);
+	lp->off_rot = off;
+	off = align_up(off + rot.size() * sb, 256);
+	std::vector<unsigned char> blob(std::max<size_t>(off, 256), 0);
+	for (int i = 0; i < P; ++i) {
+		const LargePass &ps = lp->pass[i];
+		if (sb == 4) {
+			put<float>(blob, ps.off_tw, tw[i]);
+			put<float>(blob, ps.off_roots, roots[i]);
+			put<float>(blob, ps.off_twlo, twlo[i]);
+			put<float>(blob, ps.off_twhi, twhi[i]);
+		} else {
+			put<double>(blob, ps.off_tw, tw[i]);
+			put<double>(blob, ps.off_roots, roots[i]);
+			put<double>(blob, ps.off_twlo, twlo[i]);
+			put<double>(blob, ps.off_twhi, twhi[i]);
+		}
+	}
+	if (sb == 4) {
+		put<float>(blob, lp->off_rtw, rtw);
+		put<float>(blob, lp->off_rot, rot);
+	} else {
+		put<double>(blob, lp->off_rtw, rtw);
+		put<double>(blob, lp->off_rot, rot);
+	}
+	cudaError_t e = cudaMalloc(&lp->d_tables, blob.size());
+	if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(large tables)");
+	e = cudaMemcpy(lp->d_tables, blob.data(), blob.size(), cudaMemcpyHostToDevice);
+	if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(large tables)");
+	p->table_bytes = blob.size();
+
+	// scratch: N complex per transform, for up to ~512 MiB of transforms at once
+	const size_t per = (size_t)N * eb;
+	lp->scratch_batch = std::max<size_t>(1, std::min<size_t>(p->batch, (512u << 20) / per));
+	e = cudaMalloc(&lp->d_scratch, per * lp->scratch_batch);
+	if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(scratch)");
+	p->scratch_bytes = per * lp->scratch_batch;
+
+	// kernels: every pass in both directions, plus the real split / merge
+	const std::vector<std::string> names = large_kernel_names(lp, p->dtype);
+	size_t smem_max = 0;
+	for (const LargePass &ps : lp->pass) smem_max = std::max(smem_max, ps.sub.smem_bytes);
+	std::vector<CUfunction> fns;
+	ssfft_status st = jit_kernels(names, smem_max, fns);
+	if (st != SSFFT_SUCCESS) return st;
+	for (int i = 0; i < P; ++i) {
+		lp->pass[i].fwd = fns[2 * i];
+		lp->pass[i].inv = fns[2 * i + 1];
+	}
+	if (real) {
+		lp->split_fwd = fns[2 * P];
+		lp->split_inv = fns[2 * P + 1];
+	}
+	p->launches_per_exec = P + (real ? 1 : 0);
+	return SSFFT_SUCCESS;
+}
+
+ssfft_status launch_large(Plan *p, int inverse, const void *in, void *out, size_t batch, cudaStream_t s) {
+	LargePlan *lp = p->large;
+	const size_t eb = p->dtype == SSFFT_F32 ? 8 : 16;
+	const unsigned char *tab = static_cast<const unsigned char *>(lp->d_tables);
+	const long long N = lp->N;
+	const int P = (int)lp->pass.size();
+	for (size_t b0 = 0; b0 < batch; b0 += lp->scratch_batch) {
+		const long long nb = (long long)std::min(lp->scratch_batch, batch - b0);
+		const unsigned char *src = static_cast<const unsigned char *>(in) + b0 * N * eb;
+		unsigned char *dst = static_cast<unsigned char *>(out) + b0 * N * eb;
+		const void *first_in = src;
+		if (lp->real && inverse) {
+			// pre-twiddle the bins into the output buffer (the caller's input is left alone)
+			ssfft_cl::SplitArgs a;
+			a.buf = dst;
+			a.src = src;
+			a.batch = nb;
+			a.dist = N;
+			a.rtw = tab + lp->off_rtw;
+			const long long pairs = N / 2 + 1;
+			ssfft_status st = jit_launch_grid(lp->split_inv, (unsigned)((pairs + 255) / 256), (unsigned)nb, 256, 0, s, &a);
+			if (st != SSFFT_SUCCESS) return st;
+			first_in = dst;
+		}
+		for (int i = 0; i < P; ++i) {
+			const LargePass &ps = lp->pass[i];
+			ssfft_cl::StridedArgs a;
+			a.in = i == 0 ? first_in : lp->d_scratch;
+			a.out = i == P - 1 ? (void *)dst : lp->d_scratch;
+			a.U0 = ps.U0;
+			a.U1 = ps.U1;
+			a.U2 = nb;
+			a.is0 = ps.is0;
+			a.is1 = ps.is1;
+			a.is2 = N;
+			a.in_es = ps.in_es;
+			a.os0 = ps.os0;
+			a.os1 = ps.os1;
+			a.os2 = N;
+			a.out_es = ps.out_es;
+			a.tw = tab + ps.off_tw;
+			a.roots = tab + ps.off_roots;
+			a.twlo = tab + ps.off_twlo;
+			a.twhi = tab + ps.off_twhi;
+			a.rot = tab + lp->off_rot;
+			a.rot_in_stride2 = N;
+			a.rot_out_stride2 = N;
+			const long long G = ps.sub.per_cta;
+			const long long grid = nb * ps.U1 * ((ps.U0 + G - 1) / G);
+			if (grid > 0x7fffffffLL) return SSFFT_ERR_INVALID_SIZE;
+			ssfft_status st = jit_launch(inverse ? ps.inv : ps.fwd, (unsigned)grid, (unsigned)ps.sub.cta_threads(),
+			                             ps.sub.smem_bytes, s, &a);
+			if (st != SSFFT_SUCCESS) return st;
+		}
+		if (lp->real && !inverse) {
+			ssfft_cl::SplitArgs a;
+			a.buf = dst;
+			a.src = dst;
+			a.batch = nb;
+			a.dist = N;
+			a.rtw = tab + lp->off_rtw;
+			const long long pairs = N / 2 + 1;
+			ssfft_status st = jit_launch_grid(lp->split_fwd, (unsigned)((pairs + 255) / 256), (unsigned)nb, 256, 0, s, &a);
+			if (st != SSFFT_SUCCESS) return st;
+		}
+	}
+	return SSFFT_SUCCESS;
+}
+
+// Pass factors of the multi-pass plan of n points (no GPU needed).
+bool large_describe(size_t n, ssfft_dtype dtype, ssfft_kind kind, std::vector<long long> &F) {
+	LargePlan lp;
+	LargeTables t;
+	if (large_schedule(n, dtype, kind, 227 * 1024, &lp, t) != SSFFT_SUCCESS) return false;
+	F = lp.F;
+	return true;
+}
 
 }  // namespace ssfft

@@ -443,6 +443,17 @@ ssfft_status ssfft_plan_describe(ssfft_plan_t plan, int *npasses, int *radices, 
                                  int *transforms_per_cta, int *kernel_launches) {
 	if (!plan) return SSFFT_ERR_INVALID_VALUE;
 	const Plan *p = reinterpret_cast<Plan *>(plan);
+	if (p->large) {
+		std::vector<long long> F;
+		large_describe(p->n, p->dtype, p->kind, F);
+		if (npasses) *npasses = (int)F.size();
+		if (radices)
+			for (int i = 0; i < (int)F.size() && i < cap; ++i) radices[i] = (int)F[i];
+		if (threads_per_transform) *threads_per_transform = 0;
+		if (transforms_per_cta) *transforms_per_cta = 0;
+		if (kernel_launches) *kernel_launches = p->launches_per_exec;
+		return SSFFT_SUCCESS;
+	}
 	const Schedule &s = p->main.sch;
 	if (npasses) *npasses = (int)s.radices.size();
 	if (radices)
@@ -484,7 +495,7 @@ ssfft_status ssfft_exec(ssfft_plan_t plan, int inverse, const void *d_in, void *
 ssfft_status ssfft_jit_check(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, const char *arch,
                              size_t *image_bytes) {
 	Schedule s;
-	if (!single_schedule(n, dtype, kind, batch, s)) return SSFFT_ERR_UNSUPPORTED;
+	if (!single_schedule(n, dtype, kind, batch, s)) return large_jit_check(n, dtype, kind, arch ? arch : "sm_103a", image_bytes);
 	return jit_compile_only({s.name(false), s.name(true)}, arch ? arch : "sm_103a", image_bytes);
 }
 

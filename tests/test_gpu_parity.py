@@ -77,13 +77,20 @@ COMPLEX_SIZES = [1, 2, 4, 8, 16, 32, 64, 128, 256, 3, 6, 9, 12, 18, 24, 5, 10, 1
 
 @pytest.mark.parametrize("dt", ["f64", "f32"])
 def test_complex_golden(F, golden, dt):
+    """FP64: within 1e-14 of the reference's FFT<double> output.  FP32: within 1e-6 of the FP64
+    oracle on the same inputs, and within 3e-6 of the reference's own FFT<float> output (which
+    carries up to ~1e-6 error of its own: float-rounded phases, signalsmith-fft.h:123)."""
     for n in COMPLEX_SIZES:
         x = golden[f"c2c_{dt}_{n}_in"][None, :]
         for d, inv in (("fwd", False), ("inv", True)):
             got, xin = run_complex(F, x, inv)
             ref = golden[f"c2c_{dt}_{n}_{d}"]
-            tol = f64_tol(n) if dt == "f64" else F32_TOL
-            assert rel_l2(got[0], ref) <= tol, (n, d, rel_l2(got[0], ref))
+            if dt == "f64":
+                assert rel_l2(got[0], ref) <= f64_tol(n), (n, d, rel_l2(got[0], ref))
+            else:
+                exact = oracle.fft(x[0].astype(np.complex128), inv)
+                assert rel_l2(got[0], exact) <= F32_TOL, (n, d, rel_l2(got[0], exact))
+                assert rel_l2(got[0], ref) <= 3 * F32_TOL, (n, d, rel_l2(got[0], ref))
             assert np.array_equal(xin, x), "input was changed"
 
 
@@ -95,7 +102,8 @@ def test_real_golden(F, golden, dt, kind):
         key = f"r_{dt}_m{int(mod)}_{n}"
         if key + "_in" not in golden:
             continue
-        tol = f64_tol(n // 2) if dt == "f64" else F32_TOL
+        # FP32 against the reference's own RealFFT<float> output: both carry ~1e-7 error
+        tol = f64_tol(n // 2) if dt == "f64" else 3 * F32_TOL
         x = golden[key + "_in"]
         p = F.Plan(n, dt, kind, 1)
         h = n // 2
