@@ -69,6 +69,7 @@ def _declare(l):
     l.ssfft_exec.argtypes = [_vp, _int, _vp, _vp, _vp]
     l.ssfft_exec_batch.argtypes = [_vp, _int, _vp, _vp, _sz, _vp]
     l.ssfft_exec_host.argtypes = [_vp, _int, _vp, _vp]
+    l.ssfft_plan_error.argtypes = [_vp, ctypes.POINTER(ctypes.c_uint)]
     l.ssfft_jit_check.argtypes = [_sz, _int, _int, _sz, ctypes.c_char_p, ctypes.POINTER(_sz)]
     l.ssfft_schedule_info.argtypes = [_sz, _int, _int, _sz, ctypes.POINTER(_int), _int, ctypes.POINTER(_int),
                                       ctypes.POINTER(_int), ctypes.POINTER(_int), ctypes.POINTER(_sz)]
@@ -77,7 +78,7 @@ def _declare(l):
     szp = ctypes.POINTER(_sz)
     l.ssfft_schedule_tables.argtypes = [_sz, _int, _int, _sz, dp, szp, dp, szp, dp, szp, dp, szp]
     for name in ("ssfft_plan_create", "ssfft_plan_destroy", "ssfft_plan_describe", "ssfft_exec", "ssfft_exec_batch",
-                 "ssfft_exec_host", "ssfft_jit_check", "ssfft_schedule_info", "ssfft_schedule_name",
+                 "ssfft_exec_host", "ssfft_plan_error", "ssfft_jit_check", "ssfft_schedule_info", "ssfft_schedule_name",
                  "ssfft_schedule_tables"):
         getattr(l, name).restype = _int
     return l

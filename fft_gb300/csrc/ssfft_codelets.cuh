@@ -33,10 +33,15 @@ struct Args {
 	const void *rtw;     // real split twiddles -i e^{-2 pi i (k or k+1/2)/n_real}, k <= h/2
 	const void *rot;     // half-shift rotations e^{-2 pi i k / n_real}, k < h
 	const void *roots;   // W_R^k for the direct-DFT passes, concatenated
+	unsigned int *err;   // staged kernels: set non-zero when a bounded wait gave up
+	unsigned int spin_limit;  // staged kernels: mbarrier try_wait attempts before giving up
+	unsigned int in_bytes;    // staged kernels: input bytes of one transform (multiple of 16)
 };
 
 enum : int { kComplex = 0, kReal = 1, kRealHalfShift = 2 };
-enum : int { kSmem = 0, kGlobal = 1 };
+// element sources / destinations of a pass: padded shared memory, HBM, or the unpadded staging
+// buffer a bulk copy filled
+enum : int { kSmem = 0, kGlobal = 1, kStage = 2 };
 
 template <typename T>
 struct Cx;
@@ -198,9 +203,23 @@ struct Ctx {
 	const T *gin;  // this transform's input, in scalars
 	T *gout;       // this transform's output, in scalars
 	const C *rot;  // half-shift rotations
+	const C *st;   // staged kernels: this transform's input in the unpadded staging buffer
 	int t;         // thread index inside the transform
 	bool valid;    // the transform exists (the last CTA may be partial)
 };
+
+// Element e of the staged input (same meaning as gload, but from shared memory).
+template <typename T, int KIND, bool CIN, bool COUT>
+__device__ __forceinline__ typename Cx<T>::C sload(const Ctx<T, KIND, CIN, COUT> &c, int e) {
+	using C = typename Cx<T>::C;
+	C v = c.st[e];
+	if constexpr (KIND == kComplex) {
+		return CIN ? conj(v) : v;
+	} else {
+		if constexpr (KIND == kRealHalfShift) v = mul(v, __ldg(c.rot + e));
+		return v;
+	}
+}
 
 // Global element e of the pass input / output, with the conjugation of the inverse and the
 // real packing folded in.
@@ -259,6 +278,7 @@ __device__ __forceinline__ void pass(const Ctx<T, KIND, CIN, COUT> &c, const typ
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
 					if constexpr (SRC == kSmem) v[i][r] = c.sm[pidx<PS>(j + r * NB)];
+					else if constexpr (SRC == kStage) v[i][r] = sload(c, j + r * NB);
 					else v[i][r] = gload<T, KIND, CIN, COUT, ODD>(c, j + r * NB);
 				}
 			}
@@ -302,11 +322,13 @@ __device__ __forceinline__ void pass(const Ctx<T, KIND, CIN, COUT> &c, const typ
 				const int k = e / NB, j = e - (e / NB) * NB, m = j % NS;
 				C s;
 				if constexpr (SRC == kSmem) s = c.sm[pidx<PS>(j)];
+				else if constexpr (SRC == kStage) s = sload(c, j);
 				else s = gload<T, KIND, CIN, COUT, ODD>(c, j);
 				int w = 0;
 				for (int r = 1; r < R; ++r) {
 					C x;
 					if constexpr (SRC == kSmem) x = c.sm[pidx<PS>(j + r * NB)];
+					else if constexpr (SRC == kStage) x = sload(c, j + r * NB);
 					else x = gload<T, KIND, CIN, COUT, ODD>(c, j + r * NB);
 					if constexpr (NS > 1) x = mul(x, __ldg(tw + TWO + (r - 1) * NS + m));
 					w += k;
@@ -341,17 +363,24 @@ struct RootCount {
 	static constexpr int value = Specialised<R>::value ? 0 : R;
 };
 
+struct NoHook {
+	__device__ __forceinline__ void operator()() const {}
+};
+
+// All passes of the transform; `after_first` runs (on every thread) once the first pass has
+// consumed its input.
 template <typename T, int N, int THREADS, int NS, int TWO, int ROOTS, int FIRST_SRC, int LAST_DST, int KIND, bool CIN,
-          bool COUT, bool ODD, int EMAX, int R, int... Rest>
+          bool COUT, bool ODD, int EMAX, int R, int... Rest, class Hook = NoHook>
 __device__ __forceinline__ void passes(const Ctx<T, KIND, CIN, COUT> &c, const typename Cx<T>::C *tw,
-                                       const typename Cx<T>::C *roots) {
+                                       const typename Cx<T>::C *roots, const Hook &after_first = Hook()) {
 	constexpr bool last = sizeof...(Rest) == 0;
 	constexpr int SRC = NS == 1 ? FIRST_SRC : kSmem;
 	constexpr int DST = last ? LAST_DST : kSmem;
 	pass<T, N, THREADS, R, NS, TWO, ROOTS, SRC, DST, KIND, CIN, COUT, ODD, EMAX>(c, tw, roots);
+	if constexpr (NS == 1) after_first();
 	if constexpr (!last)
 		passes<T, N, THREADS, NS * R, TWO + TwCount<R, NS>::value, ROOTS + RootCount<R>::value, FIRST_SRC, LAST_DST,
-		       KIND, CIN, COUT, ODD, EMAX, Rest...>(c, tw, roots);
+		       KIND, CIN, COUT, ODD, EMAX, Rest...>(c, tw, roots, NoHook());
 }
 
 // ------------------------------------------------------------------ real split / merge
@@ -395,24 +424,24 @@ __device__ __forceinline__ void real_post(const Ctx<T, KIND, CIN, COUT> &c, cons
 
 // Inverse pre-twiddle: H bins in HBM -> conj(first-pass input) in shared memory
 // (signalsmith-fft.h:477-492).
-template <typename T, int H, int THREADS, int KIND, bool CIN, bool COUT>
+template <typename T, int H, int THREADS, int KIND, bool CIN, bool COUT, bool STAGED = false>
 __device__ __forceinline__ void real_pre(const Ctx<T, KIND, CIN, COUT> &c, const typename Cx<T>::C *rtw) {
 	using C = typename Cx<T>::C;
 	constexpr int PS = Cx<T>::kPadShift;
 	constexpr bool MOD = KIND == kRealHalfShift;
 	constexpr int S = MOD ? 0 : 1, LAST = H / 2, NPAIRS = LAST - S + 1;
-	const C *in = reinterpret_cast<const C *>(c.gin);
+	const C *in = STAGED ? c.st : reinterpret_cast<const C *>(c.gin);
 	if (c.valid) {
 		if (!MOD && c.t == 0) {
-			const C v = __ldcs(in);
+			const C v = STAGED ? in[0] : __ldcs(in);
 			c.sm[0] = conj(mkc(v.x + v.y, v.x - v.y));
 		}
 #pragma unroll 4
 		for (int p = c.t; p < NPAIRS; p += THREADS) {
 			const int i = S + p;
 			const int ci = MOD ? H - 1 - i : H - i;
-			const C v = __ldcs(in + i);
-			const C v2c = conj(__ldcs(in + ci));
+			const C v = STAGED ? in[i] : __ldcs(in + i);
+			const C v2c = conj(STAGED ? in[ci] : __ldcs(in + ci));
 			const C odd = add(v, v2c);
 			const C even = mulc(sub(v, v2c), __ldg(rtw + i));
 			bool wi, wci;
@@ -451,6 +480,127 @@ __global__ void __launch_bounds__(THREADS *PER_CTA) batch(const Args a) {
 	passes<T, N, THREADS, 1, 0, 0, C2R ? kSmem : kGlobal, R2C ? kSmem : kGlobal, KIND, INV, INV, ODD, EMAX, Rs...>(
 	    c, tw, roots);
 	if constexpr (R2C) real_post<T, N, THREADS, KIND, INV, INV>(c, rtw);
+}
+
+// ------------------------------------------------------------------ asynchronous staging
+
+// Bulk (TMA) copy of a contiguous block into shared memory, completed on an mbarrier.  Under a
+// host emulation (no __CUDA_ARCH__) the copy is synchronous and the barrier a no-op.
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+	unsigned long long a;
+	asm volatile("cvta.to.shared.u64 %0, %1;" : "=l"(a) : "l"(p));
+	return static_cast<unsigned>(a);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+	                 smem_u32(dst)),
+	             "l"(src), "r"(bytes), "r"(smem_u32(bar))
+	             : "memory");
+}
+// generic-proxy reads of the staging buffer must be ordered before the next bulk write into it
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned phase) {
+	unsigned ok;
+	asm volatile(
+	    "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+	    : "=r"(ok)
+	    : "r"(smem_u32(bar)), "r"(phase)
+	    : "memory");
+	return ok != 0;
+}
+#else
+inline void mbar_init(unsigned long long *, unsigned) {}
+inline void bulk_load(void *dst, const void *src, unsigned bytes, unsigned long long *) {
+	const unsigned char *s = static_cast<const unsigned char *>(src);
+	unsigned char *d = static_cast<unsigned char *>(dst);
+	for (unsigned i = 0; i < bytes; ++i) d[i] = s[i];
+}
+inline void fence_async_smem() {}
+inline bool mbar_try_wait(unsigned long long *, unsigned) { return true; }
+#endif
+
+// Wait for phase `phase` of `bar`, giving up after `limit` attempts (each try_wait itself
+// suspends for a bounded, hardware-defined time).
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned phase, unsigned limit) {
+	for (unsigned i = 0; i < limit; ++i)
+		if (mbar_try_wait(bar, phase)) return true;
+	return false;
+}
+
+// The batch kernel with asynchronous input staging: persistent CTAs walk the groups of PER_CTA
+// transforms; each group's input (contiguous in HBM) arrives in an unpadded staging buffer by
+// one bulk copy, and the copy of the next group is issued as soon as the first pass (or the
+// real pre-twiddle) has read the current one, so the HBM load overlaps the remaining passes.
+// Requires in_bytes % 16 == 0 and 16-byte aligned input.  A bounded wait that runs out sets
+// *err and the CTA returns without writing.
+template <typename T, int N, int THREADS, int PER_CTA, int SMEM_STRIDE, int KIND, bool INV, int EMAX, int... Rs>
+__global__ void __launch_bounds__(THREADS *PER_CTA) batch_staged(const Args a) {
+	using C = typename Cx<T>::C;
+	constexpr bool REAL = KIND != kComplex;
+	constexpr bool R2C = REAL && !INV, C2R = REAL && INV;
+	extern __shared__ __align__(128) unsigned char smem_raw[];
+	__shared__ __align__(8) unsigned long long bar;
+	const unsigned in_bytes = a.in_bytes;
+	unsigned char *stage = smem_raw;
+	C *work = reinterpret_cast<C *>(smem_raw + ((PER_CTA * in_bytes + 127u) & ~127u));
+	const long long ngroups = (a.batch + PER_CTA - 1) / PER_CTA;
+	const unsigned char *in = reinterpret_cast<const unsigned char *>(a.in);
+	const int g = threadIdx.x / THREADS;
+	Ctx<T, KIND, INV, INV> c;
+	c.t = threadIdx.x - g * THREADS;
+	c.sm = work + g * SMEM_STRIDE;
+	c.st = reinterpret_cast<const C *>(stage + g * in_bytes);
+	c.rot = reinterpret_cast<const C *>(a.rot);
+	c.gin = nullptr;
+	const C *tw = reinterpret_cast<const C *>(a.tw);
+	const C *roots = reinterpret_cast<const C *>(a.roots);
+	const C *rtw = reinterpret_cast<const C *>(a.rtw);
+	auto issue = [&](long long grp) {
+		const long long nt = a.batch - grp * PER_CTA < PER_CTA ? a.batch - grp * PER_CTA : PER_CTA;
+		bulk_load(stage, in + grp * PER_CTA * (long long)in_bytes, (unsigned)(nt * in_bytes), &bar);
+	};
+	if (threadIdx.x == 0) {
+		mbar_init(&bar, 1);
+		if (blockIdx.x < ngroups) issue(blockIdx.x);
+	}
+	__syncthreads();
+	unsigned phase = 0;
+	for (long long grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+		const bool ok = mbar_wait_bounded(&bar, phase, a.spin_limit);
+		if (__syncthreads_or(!ok)) {
+			if (threadIdx.x == 0) atomicOr(a.err, 1u);
+			mbar_wait_bounded(&bar, phase, a.spin_limit);  // let the copy in flight land
+			return;
+		}
+		phase ^= 1u;
+		const long long gi = grp * PER_CTA + g;
+		c.valid = gi < a.batch;
+		c.gout = reinterpret_cast<T *>(a.out) + (c.valid ? gi * a.out_dist : 0);
+		const long long next = grp + gridDim.x;
+		auto refill = [&]() {
+			__syncthreads();  // every thread has read the staging buffer
+			if (threadIdx.x == 0 && next < ngroups) {
+				fence_async_smem();
+				issue(next);
+			}
+		};
+		if constexpr (C2R) {
+			real_pre<T, N, THREADS, KIND, INV, INV, true>(c, rtw);
+			refill();
+			passes<T, N, THREADS, 1, 0, 0, kSmem, kGlobal, KIND, INV, INV, false, EMAX, Rs...>(c, tw, roots);
+		} else {
+			passes<T, N, THREADS, 1, 0, 0, kStage, R2C ? kSmem : kGlobal, KIND, INV, INV, false, EMAX, Rs...>(c, tw, roots,
+			                                                                                                refill);
+		}
+		if constexpr (R2C) real_post<T, N, THREADS, KIND, INV, INV>(c, rtw);
+		__syncthreads();  // the work buffer is reused by the next group
+	}
 }
 
 // ------------------------------------------------------------------ multi-pass (four-step) kernel

@@ -29,6 +29,8 @@ struct Schedule {
 	int smem_stride = 0;      // padded complex slots per transform
 	int kind = 0;             // ssfft_cl::kComplex / kReal / kRealHalfShift
 	bool odd = false;         // real length is odd (scalar loads/stores)
+	bool staged = false;      // ssfft_cl::batch_staged (bulk-copy input staging, persistent CTAs)
+	unsigned in_bytes = 0;    // staged: input bytes of one transform
 	size_t smem_bytes = 0;
 	int cta_threads() const { return threads * per_cta; }
 	std::string name(bool inverse) const;
@@ -43,6 +45,8 @@ struct SubPlan {
 	Schedule sch;
 	Tables tab;
 	CUfunction fwd = nullptr, inv = nullptr;
+	int grid_cap = 0;        // staged: resident CTAs (persistent grid)
+	unsigned *err = nullptr; // staged: device error word
 };
 
 // Multi-pass (four-step) schedule for transforms longer than one CTA holds; see ssfft_large.cu.
@@ -81,7 +85,7 @@ ssfft_status cuda_fail(cudaError_t e, const char *what);
 // roots of unity, schedules and tables
 void unit_root(unsigned long long k, unsigned long long L, double *re, double *im);
 bool choose_radices(int n, std::vector<int> &radices);
-bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, Schedule &s);
+bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, Schedule &s, bool allow_staged = true);
 void schedule_twiddles(const Schedule &s, std::vector<double> &tw, std::vector<double> &roots);
 size_t device_smem_limit(int dev);
 
@@ -92,6 +96,7 @@ ssfft_status jit_compile_only(const std::vector<std::string> &names, const std::
 ssfft_status jit_launch(CUfunction f, unsigned grid, unsigned block, size_t smem, cudaStream_t stream, void *args);
 ssfft_status jit_launch_grid(CUfunction f, unsigned grid_x, unsigned grid_y, unsigned block, size_t smem,
                              cudaStream_t stream, void *args);
+int jit_occupancy(CUfunction f, int block, size_t smem);
 const char *jit_last_log();
 
 // plans

@@ -46,6 +46,7 @@ struct Driver {
 	CUresult (*launchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, CUstream,
 	                         void **, void **) = nullptr;
 	CUresult (*getErrorString)(CUresult, const char **) = nullptr;
+	CUresult (*occupancy)(int *, CUfunction, int, size_t) = nullptr;
 	bool ok = false;
 };
 
@@ -69,7 +70,8 @@ const Driver &driver() {
 		d.ok = resolve("cuModuleLoadData", d.moduleLoadData) && resolve("cuModuleUnload", d.moduleUnload) &&
 		       resolve("cuModuleGetFunction", d.moduleGetFunction) &&
 		       resolve("cuFuncSetAttribute", d.funcSetAttribute) && resolve("cuLaunchKernel", d.launchKernel) &&
-		       resolve("cuGetErrorString", d.getErrorString);
+		       resolve("cuGetErrorString", d.getErrorString) &&
+		       resolve("cuOccupancyMaxActiveBlocksPerMultiprocessor", d.occupancy);
 		g_drv = d;
 	});
 	return g_drv;
@@ -279,6 +281,9 @@ loaded:
 	for (CUfunction f : fns) {
 		CUresult r = drv.funcSetAttribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem_bytes);
 		if (r != CUDA_SUCCESS) return cu_fail(r, "cuFuncSetAttribute");
+		// prefer the largest shared-memory carveout so smem, not the L1 split, bounds occupancy
+		r = drv.funcSetAttribute(f, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, 100);
+		if (r != CUDA_SUCCESS) return cu_fail(r, "cuFuncSetAttribute(carveout)");
 	}
 	return SSFFT_SUCCESS;
 }
@@ -299,6 +304,12 @@ ssfft_status jit_launch_grid(CUfunction f, unsigned grid_x, unsigned grid_y, uns
 	    driver().launchKernel(f, grid_x, grid_y, 1, block, 1, 1, (unsigned)smem, (CUstream)stream, params, nullptr);
 	if (r != CUDA_SUCCESS) return cu_fail(r, "cuLaunchKernel");
 	return SSFFT_SUCCESS;
+}
+
+int jit_occupancy(CUfunction f, int block, size_t smem) {
+	int n = 0;
+	if (!driver().occupancy || driver().occupancy(&n, f, block, smem) != CUDA_SUCCESS) return 1;
+	return n > 0 ? n : 1;
 }
 
 ssfft_status jit_launch(CUfunction f, unsigned grid, unsigned block, size_t smem, cudaStream_t stream, void *args) {

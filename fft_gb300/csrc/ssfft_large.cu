@@ -144,7 +144,7 @@ static ssfft_status large_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind,
 		const long long Fi = F[i], R = L / Fi, Q = N / L;
 		const bool last = i == P - 1;
 		Schedule s;
-		if (!make_schedule(dtype, (int)Fi, 0, false, 1, s)) return SSFFT_ERR_UNSUPPORTED;
+		if (!make_schedule(dtype, (int)Fi, 0, false, 1, s, false)) return SSFFT_ERR_UNSUPPORTED;
 		// G sub-transforms per CTA: 128-256 B segments, <= 1024 threads, <= ~100 KiB smem
 		const long long U0 = last ? F[0] : R;
 		int G = (int)std::min<long long>(kGroup, U0);

@@ -155,7 +155,7 @@ size_t device_smem_limit(int dev) {
 }
 
 // Threads per transform, transforms per CTA and shared memory for n points.
-bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, Schedule &s) {
+bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, Schedule &s, bool allow_staged) {
 	s = Schedule();
 	s.dtype = dtype;
 	s.n = n;
@@ -186,15 +186,31 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	s.smem_bytes = (size_t)s.per_cta * per;
 	// a single-pass complex transform never touches shared memory
 	if (kind == 0 && s.radices.size() == 1) s.smem_bytes = 0;
+	// Staged input (bulk copies into shared memory, persistent CTAs) when one transform's input is
+	// a whole number of 16-byte units and a group of them fits the copy and shared-memory limits.
+	const size_t sb = eb / 2;
+	const size_t in_bytes = kind == 0 ? (size_t)n * eb : (size_t)2 * n * sb;  // real: n_real = 2h reals or h bins
+	if (allow_staged && !odd && in_bytes % 16 == 0 && n >= 16) {
+		int gs = s.per_cta;
+		auto staged_smem = [&](int gg) { return (((size_t)gg * in_bytes + 127) & ~(size_t)127) + (size_t)gg * per; };
+		while (gs > 1 && staged_smem(gs) > 76 * 1024) --gs;
+		if ((size_t)gs * in_bytes < (1u << 20) && staged_smem(gs) <= 200 * 1024) {
+			s.staged = true;
+			s.per_cta = gs;
+			s.in_bytes = (unsigned)in_bytes;
+			s.smem_bytes = staged_smem(gs);
+		}
+	}
 	return true;
 }
 
 std::string Schedule::name(bool inverse) const {
-	std::string r = "ssfft_cl::batch<";
+	std::string r = staged ? "ssfft_cl::batch_staged<" : "ssfft_cl::batch<";
 	r += dtype == SSFFT_F32 ? "float" : "double";
 	r += ", " + std::to_string(n) + ", " + std::to_string(threads) + ", " + std::to_string(per_cta) + ", " +
-	     std::to_string(smem_stride) + ", " + std::to_string(kind) + ", " + (inverse ? "true" : "false") + ", " +
-	     (odd ? "true" : "false") + ", " + std::to_string(kElemsPerThread);
+	     std::to_string(smem_stride) + ", " + std::to_string(kind) + ", " + (inverse ? "true" : "false") + ", ";
+	if (!staged) r += std::string(odd ? "true" : "false") + ", ";
+	r += std::to_string(kElemsPerThread);
 	for (int x : radices) r += ", " + std::to_string(x);
 	r += ">";
 	return r;
@@ -244,7 +260,7 @@ static bool single_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t
 	const size_t cn = real ? n / 2 : n;
 	const int max_n = dtype == SSFFT_F32 ? kMaxSubTransform : kMaxSubTransform / 2;
 	if (cn == 0 || cn > (size_t)max_n) return false;
-	return make_schedule(dtype, (int)cn, kind_code(kind), real && (n & 1), batch, s);
+	return make_schedule(dtype, (int)cn, kind_code(kind), real && (n & 1), batch, s, true);
 }
 
 // FP64 tables of a single-CTA schedule: pass twiddles, direct-pass roots, and for real kinds
@@ -283,7 +299,8 @@ static ssfft_status plan_build_single(Plan *p) {
 	const size_t off_roots = align_up(off_tw + tw.size() * sb, 256);
 	const size_t off_rtw = align_up(off_roots + roots.size() * sb, 256);
 	const size_t off_rot = align_up(off_rtw + rtw.size() * sb, 256);
-	const size_t total = std::max<size_t>(256, align_up(off_rot + rot.size() * sb, 256));
+	const size_t off_err = align_up(off_rot + rot.size() * sb, 256);
+	const size_t total = align_up(off_err + 16, 256);
 	std::vector<unsigned char> blob(total, 0);
 	if (sb == 4) {
 		put_table<float>(blob, off_tw, tw);
@@ -306,12 +323,20 @@ static ssfft_status plan_build_single(Plan *p) {
 	p->main.tab.roots = base + off_roots;
 	p->main.tab.rtw = base + off_rtw;
 	p->main.tab.rot = base + off_rot;
+	p->main.err = reinterpret_cast<unsigned *>(static_cast<unsigned char *>(p->d_tables) + off_err);
 
 	std::vector<CUfunction> fns;
 	ssfft_status st = jit_kernels({s.name(false), s.name(true)}, s.smem_bytes, fns);
 	if (st != SSFFT_SUCCESS) return st;
 	p->main.fwd = fns[0];
 	p->main.inv = fns[1];
+	if (s.staged) {
+		int sms = 0;
+		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
+		const int occ = std::min(jit_occupancy(fns[0], s.cta_threads(), s.smem_bytes),
+		                         jit_occupancy(fns[1], s.cta_threads(), s.smem_bytes));
+		p->main.grid_cap = std::max(1, occ) * std::max(1, sms);
+	}
 	p->launches_per_exec = 1;
 	return SSFFT_SUCCESS;
 }
@@ -342,10 +367,18 @@ size_t plan_out_bytes(const Plan *p, int inverse, size_t batch) {
 	return (size_t)dout * batch * (p->dtype == SSFFT_F32 ? 4 : 8);
 }
 
-ssfft_status launch_batch(const Plan *p, int inverse, const void *in, void *out, size_t batch, cudaStream_t s) {
-	if (batch == 0) return SSFFT_SUCCESS;
-	const Schedule &sch = p->main.sch;
+// A staged plan given an input that is not 16-byte aligned runs the plain kernel of the same
+// schedule (compiled on first use).
+static ssfft_status launch_unstaged(const Plan *p, int inverse, const void *in, void *out, size_t batch,
+                                    cudaStream_t s) {
+	const Schedule &st = p->main.sch;
+	Schedule u;
+	if (!make_schedule(st.dtype, st.n, st.kind, st.odd, p->batch, u, false)) return SSFFT_ERR_UNSUPPORTED;
+	std::vector<CUfunction> fns;
+	ssfft_status rc = jit_kernels({u.name(false), u.name(true)}, u.smem_bytes, fns);
+	if (rc != SSFFT_SUCCESS) return rc;
 	ssfft_cl::Args a;
+	std::memset(&a, 0, sizeof a);
 	a.in = in;
 	a.out = out;
 	a.batch = (long long)batch;
@@ -354,7 +387,32 @@ ssfft_status launch_batch(const Plan *p, int inverse, const void *in, void *out,
 	a.rtw = p->main.tab.rtw;
 	a.rot = p->main.tab.rot;
 	a.roots = p->main.tab.roots;
-	const long long grid = ((long long)batch + sch.per_cta - 1) / sch.per_cta;
+	const long long grid = ((long long)batch + u.per_cta - 1) / u.per_cta;
+	if (grid > 0x7fffffffLL) return SSFFT_ERR_INVALID_SIZE;
+	return jit_launch(inverse ? fns[1] : fns[0], (unsigned)grid, (unsigned)u.cta_threads(), u.smem_bytes, s, &a);
+}
+
+ssfft_status launch_batch(const Plan *p, int inverse, const void *in, void *out, size_t batch, cudaStream_t s) {
+	if (batch == 0) return SSFFT_SUCCESS;
+	const Schedule &sch = p->main.sch;
+	ssfft_cl::Args a;
+	std::memset(&a, 0, sizeof a);
+	a.in = in;
+	a.out = out;
+	a.batch = (long long)batch;
+	plan_dists(p, inverse, a.in_dist, a.out_dist);
+	a.tw = p->main.tab.tw;
+	a.rtw = p->main.tab.rtw;
+	a.rot = p->main.tab.rot;
+	a.roots = p->main.tab.roots;
+	a.err = p->main.err;
+	a.spin_limit = 1u << 22;
+	a.in_bytes = sch.in_bytes;
+	long long grid = ((long long)batch + sch.per_cta - 1) / sch.per_cta;
+	if (sch.staged) {
+		if ((uintptr_t)in % 16) return launch_unstaged(p, inverse, in, out, batch, s);
+		grid = std::min<long long>(grid, p->main.grid_cap);
+	}
 	if (grid > 0x7fffffffLL) return SSFFT_ERR_INVALID_SIZE;
 	return jit_launch(inverse ? p->main.inv : p->main.fwd, (unsigned)grid, (unsigned)sch.cta_threads(),
 	                  sch.smem_bytes, s, &a);
@@ -482,6 +540,18 @@ ssfft_status ssfft_exec_batch(ssfft_plan_t plan, int inverse, const void *d_in, 
 	cudaStream_t s = static_cast<cudaStream_t>(stream);
 	if (p->large) return launch_large(p, inverse, d_in, d_out, batch, s);
 	return launch_batch(p, inverse, d_in, d_out, batch, s);
+}
+
+ssfft_status ssfft_plan_error(ssfft_plan_t plan, unsigned *flags) {
+	if (!plan || !flags) return SSFFT_ERR_INVALID_VALUE;
+	Plan *p = reinterpret_cast<Plan *>(plan);
+	*flags = 0;
+	if (!p->main.err) return SSFFT_SUCCESS;
+	cudaError_t e = cudaMemcpy(flags, p->main.err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+	if (e != cudaSuccess) return cuda_fail(e, "plan_error read");
+	e = cudaMemset(p->main.err, 0, sizeof(unsigned));
+	if (e != cudaSuccess) return cuda_fail(e, "plan_error clear");
+	return *flags ? SSFFT_ERR_TIMEOUT : SSFFT_SUCCESS;
 }
 
 ssfft_status ssfft_exec(ssfft_plan_t plan, int inverse, const void *d_in, void *d_out, void *stream) {

@@ -95,6 +95,11 @@ ssfft_status ssfft_exec(ssfft_plan_t plan, int inverse, const void *d_in, void *
 /* As ssfft_exec for the first `batch` (<= plan batch) transforms only. */
 ssfft_status ssfft_exec_batch(ssfft_plan_t plan, int inverse, const void *d_in, void *d_out, size_t batch,
                               void *stream);
+/* Device-side failure report: the staged kernels bound every wait on their bulk copies; a wait
+ * that runs out sets a per-plan flag instead of hanging.  Reads and clears it (synchronises the
+ * device); returns SSFFT_ERR_TIMEOUT and *flags != 0 if a launch gave up.  No reference
+ * counterpart (the reference reports no errors). */
+ssfft_status ssfft_plan_error(ssfft_plan_t plan, unsigned *flags);
 /* Host-memory variant of FFT<V>::fft / ifft: `h_in` / `h_out` are host buffers (pinned or
  * pageable).  The batch is cut into chunks whose host->device copy, transform and device->host
  * copy overlap on internal streams; returns when h_out is complete. */

@@ -34,10 +34,28 @@ inline void __stcs(T *p, T v) { *p = v; }
 struct EmuIdx {
 	unsigned x = 0, y = 0, z = 0;
 };
-extern thread_local EmuIdx threadIdx, blockIdx;
+extern thread_local EmuIdx threadIdx, blockIdx, gridDim;
 extern thread_local std::barrier<> *emu_barrier;
 inline void __syncthreads() { emu_barrier->arrive_and_wait(); }
 
 namespace ssfft_cl {
 extern unsigned char smem_raw[];
+}
+
+// __syncthreads_or / atomicOr for the staged kernels
+#include <atomic>
+extern std::atomic<int> emu_or_acc;
+inline int __syncthreads_or(int pred) {
+	if (pred) emu_or_acc.fetch_or(1);
+	__syncthreads();
+	const int r = emu_or_acc.load();
+	__syncthreads();
+	if (threadIdx.x == 0) emu_or_acc.store(0);
+	__syncthreads();
+	return r;
+}
+inline unsigned atomicOr(unsigned *p, unsigned v) {
+	unsigned old = *p;
+	*p |= v;
+	return old;
 }

@@ -1,7 +1,7 @@
 // tests/emu/emu_main.cpp -- runs one emulated kernel launch.  Compiled together with a generated
 // case table (emu_cases.inc: `{name, &ssfft_cl::batch<...>, cta_threads, smem_bytes},` lines).
 // argv: case index, grid, raw input file, raw output file (pre-filled), table file, batch,
-//       in_dist, out_dist (scalars), scalar bytes.
+//       in_dist, out_dist (scalars), scalar bytes, input bytes per transform (staged kernels).
 // The table file holds tw, roots, rtw, rot back to back in the kernel's dtype, preceded by four
 // uint64 element counts (scalars).
 #include "cuda_emu.h"
@@ -14,8 +14,9 @@
 #include <thread>
 #include <vector>
 
-thread_local EmuIdx threadIdx, blockIdx;
+thread_local EmuIdx threadIdx, blockIdx, gridDim;
 thread_local std::barrier<> *emu_barrier;
+std::atomic<int> emu_or_acc{0};
 namespace ssfft_cl {
 alignas(16) unsigned char smem_raw[232 * 1024];
 }
@@ -36,7 +37,7 @@ static std::vector<char> slurp(const char *path) {
 }
 
 int main(int argc, char **argv) {
-	if (argc != 10) return 2;
+	if (argc != 11) return 2;
 	const Case &c = kCases[std::atoi(argv[1])];
 	const int grid = std::atoi(argv[2]);
 	std::vector<char> in = slurp(argv[3]), out = slurp(argv[4]), tab = slurp(argv[5]);
@@ -53,6 +54,10 @@ int main(int argc, char **argv) {
 	a.roots = base + cnt[0] * sb;
 	a.rtw = base + (cnt[0] + cnt[1]) * sb;
 	a.rot = base + (cnt[0] + cnt[1] + cnt[2]) * sb;
+	unsigned err = 0;
+	a.err = &err;
+	a.spin_limit = 1;
+	a.in_bytes = (unsigned)std::atoi(argv[10]);
 	for (int b = 0; b < grid; ++b) {
 		std::barrier<> bar(c.cta_threads);
 		std::vector<std::thread> th;
@@ -61,11 +66,13 @@ int main(int argc, char **argv) {
 			th.emplace_back([&, t, b] {
 				threadIdx.x = (unsigned)t;
 				blockIdx.x = (unsigned)b;
+				gridDim.x = (unsigned)grid;
 				emu_barrier = &bar;
 				c.fn(a);
 			});
 		for (auto &x : th) x.join();
 	}
+	if (err) return 3;
 	std::ofstream f(argv[4], std::ios::binary);
 	f.write(out.data(), (std::streamsize)out.size());
 	return 0;

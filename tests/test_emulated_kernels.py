@@ -23,6 +23,8 @@ CASES = [
     (4096, "f32", "complex", 1, 1),
     (2, "f64", "real", 1, 1), (3, "f64", "real", 2, 2), (7, "f32", "real", 1, 1), (10, "f64", "real", 4, 4),
     (98, "f32", "real", 3, 3), (480, "f32", "real", 5, 5), (3840, "f32", "real", 2, 2),
+    (64, "f32", "complex", 300, 300), (1024, "f64", "complex", 7, 7), (480, "f32", "real", 40, 40),
+    (3840, "f32", "real", 5, 5), (960, "f32", "real_halfshift", 9, 9),
     (2, "f64", "real_halfshift", 1, 1), (4, "f64", "real_halfshift", 2, 2), (9, "f64", "real_halfshift", 1, 1),
     (12, "f32", "real_halfshift", 2, 2), (98, "f64", "real_halfshift", 1, 1), (960, "f32", "real_halfshift", 2, 2),
 ]
@@ -72,9 +74,13 @@ def _run(emulator, n, dt, kind, pb, eb, inv, x):
     fi.write_bytes(xin.tobytes())
     fo.write_bytes(out.tobytes())
     ft.write_bytes(blob)
-    grid = -(-eb // info["per_cta"])
+    groups = -(-eb // info["per_cta"])
+    name = F.schedule_name(n, dt, kind, pb, inv)
+    # persistent (staged) kernels: fewer CTAs than groups, so each CTA walks several groups
+    grid = max(1, groups // 2) if "batch_staged" in name else groups
+    in_bytes = in_dist * np.dtype(sdt).itemsize
     subprocess.run([str(exe), str(ci), str(grid), str(fi), str(fo), str(ft), str(eb), str(in_dist), str(out_dist),
-                    str(np.dtype(sdt).itemsize)], check=True, timeout=300)
+                    str(np.dtype(sdt).itemsize), str(in_bytes)], check=True, timeout=300)
     return np.frombuffer(fo.read_bytes(), dtype=sdt).reshape(eb, out_dist)
 
 

@@ -254,3 +254,28 @@ def test_reference_shaped_api(F):
     assert rel_l2(m.ifft(s), oracle.irfft(s, 480, True)) <= F64_TOL
     t = torch.from_numpy(xr).cuda()
     assert rel_l2(F.rfft(t).cpu().numpy(), oracle.rfft(xr)) <= F64_TOL
+
+
+def test_staged_kernels_report_no_error(F):
+    """The bulk-copy staged kernels bound their waits and report a per-plan flag; after normal
+    runs (aligned and misaligned inputs, partial last group) it must read zero."""
+    rng = np.random.default_rng(12)
+    n, b = 1920, 301
+    x = rng.standard_normal((b, n)).astype(np.float32)
+    p = F.Plan(n, "f32", "real", b)
+    xi = dev(x)
+    out = torch.empty((b, n // 2), dtype=torch.complex64, device="cuda")
+    p.exec(False, xi.data_ptr(), out.data_ptr(), 0)
+    # a 4-byte-offset view of the same data forces the unstaged kernel of the schedule
+    buf = torch.zeros(b * n + 1, dtype=torch.float32, device="cuda")
+    buf[1:] = xi.reshape(-1)
+    out2 = torch.empty_like(out)
+    ctypes_ok = F.lib().ssfft_exec(p.handle, 0, F._vp(buf.data_ptr() + 4), F._vp(out2.data_ptr()), None)
+    torch.cuda.synchronize()
+    assert ctypes_ok == 0
+    import ctypes
+    flags = ctypes.c_uint(99)
+    assert F.lib().ssfft_plan_error(p.handle, ctypes.byref(flags)) == 0 and flags.value == 0
+    ref = np.stack([oracle.rfft(r.astype(np.float64)) for r in x])
+    assert rel_l2(out.cpu().numpy(), ref) <= F32_TOL
+    assert np.array_equal(out.cpu().numpy(), out2.cpu().numpy())
