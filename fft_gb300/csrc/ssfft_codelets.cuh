@@ -177,9 +177,58 @@ __device__ __forceinline__ void dft16(C *v) {
 	for (int k = 0; k < 16; ++k) v[k] = t[k];
 }
 
+// Prime-factor (Good-Thomas) composites R = A * B with gcd(A, B) = 1: input n = (B a + A b) mod R,
+// output k = (B (B^-1 mod A) ka + A (A^-1 mod B) kb) mod R; an A-point DFT over a for each b,
+// then a B-point DFT over b for each ka, with no twiddles in between.  The index maps are
+// register renaming only.
+template <int A>
+struct SmallDft;
+template <>
+struct SmallDft<2> {
+	template <class C>
+	__device__ __forceinline__ static void run(C *v) { dft2(v[0], v[1]); }
+};
+template <>
+struct SmallDft<3> {
+	template <class C>
+	__device__ __forceinline__ static void run(C *v) { dft3(v[0], v[1], v[2]); }
+};
+template <>
+struct SmallDft<4> {
+	template <class C>
+	__device__ __forceinline__ static void run(C *v) { dft4(v[0], v[1], v[2], v[3]); }
+};
+template <>
+struct SmallDft<5> {
+	template <class C>
+	__device__ __forceinline__ static void run(C *v) { dft5(v[0], v[1], v[2], v[3], v[4]); }
+};
+
+template <int A, int B, int KA, int KB, class C>
+__device__ __forceinline__ void dft_pfa(C *v) {
+	constexpr int R = A * B;
+	C t[B][A];
+#pragma unroll
+	for (int b = 0; b < B; ++b) {
+#pragma unroll
+		for (int a = 0; a < A; ++a) t[b][a] = v[(B * a + A * b) % R];
+		SmallDft<A>::run(t[b]);
+	}
+#pragma unroll
+	for (int ka = 0; ka < A; ++ka) {
+		C u[B];
+#pragma unroll
+		for (int b = 0; b < B; ++b) u[b] = t[b][ka];
+		SmallDft<B>::run(u);
+#pragma unroll
+		for (int kb = 0; kb < B; ++kb) v[(KA * ka + KB * kb) % R] = u[kb];
+	}
+}
+
 template <int R>
 struct Specialised {
-	static constexpr bool value = R == 1 || R == 2 || R == 3 || R == 4 || R == 5 || R == 8 || R == 16;
+	static constexpr bool value = R == 1 || R == 2 || R == 3 || R == 4 || R == 5 || R == 6 || R == 8 || R == 10 ||
+	                              R == 12 || R == 15 || R == 16;
 };
 
 template <int R, class C>
@@ -188,7 +237,11 @@ __device__ __forceinline__ void dft(C *v) {
 	else if constexpr (R == 3) dft3(v[0], v[1], v[2]);
 	else if constexpr (R == 4) dft4(v[0], v[1], v[2], v[3]);
 	else if constexpr (R == 5) dft5(v[0], v[1], v[2], v[3], v[4]);
+	else if constexpr (R == 6) dft_pfa<2, 3, 3, 4>(v);     // 3 (3^-1 mod 2), 2 (2^-1 mod 3)
 	else if constexpr (R == 8) dft8(v);
+	else if constexpr (R == 10) dft_pfa<2, 5, 5, 6>(v);    // 5 (5^-1 mod 2), 2 (2^-1 mod 5)
+	else if constexpr (R == 12) dft_pfa<4, 3, 9, 4>(v);    // 3 (3^-1 mod 4), 4 (4^-1 mod 3)
+	else if constexpr (R == 15) dft_pfa<3, 5, 10, 6>(v);   // 5 (5^-1 mod 3), 3 (3^-1 mod 5)
 	else if constexpr (R == 16) dft16(v);
 }
 
@@ -538,9 +591,10 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsig
 // one bulk copy, and the copy of the next group is issued as soon as the first pass (or the
 // real pre-twiddle) has read the current one, so the HBM load overlaps the remaining passes.
 // Requires in_bytes % 16 == 0 and 16-byte aligned input.  A bounded wait that runs out sets
-// *err and the CTA returns without writing.
+// *err and the CTA returns without writing.  (The persistent loop makes the compiler keep far
+// more registers live than one pass needs, so the launch bound asks for two resident CTAs.)
 template <typename T, int N, int THREADS, int PER_CTA, int SMEM_STRIDE, int KIND, bool INV, int EMAX, int... Rs>
-__global__ void __launch_bounds__(THREADS *PER_CTA) batch_staged(const Args a) {
+__global__ void __launch_bounds__(THREADS *PER_CTA, 2) batch_staged(const Args a) {
 	using C = typename Cx<T>::C;
 	constexpr bool REAL = KIND != kComplex;
 	constexpr bool R2C = REAL && !INV, C2R = REAL && INV;

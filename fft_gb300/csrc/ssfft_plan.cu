@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -103,10 +104,38 @@ void unit_root(unsigned long long k, unsigned long long L, double *re, double *i
 
 // ------------------------------------------------------------------ schedules
 
-static bool specialised(int r) { return r == 1 || r == 2 || r == 3 || r == 4 || r == 5 || r == 8 || r == 16; }
+static bool specialised(int r) {
+	return r == 1 || r == 2 || r == 3 || r == 4 || r == 5 || r == 6 || r == 8 || r == 10 || r == 12 || r == 15 ||
+	       r == 16;
+}
 
-// Radix list for an in-CTA transform of n points: powers of two in ceil(a/4) balanced passes of
-// 16/8/4/2, then 3s, then 5s, then the remaining primes (direct passes).
+// Radices for n = 2^a 3^b 5^c * rest: 3 x 5 pairs become radix-15 prime-factor butterflies;
+// with `borrow`, leftover 5s and 3s also take factors of two (10, 12, 6); the remaining powers of
+// two run in ceil(a/4) balanced passes of 16/8/4/2; other primes run direct passes.
+static void radices_for(int a, int b, int c, const std::vector<int> &rest, bool borrow, std::vector<int> &out) {
+	std::vector<int> comp;
+	const int k15 = std::min(b, c);
+	for (int i = 0; i < k15; ++i) comp.push_back(15);
+	b -= k15;
+	c -= k15;
+	if (borrow) {
+		for (; c > 0 && a > 0; --c, --a) comp.push_back(10);
+		for (; b > 0 && a >= 2; --b, a -= 2) comp.push_back(12);
+		for (; b > 0 && a >= 1; --b, --a) comp.push_back(6);
+	}
+	std::vector<int> p2;
+	if (a > 0) {
+		const int passes = (a + 3) / 4;
+		for (int p = 0; p < passes; ++p) p2.push_back(1 << (a / passes + (p < a % passes ? 1 : 0)));
+		std::sort(p2.begin(), p2.end(), [](int x, int y) { return x > y; });
+	}
+	out = p2;
+	out.insert(out.end(), comp.begin(), comp.end());
+	for (; c > 0; --c) out.push_back(5);
+	for (; b > 0; --b) out.push_back(3);
+	out.insert(out.end(), rest.begin(), rest.end());
+}
+
 bool choose_radices(int n, std::vector<int> &radices) {
 	radices.clear();
 	if (n < 1) return false;
@@ -114,36 +143,27 @@ bool choose_radices(int n, std::vector<int> &radices) {
 		radices.push_back(1);
 		return true;
 	}
-	int m = n, a = 0;
-	while (m % 2 == 0) {
-		m /= 2;
-		++a;
-	}
-	if (a > 0) {
-		const int passes = (a + 3) / 4;
-		for (int p = 0; p < passes; ++p) radices.push_back(1 << (a / passes + (p < a % passes ? 1 : 0)));
-		std::sort(radices.begin(), radices.end(), [](int x, int y) { return x > y; });
-	}
-	while (m % 3 == 0) {
-		m /= 3;
-		radices.push_back(3);
-	}
-	while (m % 5 == 0) {
-		m /= 5;
-		radices.push_back(5);
-	}
+	int m = n, a = 0, b = 0, c = 0;
+	while (m % 2 == 0) m /= 2, ++a;
+	while (m % 3 == 0) m /= 3, ++b;
+	while (m % 5 == 0) m /= 5, ++c;
+	std::vector<int> rest;
 	for (int p = 7; m > 1;) {
 		if ((long long)p * p > m) {
-			radices.push_back(m);
+			rest.push_back(m);
 			break;
 		}
 		if (m % p == 0) {
-			radices.push_back(p);
+			rest.push_back(p);
 			m /= p;
 		} else {
 			p += 2;
 		}
 	}
+	std::vector<int> plain, borrowed;
+	radices_for(a, b, c, rest, false, plain);
+	radices_for(a, b, c, rest, true, borrowed);
+	radices = borrowed.size() < plain.size() ? borrowed : plain;
 	return radices.size() <= 24;
 }
 
@@ -190,7 +210,12 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	// a whole number of 16-byte units and a group of them fits the copy and shared-memory limits.
 	const size_t sb = eb / 2;
 	const size_t in_bytes = kind == 0 ? (size_t)n * eb : (size_t)2 * n * sb;  // real: n_real = 2h reals or h bins
-	if (allow_staged && !odd && in_bytes % 16 == 0 && n >= 16) {
+	// Opt-in (SSFFT_STAGED=1): measured slower than the unstaged kernel on GB300 so far.
+	static const bool staged_enabled = [] {
+		const char *e = std::getenv("SSFFT_STAGED");
+		return e && e[0] == '1';
+	}();
+	if (allow_staged && staged_enabled && !odd && in_bytes % 16 == 0 && n >= 16) {
 		int gs = s.per_cta;
 		auto staged_smem = [&](int gg) { return (((size_t)gg * in_bytes + 127) & ~(size_t)127) + (size_t)gg * per; };
 		while (gs > 1 && staged_smem(gs) > 76 * 1024) --gs;
