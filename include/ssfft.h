@@ -105,6 +105,25 @@ ssfft_status ssfft_plan_error(ssfft_plan_t plan, unsigned *flags);
  * copy overlap on internal streams; returns when h_out is complete. */
 ssfft_status ssfft_exec_host(ssfft_plan_t plan, int inverse, const void *h_in, void *h_out);
 
+/* ---------------------------------------------------------------- allocation-free transform
+ * No counterpart in the reference.  For callers that cannot allocate device memory at the moment
+ * they need a transform -- a real-time audio callback that must never block inside the CUDA
+ * allocator, or an application whose own memory manager owns every byte of device memory -- this
+ * computes one complex FP32 transform using only the caller's input and output and a scratch
+ * array of 2^20 complex values (8 MiB) that the library keeps on every GPU that loads it, until
+ * the process exits.  It creates no plan and calls no allocator.
+ *   - n must be 2^a 3^b 5^c and at most ssfft_fft_noalloc_max_size() (= 1048576); larger sizes
+ *     return SSFFT_ERR_INVALID_SIZE, other prime factors SSFFT_ERR_UNSUPPORTED;
+ *   - d_in and d_out are distinct, 8-byte aligned device buffers of n complex floats; inverse != 0
+ *     computes the unnormalised inverse, as ssfft_exec does;
+ *   - the first call on each device looks up the scratch array's device address; make that first
+ *     call before any stream capture;
+ *   - every call uses the same array: calls that can overlap on the GPU (other streams, other
+ *     host threads) race, so the caller must serialise them.  Nothing needs clearing between
+ *     calls: a call reads only scratch values it wrote itself. */
+size_t ssfft_fft_noalloc_max_size(void);
+ssfft_status ssfft_fft_noalloc_f32(const void *d_in, void *d_out, size_t n, int inverse, void *stream);
+
 /* ---------------------------------------------------------------- diagnostics
  * Host-only helpers (no GPU needed) that expose the planner's choices; they have no counterpart
  * in the reference.  ssfft_jit_check compiles the kernels of a single-CTA plan for `arch`

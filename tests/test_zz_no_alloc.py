@@ -1,0 +1,86 @@
+"""The allocation-free entry point ssfft_fft_noalloc_f32, called through the C ABI.
+
+It exists for callers that cannot allocate device memory when they need a transform (a real-time
+thread that must not enter the allocator, a host framework that owns all device memory); its
+only working memory is a fixed array inside the library.  Checked against the plan-based entry
+point (ssfft_plan_create + ssfft_exec) within the FP32 tolerance of the other parity tests, on two
+calls in a row (the shared scratch array keeps the previous call's contents), and the device's
+free memory must not change across calls once the first call has done its set-up.
+
+This file is collected last on purpose, so that a run stopping at its first failure has already
+run every other test."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+F32_TOL = 1e-6
+
+
+@pytest.fixture(scope="module")
+def F():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import fft_gb300
+    l = fft_gb300.lib()
+    l.ssfft_fft_noalloc_f32.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
+                                        ctypes.c_void_p]
+    l.ssfft_fft_noalloc_f32.restype = ctypes.c_int
+    l.ssfft_fft_noalloc_max_size.restype = ctypes.c_size_t
+    return fft_gb300
+
+
+def noalloc(F, xi, out, inverse):
+    rc = F.lib().ssfft_fft_noalloc_f32(xi.data_ptr(), out.data_ptr(), xi.numel(), int(inverse), None)
+    assert rc == 0, F.lib().ssfft_last_cuda_error()
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 16, 1920, 4096, 3 ** 7, 1000, 2 ** 17, 2 ** 20])
+def test_noalloc_matches_plan_entry_point_twice(F, n):
+    rng = np.random.default_rng(n)
+    x = (rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)).astype(np.complex64)
+    xi = torch.from_numpy(x).cuda()
+    for inverse in (False, True):
+        plan = F.Plan(n, "f32", "complex", 1)
+        ref = torch.empty_like(xi)
+        plan.exec(inverse, xi.data_ptr(), ref.data_ptr(), 0)
+        torch.cuda.synchronize()
+        r = ref.cpu().numpy()
+        for _ in range(2):
+            out = torch.full_like(xi, complex(7, 7))
+            noalloc(F, xi, out, inverse)
+            torch.cuda.synchronize()
+            assert rel_l2(out.cpu().numpy(), r) <= F32_TOL, (n, inverse, rel_l2(out.cpu().numpy(), r))
+        assert np.array_equal(xi.cpu().numpy(), x), "input was changed"
+
+
+def test_noalloc_allocates_nothing_per_call(F):
+    n = 2 ** 16
+    xi = torch.randn(n, dtype=torch.complex64, device="cuda")
+    out = torch.empty_like(xi)
+    noalloc(F, xi, out, False)   # first call on the device does the set-up
+    noalloc(F, xi, out, True)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        noalloc(F, xi, out, False)
+        noalloc(F, xi, out, True)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+
+
+def test_noalloc_rejects_sizes_beyond_its_scratch(F):
+    l = F.lib()
+    mx = l.ssfft_fft_noalloc_max_size()
+    assert mx == 2 ** 20
+    x = torch.zeros(8, dtype=torch.complex64, device="cuda")
+    y = torch.zeros(8, dtype=torch.complex64, device="cuda")
+    assert l.ssfft_fft_noalloc_f32(x.data_ptr(), y.data_ptr(), mx + 1, 0, None) == 1      # invalid size
+    assert l.ssfft_fft_noalloc_f32(x.data_ptr(), y.data_ptr(), 0, 0, None) == 1
+    assert l.ssfft_fft_noalloc_f32(x.data_ptr(), y.data_ptr(), 7, 0, None) == 5         # prime 7: unsupported
+    assert l.ssfft_fft_noalloc_f32(x.data_ptr(), x.data_ptr(), 8, 0, None) == 2         # in place refused
