@@ -48,6 +48,10 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the host-buffer leg (default: steps/10)")
+    ap.add_argument("--workload", default="realfft", choices=["realfft", "fp64", "large", "serve"],
+                    help="realfft: the batched RealFFT<float> line (default); fp64: FFT<double> N=1024 x256; "
+                         "large: single FP32 transforms of 2^24, 3^15, 2^12 3^4 5^2; serve: request serving sweep")
+    ap.add_argument("--serve-duration", type=float, default=1.0)
     return ap.parse_args()
 
 
@@ -337,12 +341,120 @@ def run_gpu(args, rank: int, world: int):
         dist.destroy_process_group()
 
 
+def _time_device(fn, steps: int, warmup: int) -> float:
+    """Seconds per call of fn() (launches on the current stream), CUDA events, after warm-up."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / 1e3 / steps
+
+
+def run_fp64(args):
+    """FFT<double> N=1024, 256 transforms, forward then inverse per step, U[-1,1)."""
+    import torch
+    import fft_gb300 as F
+    import oracle
+    n, b = 1024, 256
+    rng = np.random.default_rng(1)
+    x = rng.uniform(-1, 1, (b, n)) + 1j * rng.uniform(-1, 1, (b, n))
+    xi = torch.from_numpy(x).cuda()
+    y = torch.empty_like(xi)
+    z = torch.empty_like(xi)
+    p = F.Plan(n, "f64", "complex", b)
+    sh = int(torch.cuda.current_stream().cuda_stream)
+
+    def step():
+        p.exec(False, xi.data_ptr(), y.data_ptr(), sh)
+        p.exec(True, y.data_ptr(), z.data_ptr(), sh)
+    t = _time_device(step, max(args.steps, 200), max(args.warmup, 5))
+    flops = 2 * b * 5 * n * math.log2(n)
+    ref = np.stack([oracle.fft(r) for r in x])
+    rel = float(np.linalg.norm(y.cpu().numpy() - ref) / np.linalg.norm(ref))
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    reps = 20
+    for _ in range(reps):
+        yy = oracle.batch(x, n, real=False, inverse=False, threads=threads)
+        oracle.batch(yy, n, real=False, inverse=True, threads=threads)
+    tc = (time.perf_counter() - t0) / reps
+    print(json.dumps({"workload": "FFT<double> N=1024 x256, fwd+inv", "value": flops / t / 1e9, "unit": "GFLOP/s",
+                      "ms_per_step": t * 1e3, "GB_s": 2 * 2 * b * n * 16 / t / 1e9, "relL2_vs_oracle": rel,
+                      "cpu_baseline": {"value": flops / tc / 1e9, "unit": "GFLOP/s", "cores": threads, "kind": "port"},
+                      "plan": p.describe()}), flush=True)
+
+
+def run_large(args):
+    """One FP32 complex transform each at 2^24, 3^15, 2^12 3^4 5^2 (forward), U[-1,1)."""
+    import torch
+    import fft_gb300 as F
+    out = []
+    sh = int(torch.cuda.current_stream().cuda_stream)
+    for n in (2 ** 24, 3 ** 15, 2 ** 12 * 3 ** 4 * 5 ** 2):
+        rng = np.random.default_rng(n % 997)
+        x = (rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)).astype(np.complex64)
+        xi = torch.from_numpy(x).cuda()
+        y = torch.empty_like(xi)
+        p = F.Plan(n, "f32", "complex", 1)
+        t = _time_device(lambda: p.exec(False, xi.data_ptr(), y.data_ptr(), sh), 20, 3)
+        alg = 16 * n
+        out.append({"n": n, "ms": t * 1e3, "GFLOP_s": 5 * n * math.log2(n) / t / 1e9, "alg_GB_s": alg / t / 1e9,
+                    "passes": p.describe()["radices"], "launches": p.describe()["launches"]})
+        del xi, y, p
+        torch.cuda.empty_cache()
+    peak, kind = measured_peak_hbm()
+    for o in out:
+        o["frac_of_hbm"] = o["alg_GB_s"] / peak
+    print(json.dumps({"workload": "single large complex FP32 transforms", "results": out, "peak_GB_s": peak,
+                      "peak_source": kind}), flush=True)
+
+
+def run_serve(args):
+    """Open-loop Poisson request stream (1-64 frames of one size, log-uniform over 2^a 3^b 5^c
+    sizes in [256, 65536], 70% real / 30% complex, 50/50 forward/inverse, FP32, 16 GB HBM budget):
+    p50/p99 latency and throughput of the batched server against plain per-request execution."""
+    import fft_gb300 as F
+    loads = [1e4, 1e5, 5e5, 1e6, 2e6]
+    sweep = []
+    batched = F.Server(hbm_budget_bytes=16 << 30, waves=4, max_requests_per_wave=256, coalesce=True)
+    plain = F.Server(hbm_budget_bytes=16 << 30, coalesce=False)
+    for i, rate in enumerate(loads):
+        row = {"offered_transforms_per_s": rate}
+        for name, srv in (("batched", batched), ("plain", plain)):
+            st = srv.loadgen(offered_rate=rate, duration_s=args.serve_duration, seed=100 + i)
+            row[name] = {"p50_us": st["p50_latency_us"], "p99_us": st["p99_latency_us"],
+                         "transforms_per_s": st["frames"] / st["span_seconds"] if st["span_seconds"] else 0,
+                         "GFLOP_s": st["flops"] / st["span_seconds"] / 1e9 if st["span_seconds"] else 0,
+                         "requests": st["completed"], "waves": st["waves"], "launches": st["launches"]}
+        sweep.append(row)
+        print(json.dumps(row), flush=True)
+    best_b = max(r["batched"]["GFLOP_s"] for r in sweep)
+    best_p = max(r["plain"]["GFLOP_s"] for r in sweep)
+    print(json.dumps({"workload": "serving sweep", "metric": METRIC, "value": best_b, "unit": "GFLOP/s",
+                      "plain_value": best_p, "ratio_vs_plain": best_b / best_p if best_p else None,
+                      "p99_us_at_max_load": sweep[-1]["batched"]["p99_us"], "sweep": sweep}), flush=True)
+    batched.close()
+    plain.close()
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload != "realfft":
+        import torch
+        from fft_gb300 import build as fb
+        fb.build()
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        {"fp64": run_fp64, "large": run_large, "serve": run_serve}[args.workload](args)
     else:
         run_gpu(args, rank, world if "WORLD_SIZE" in os.environ else 1)
 

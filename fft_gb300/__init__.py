@@ -446,3 +446,107 @@ class ModifiedRealFFT(RealFFT):
     """signalsmith::ModifiedRealFFT<V> (signalsmith-fft.h:505-508): bins at k + 1/2."""
 
     modified = True
+
+
+# ------------------------------------------------------------------ serving
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_size_t), ("max_waves_in_flight", ctypes.c_int),
+                ("max_requests_per_wave", ctypes.c_int), ("coalesce", ctypes.c_int)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("dtype", ctypes.c_int), ("inverse", ctypes.c_int), ("n", ctypes.c_size_t),
+                ("frames", ctypes.c_size_t), ("h_in", ctypes.c_void_p), ("h_out", ctypes.c_void_p)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("waves", ctypes.c_uint64), ("launches", ctypes.c_uint64), ("p50_latency_us", ctypes.c_double),
+                ("p99_latency_us", ctypes.c_double), ("mean_latency_us", ctypes.c_double),
+                ("max_latency_us", ctypes.c_double), ("span_seconds", ctypes.c_double), ("frames", ctypes.c_double),
+                ("flops", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class LoadgenConfig(ctypes.Structure):
+    _fields_ = [("offered_rate", ctypes.c_double), ("duration_s", ctypes.c_double), ("seed", ctypes.c_uint64),
+                ("n_min", ctypes.c_size_t), ("n_max", ctypes.c_size_t), ("max_frames", ctypes.c_int),
+                ("real_fraction", ctypes.c_double)]
+
+
+def _declare_server(l):
+    if getattr(l, "_server_declared", False):
+        return l
+    l.ssfft_server_create.argtypes = [ctypes.POINTER(_vp), ctypes.POINTER(ServerConfig)]
+    l.ssfft_server_prepare.argtypes = [_vp, _sz, _int, _int]
+    l.ssfft_server_submit.argtypes = [_vp, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]
+    l.ssfft_server_wait.argtypes = [_vp, ctypes.c_uint64, ctypes.c_double]
+    l.ssfft_server_drain.argtypes = [_vp, ctypes.c_double]
+    l.ssfft_server_get_stats.argtypes = [_vp, ctypes.POINTER(ServerStats), _int]
+    l.ssfft_server_destroy.argtypes = [_vp]
+    l.ssfft_server_loadgen.argtypes = [_vp, ctypes.POINTER(LoadgenConfig), ctypes.POINTER(ServerStats)]
+    for name in ("ssfft_server_create", "ssfft_server_prepare", "ssfft_server_submit", "ssfft_server_wait",
+                 "ssfft_server_drain", "ssfft_server_get_stats", "ssfft_server_destroy", "ssfft_server_loadgen"):
+        getattr(l, name).restype = _int
+    l._server_declared = True
+    return l
+
+
+class Server:
+    """Continuous-batching request server (ssfft_server_* in include/ssfft.h)."""
+
+    def __init__(self, hbm_budget_bytes: int = 1 << 30, waves: int = 4, max_requests_per_wave: int = 256,
+                 coalesce: bool = True):
+        l = _declare_server(lib())
+        cfg = ServerConfig(hbm_budget_bytes, waves, max_requests_per_wave, int(bool(coalesce)))
+        h = _vp()
+        check(l.ssfft_server_create(ctypes.byref(h), ctypes.byref(cfg)), "server_create")
+        self._h = h
+        self._keep = {}
+
+    def prepare(self, n: int, dtype="f32", kind="complex") -> None:
+        check(lib().ssfft_server_prepare(self._h, n, _dtype_code(dtype), _kind_code(kind)), "server_prepare")
+
+    def submit(self, n: int, kind, inverse: bool, h_in: np.ndarray, h_out: np.ndarray, frames: int = 1,
+               dtype="f32") -> int:
+        """Queue a request on host arrays (kept alive until the request completes)."""
+        r = Request(_kind_code(kind), _dtype_code(dtype), int(bool(inverse)), n, frames, h_in.ctypes.data,
+                    h_out.ctypes.data)
+        t = ctypes.c_uint64()
+        check(lib().ssfft_server_submit(self._h, ctypes.byref(r), ctypes.byref(t)), "server_submit")
+        self._keep[t.value] = (h_in, h_out)
+        return t.value
+
+    def wait(self, ticket: int, timeout: float = 60.0) -> None:
+        check(lib().ssfft_server_wait(self._h, ticket, timeout), "server_wait")
+        self._keep.pop(ticket, None)
+
+    def drain(self, timeout: float = 600.0) -> None:
+        check(lib().ssfft_server_drain(self._h, timeout), "server_drain")
+        self._keep.clear()
+
+    def stats(self, reset: bool = False) -> dict:
+        st = ServerStats()
+        check(lib().ssfft_server_get_stats(self._h, ctypes.byref(st), int(reset)), "server_stats")
+        return st.as_dict()
+
+    def loadgen(self, offered_rate: float, duration_s: float, seed: int = 1, n_min: int = 256, n_max: int = 65536,
+                max_frames: int = 64, real_fraction: float = 0.7) -> dict:
+        cfg = LoadgenConfig(offered_rate, duration_s, seed, n_min, n_max, max_frames, real_fraction)
+        st = ServerStats()
+        check(lib().ssfft_server_loadgen(self._h, ctypes.byref(cfg), ctypes.byref(st)), "server_loadgen")
+        return st.as_dict()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().ssfft_server_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

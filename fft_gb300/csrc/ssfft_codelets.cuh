@@ -509,10 +509,12 @@ __device__ __forceinline__ void real_pre(const Ctx<T, KIND, CIN, COUT> &c, const
 
 // ------------------------------------------------------------------ the batch kernel
 
-// SMEM_STRIDE: padded complex slots per transform.  EMAX bounds registers per thread.
+// SMEM_STRIDE: padded complex slots per transform.  EMAX bounds the values a thread holds in
+// one pass.  MINB: CTAs the compiler must fit per SM (caps registers; more resident warps hide the
+// first pass's HBM latency).
 template <typename T, int N, int THREADS, int PER_CTA, int SMEM_STRIDE, int KIND, bool INV, bool ODD, int EMAX,
-          int... Rs>
-__global__ void __launch_bounds__(THREADS *PER_CTA) batch(const Args a) {
+          int MINB, int... Rs>
+__global__ void __launch_bounds__(THREADS *PER_CTA, MINB) batch(const Args a) {
 	using C = typename Cx<T>::C;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	constexpr bool REAL = KIND != kComplex;
@@ -591,14 +593,15 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsig
 // one bulk copy, and the copy of the next group is issued as soon as the first pass (or the
 // real pre-twiddle) has read the current one, so the HBM load overlaps the remaining passes.
 // Requires in_bytes % 16 == 0 and 16-byte aligned input.  A bounded wait that runs out sets
-// *err and the CTA returns without writing.  (The persistent loop makes the compiler keep far
-// more registers live than one pass needs, so the launch bound asks for two resident CTAs.)
-template <typename T, int N, int THREADS, int PER_CTA, int SMEM_STRIDE, int KIND, bool INV, int EMAX, int... Rs>
-__global__ void __launch_bounds__(THREADS *PER_CTA, 2) batch_staged(const Args a) {
+// *err and the CTA returns without writing.  (Inside the persistent loop the compiler keeps far
+// more registers live than one pass needs; MINB caps them.)
+template <typename T, int N, int THREADS, int PER_CTA, int SMEM_STRIDE, int KIND, bool INV, int EMAX, int MINB,
+          int... Rs>
+__global__ void __launch_bounds__(THREADS *PER_CTA, MINB) batch_staged(const Args a) {
 	using C = typename Cx<T>::C;
 	constexpr bool REAL = KIND != kComplex;
 	constexpr bool R2C = REAL && !INV, C2R = REAL && INV;
-	extern __shared__ __align__(128) unsigned char smem_raw[];
+	extern __shared__ __align__(16) unsigned char smem_raw[];
 	__shared__ __align__(8) unsigned long long bar;
 	const unsigned in_bytes = a.in_bytes;
 	unsigned char *stage = smem_raw;

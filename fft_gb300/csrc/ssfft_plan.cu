@@ -226,6 +226,19 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 			s.smem_bytes = staged_smem(gs);
 		}
 	}
+	// Register cap: aim at ~48 resident warps per SM (1536 threads), never below what the shared
+	// memory allows anyway, and at most 2 CTAs for the staged kernel (whose loop needs more).
+	static const int minb_env = [] {
+		const char *e = std::getenv("SSFFT_MINB");
+		return e ? std::atoi(e) : 0;
+	}();
+	const int cta = s.cta_threads();
+	int mb = std::max(1, 1536 / cta);
+	const size_t smem_cta = s.smem_bytes + 1024;
+	if (s.smem_bytes) mb = std::min<int>(mb, std::max<size_t>(1, (228 * 1024) / smem_cta));
+	if (s.staged) mb = std::min(mb, 2);
+	if (minb_env > 0) mb = minb_env;
+	s.minb = std::max(1, mb);
 	return true;
 }
 
@@ -235,7 +248,7 @@ std::string Schedule::name(bool inverse) const {
 	r += ", " + std::to_string(n) + ", " + std::to_string(threads) + ", " + std::to_string(per_cta) + ", " +
 	     std::to_string(smem_stride) + ", " + std::to_string(kind) + ", " + (inverse ? "true" : "false") + ", ";
 	if (!staged) r += std::string(odd ? "true" : "false") + ", ";
-	r += std::to_string(kElemsPerThread);
+	r += std::to_string(kElemsPerThread) + ", " + std::to_string(minb);
 	for (int x : radices) r += ", " + std::to_string(x);
 	r += ">";
 	return r;

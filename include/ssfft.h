@@ -105,6 +105,69 @@ ssfft_status ssfft_plan_error(ssfft_plan_t plan, unsigned *flags);
  * copy overlap on internal streams; returns when h_out is complete. */
 ssfft_status ssfft_exec_host(ssfft_plan_t plan, int inverse, const void *h_in, void *h_out);
 
+/* ---------------------------------------------------------------- serving (continuous batching)
+ * No reference counterpart: the reference transforms one buffer per call.  A server takes
+ * fft/ifft requests of mixed sizes and kinds from many callers (e.g. audio blocks from many
+ * streams), admits each against an HBM budget for its device buffers, and executes admitted
+ * requests in waves: a wave groups its requests by (n, dtype, kind, direction), copies inputs in,
+ * runs one batched launch per group, copies outputs back, on its own stream; several waves are
+ * in flight at once, so requests arriving while others run are admitted as buffers and wave
+ * slots free up.  A request's result does not depend on what it was batched with (the kernel of
+ * a given shape computes every transform identically). */
+typedef struct ssfft_server_s *ssfft_server_t;
+
+typedef struct {
+	size_t hbm_budget_bytes;   /* device arena for in-flight request buffers (0: 1 GiB) */
+	int max_waves_in_flight;   /* concurrent waves, one stream each (0: 4) */
+	int max_requests_per_wave; /* (0: 256) */
+	int coalesce;              /* 1: batched waves; 0: plain, one request at a time, synchronously */
+} ssfft_server_config;
+
+typedef struct {
+	ssfft_kind kind;
+	ssfft_dtype dtype;
+	int inverse;
+	size_t n;          /* transform size (real length for real kinds) */
+	size_t frames;     /* transforms in this request, stored back to back */
+	const void *h_in;  /* host input (pinned memory overlaps best); valid until completion */
+	void *h_out;       /* host output; valid until completion */
+} ssfft_request;
+
+typedef struct {
+	uint64_t submitted, completed, failed, waves, launches;
+	double p50_latency_us, p99_latency_us, mean_latency_us, max_latency_us;
+	double span_seconds;   /* first submit to last completion */
+	double frames;         /* transforms completed */
+	double flops;          /* 5 n log2 n per complex, 2.5 n log2 n per real transform completed */
+} ssfft_server_stats;
+
+ssfft_status ssfft_server_create(ssfft_server_t *srv, const ssfft_server_config *cfg);
+/* Build (compile) the plan of one request shape ahead of traffic. */
+ssfft_status ssfft_server_prepare(ssfft_server_t srv, size_t n, ssfft_dtype dtype, ssfft_kind kind);
+/* Queue a request (non-blocking); SSFFT_ERR_BUDGET if it alone exceeds the HBM budget. */
+ssfft_status ssfft_server_submit(ssfft_server_t srv, const ssfft_request *req, uint64_t *ticket);
+/* Wait for one request (SSFFT_ERR_TIMEOUT after timeout_seconds; its result status otherwise).
+ * Tickets stay valid until a million newer requests have been submitted. */
+ssfft_status ssfft_server_wait(ssfft_server_t srv, uint64_t ticket, double timeout_seconds);
+/* Wait until every submitted request has completed. */
+ssfft_status ssfft_server_drain(ssfft_server_t srv, double timeout_seconds);
+ssfft_status ssfft_server_get_stats(ssfft_server_t srv, ssfft_server_stats *stats, int reset);
+ssfft_status ssfft_server_destroy(ssfft_server_t srv);
+
+/* Synthetic open-loop load for measurement: Poisson arrivals at `offered_rate` transforms/s for
+ * `duration_s`, each request 1..max_frames frames of one size drawn log-uniformly from the
+ * 2^a 3^b 5^c sizes in [n_min, n_max], real with probability real_fraction, inverse with
+ * probability 1/2, FP32, N(0,1) inputs from pinned host memory.  Fills *stats over the run. */
+typedef struct {
+	double offered_rate;
+	double duration_s;
+	uint64_t seed;
+	size_t n_min, n_max;
+	int max_frames;
+	double real_fraction;
+} ssfft_loadgen_config;
+ssfft_status ssfft_server_loadgen(ssfft_server_t srv, const ssfft_loadgen_config *cfg, ssfft_server_stats *stats);
+
 /* ---------------------------------------------------------------- allocation-free transform
  * No counterpart in the reference.  For callers that cannot allocate device memory at the moment
  * they need a transform -- a real-time audio callback that must never block inside the CUDA
