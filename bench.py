@@ -48,10 +48,12 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the host-buffer leg (default: steps/10)")
-    ap.add_argument("--workload", default="realfft", choices=["realfft", "fp64", "large", "serve"],
+    ap.add_argument("--workload", default="realfft", choices=["realfft", "fp64", "large", "serve", "uneven"],
                     help="realfft: the batched RealFFT<float> line (default); fp64: FFT<double> N=1024 x256; "
                          "large: single FP32 transforms of 2^24, 3^15, 2^12 3^4 5^2; serve: request serving sweep")
     ap.add_argument("--serve-duration", type=float, default=1.0)
+    ap.add_argument("--streams", type=int, default=1,
+                    help="run each size's forward->inverse chain on its own stream (1..4)")
     return ap.parse_args()
 
 
@@ -200,6 +202,11 @@ def run_gpu(args, rank: int, world: int):
     frames = args.frames
     stream = torch.cuda.current_stream()
     sh = int(stream.cuda_stream)
+    # independent size chains may run on side streams (forked from / joined to the main stream)
+    nstreams = max(1, min(args.streams, len(SIZES)))
+    side = [stream] + [torch.cuda.Stream() for _ in range(nstreams - 1)]
+    fork_ev = torch.cuda.Event()
+    join_ev = [torch.cuda.Event() for _ in side]
 
     # buffers and plans (outside the timed region)
     plans, xs, specs, backs = [], [], [], []
@@ -213,17 +220,27 @@ def run_gpu(args, rank: int, world: int):
 
     def step(evs=None):
         k = 0
-        for p, x, s, b in zip(plans, xs, specs, backs):
+        if nstreams > 1:
+            fork_ev.record(stream)
+            for st in side[1:]:
+                st.wait_event(fork_ev)
+        for i, (p, x, s, b) in enumerate(zip(plans, xs, specs, backs)):
+            st = side[i % nstreams]
+            h = int(st.cuda_stream)
             if evs is not None:
-                evs[k][0].record(stream)
-            p.exec(False, x.data_ptr(), s.data_ptr(), sh)
+                evs[k][0].record(st)
+            p.exec(False, x.data_ptr(), s.data_ptr(), h)
             if evs is not None:
-                evs[k][1].record(stream)
-                evs[k + 1][0].record(stream)
-            p.exec(True, s.data_ptr(), b.data_ptr(), sh)
+                evs[k][1].record(st)
+                evs[k + 1][0].record(st)
+            p.exec(True, s.data_ptr(), b.data_ptr(), h)
             if evs is not None:
-                evs[k + 1][1].record(stream)
+                evs[k + 1][1].record(st)
             k += 2
+        if nstreams > 1:
+            for st, ev in zip(side[1:], join_ev[1:]):
+                ev.record(st)
+                stream.wait_event(ev)
 
     for _ in range(max(3, args.warmup)):
         step()
@@ -324,7 +341,7 @@ def run_gpu(args, rank: int, world: int):
             "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "RealFFT<float> N in {480,960,1920,3840}, 16384 frames each, fwd+inv",
-                       "frames": frames, "parallelism": f"replicas x{world}",
+                       "frames": frames, "parallelism": f"replicas x{world}", "streams": nstreams,
                        "l2": "each step streams ~1.9 GB (> 129 MB L2), no flush"},
             "gpu_launches": nl * args.steps,
             "relL2_vs_fp64_oracle": rel,
@@ -443,6 +460,48 @@ def run_serve(args):
     plain.close()
 
 
+def run_uneven(args):
+    """One submission of 32768 complex FP32 transforms, sizes log-uniform over the 175 sizes
+    2^a 3^b 5^c in [64, 16384], U[-1,1): the CUDA-graph batch against one plain launch per size."""
+    import torch
+    import fft_gb300 as F
+    import oracle
+    rng = np.random.default_rng(4)
+    pool = np.array(F.fast_sizes(64, 16384))
+    lg = rng.uniform(np.log(64), np.log(16384), 32768)
+    sizes = pool[np.abs(np.log(pool)[None, :] - lg[:, None]).argmin(axis=1)].tolist()
+    total = int(sum(sizes))
+    x = torch.empty(total, dtype=torch.complex64, device="cuda")
+    x.real.uniform_(-1, 1)
+    x.imag.uniform_(-1, 1)
+    y = torch.empty_like(x)
+    t0 = time.perf_counter()
+    m = F.Multi(sizes, "f32")
+    build_s = time.perf_counter() - t0
+    sh = int(torch.cuda.current_stream().cuda_stream)
+    tg = _time_device(lambda: m.exec(False, x.data_ptr(), y.data_ptr(), sh), max(args.steps // 4, 50), 5)
+    tp = _time_device(lambda: m.exec_plain(False, x.data_ptr(), y.data_ptr(), sh), max(args.steps // 4, 50), 5)
+    flops = sum(5 * n * math.log2(n) for n in sizes)
+    alg = 16 * total
+    m.exec(False, x.data_ptr(), y.data_ptr(), sh)
+    torch.cuda.synchronize()
+    xs, ys = x.cpu().numpy(), y.cpu().numpy()
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    worst = 0.0
+    for i in range(0, 32768, 512):
+        a, b = offs[i], offs[i + 1]
+        ref = oracle.fft(xs[a:b].astype(np.complex128))
+        worst = max(worst, float(np.linalg.norm(ys[a:b] - ref) / np.linalg.norm(ref)))
+    peak, kind = measured_peak_hbm()
+    print(json.dumps({"workload": "32768 complex FP32 transforms, uneven sizes in [64,16384]",
+                      "distinct_sizes": m.info()["distinct_sizes"], "alg_bytes": alg,
+                      "graph": {"ms": tg * 1e3, "GFLOP_s": flops / tg / 1e9, "alg_GB_s": alg / tg / 1e9,
+                                "frac_of_hbm": alg / tg / 1e9 / peak},
+                      "plain_per_size": {"ms": tp * 1e3, "GFLOP_s": flops / tp / 1e9, "alg_GB_s": alg / tp / 1e9},
+                      "speedup_vs_plain": tp / tg, "plan_build_s": build_s, "worst_relL2_sampled": worst,
+                      "split_bf16_variant": "not built (see DESIGN.md)"}), flush=True)
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -454,7 +513,7 @@ def main():
         from fft_gb300 import build as fb
         fb.build()
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        {"fp64": run_fp64, "large": run_large, "serve": run_serve}[args.workload](args)
+        {"fp64": run_fp64, "large": run_large, "serve": run_serve, "uneven": run_uneven}[args.workload](args)
     else:
         run_gpu(args, rank, world if "WORLD_SIZE" in os.environ else 1)
 

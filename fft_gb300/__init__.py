@@ -550,3 +550,67 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+# ------------------------------------------------------------------ uneven-size batches
+
+def fast_sizes(lo: int, hi: int) -> list:
+    """The 2^a 3^b 5^c sizes in [lo, hi], ascending."""
+    out = []
+    a = 1
+    while a <= hi:
+        b = a
+        while b <= hi:
+            c = b
+            while c <= hi:
+                if c >= lo:
+                    out.append(c)
+                c *= 5
+            b *= 3
+        a *= 2
+    return sorted(out)
+
+
+class Multi:
+    """ssfft_multi_*: one submission of complex transforms of uneven sizes stored back to back."""
+
+    def __init__(self, sizes, dtype="f32"):
+        l = lib()
+        if not getattr(l, "_multi_declared", False):
+            l.ssfft_multi_create.argtypes = [ctypes.POINTER(_vp), ctypes.POINTER(_sz), _sz, _int]
+            l.ssfft_multi_exec.argtypes = [_vp, _int, _vp, _vp, _vp]
+            l.ssfft_multi_exec_plain.argtypes = [_vp, _int, _vp, _vp, _vp]
+            l.ssfft_multi_info.argtypes = [_vp, ctypes.POINTER(_sz), ctypes.POINTER(_sz)]
+            l.ssfft_multi_destroy.argtypes = [_vp]
+            for name in ("ssfft_multi_create", "ssfft_multi_exec", "ssfft_multi_exec_plain", "ssfft_multi_info",
+                         "ssfft_multi_destroy"):
+                getattr(l, name).restype = _int
+            l._multi_declared = True
+        self.sizes = [int(n) for n in sizes]
+        arr = (_sz * len(self.sizes))(*self.sizes)
+        h = _vp()
+        check(l.ssfft_multi_create(ctypes.byref(h), arr, len(self.sizes), _dtype_code(dtype)), "multi_create")
+        self._h = h
+
+    def exec(self, inverse: bool, d_in: int, d_out: int, stream: int = 0) -> None:
+        check(lib().ssfft_multi_exec(self._h, int(bool(inverse)), _vp(d_in), _vp(d_out), _vp(stream)), "multi_exec")
+
+    def exec_plain(self, inverse: bool, d_in: int, d_out: int, stream: int = 0) -> None:
+        check(lib().ssfft_multi_exec_plain(self._h, int(bool(inverse)), _vp(d_in), _vp(d_out), _vp(stream)),
+              "multi_exec_plain")
+
+    def info(self) -> dict:
+        a, b = _sz(), _sz()
+        check(lib().ssfft_multi_info(self._h, ctypes.byref(a), ctypes.byref(b)), "multi_info")
+        return {"distinct_sizes": a.value, "total_elements": b.value}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().ssfft_multi_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -36,6 +36,7 @@ struct Args {
 	unsigned int *err;   // staged kernels: set non-zero when a bounded wait gave up
 	unsigned int spin_limit;  // staged kernels: mbarrier try_wait attempts before giving up
 	unsigned int in_bytes;    // staged kernels: input bytes of one transform (multiple of 16)
+	const long long *offs;    // batch kernel: if set, transform g starts offs[g] scalars into in and out
 };
 
 enum : int { kComplex = 0, kReal = 1, kRealHalfShift = 2 };
@@ -525,8 +526,13 @@ __global__ void __launch_bounds__(THREADS *PER_CTA, MINB) batch(const Args a) {
 	c.t = threadIdx.x - g * THREADS;
 	c.valid = gi < a.batch;
 	c.sm = reinterpret_cast<C *>(smem_raw) + g * SMEM_STRIDE;
-	c.gin = reinterpret_cast<const T *>(a.in) + (c.valid ? gi * a.in_dist : 0);
-	c.gout = reinterpret_cast<T *>(a.out) + (c.valid ? gi * a.out_dist : 0);
+	long long oin = 0, oout = 0;
+	if (c.valid) {
+		if (a.offs) oin = oout = a.offs[gi];
+		else oin = gi * a.in_dist, oout = gi * a.out_dist;
+	}
+	c.gin = reinterpret_cast<const T *>(a.in) + oin;
+	c.gout = reinterpret_cast<T *>(a.out) + oout;
 	c.rot = reinterpret_cast<const C *>(a.rot);
 	const C *tw = reinterpret_cast<const C *>(a.tw);
 	const C *roots = reinterpret_cast<const C *>(a.roots);

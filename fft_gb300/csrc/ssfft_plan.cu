@@ -197,8 +197,14 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	if (s.smem_stride % 2 == 0) s.smem_stride += 1;  // neighbouring transforms start on other banks
 	const size_t per = (size_t)s.smem_stride * eb;
 	if (per > 227 * 1024) return false;
-	// about 256 threads per CTA, at most 48 KiB of shared memory unless one transform needs more
-	int g = std::max(1, 256 / t);
+	// about 256 threads per CTA (SSFFT_CTA_THREADS overrides), at most 48 KiB of shared memory
+	// unless one transform needs more
+	static const int cta_target = [] {
+		const char *e = std::getenv("SSFFT_CTA_THREADS");
+		const int v = e ? std::atoi(e) : 0;
+		return v > 0 ? v : 256;
+	}();
+	int g = std::max(1, cta_target / t);
 	const size_t soft = std::max<size_t>(per, 48 * 1024);
 	while (g > 1 && (size_t)g * per > soft) --g;
 	if (batch > 0 && (size_t)g > batch) g = (int)batch;
@@ -226,17 +232,14 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 			s.smem_bytes = staged_smem(gs);
 		}
 	}
-	// Register cap: aim at ~48 resident warps per SM (1536 threads), never below what the shared
-	// memory allows anyway, and at most 2 CTAs for the staged kernel (whose loop needs more).
 	static const int minb_env = [] {
 		const char *e = std::getenv("SSFFT_MINB");
 		return e ? std::atoi(e) : 0;
 	}();
-	const int cta = s.cta_threads();
-	int mb = std::max(1, 1536 / cta);
-	const size_t smem_cta = s.smem_bytes + 1024;
-	if (s.smem_bytes) mb = std::min<int>(mb, std::max<size_t>(1, (228 * 1024) / smem_cta));
-	if (s.staged) mb = std::min(mb, 2);
+	// Measured on GB300: forcing more resident CTAs (register caps with small spills) did not
+	// beat the compiler's own allocation for the plain kernel; the staged kernel's loop needs a
+	// cap of two CTAs.  SSFFT_MINB overrides for experiments.
+	int mb = s.staged ? 2 : 1;
 	if (minb_env > 0) mb = minb_env;
 	s.minb = std::max(1, mb);
 	return true;
@@ -408,7 +411,7 @@ size_t plan_out_bytes(const Plan *p, int inverse, size_t batch) {
 // A staged plan given an input that is not 16-byte aligned runs the plain kernel of the same
 // schedule (compiled on first use).
 static ssfft_status launch_unstaged(const Plan *p, int inverse, const void *in, void *out, size_t batch,
-                                    cudaStream_t s) {
+                                    cudaStream_t s, const long long *offs = nullptr) {
 	const Schedule &st = p->main.sch;
 	Schedule u;
 	if (!make_schedule(st.dtype, st.n, st.kind, st.odd, p->batch, u, false)) return SSFFT_ERR_UNSUPPORTED;
@@ -425,9 +428,34 @@ static ssfft_status launch_unstaged(const Plan *p, int inverse, const void *in, 
 	a.rtw = p->main.tab.rtw;
 	a.rot = p->main.tab.rot;
 	a.roots = p->main.tab.roots;
+	a.offs = offs;
 	const long long grid = ((long long)batch + u.per_cta - 1) / u.per_cta;
 	if (grid > 0x7fffffffLL) return SSFFT_ERR_INVALID_SIZE;
 	return jit_launch(inverse ? fns[1] : fns[0], (unsigned)grid, (unsigned)u.cta_threads(), u.smem_bytes, s, &a);
+}
+
+// Transforms at scattered offsets (d_offs[g] scalars into in and out), for uneven-size batches.
+ssfft_status launch_batch_offs(const Plan *p, int inverse, const void *in, void *out, size_t batch,
+                               const long long *d_offs, cudaStream_t s) {
+	if (batch == 0) return SSFFT_SUCCESS;
+	if (p->large) return SSFFT_ERR_UNSUPPORTED;
+	if (p->main.sch.staged) return launch_unstaged(p, inverse, in, out, batch, s, d_offs);
+	const Schedule &sch = p->main.sch;
+	ssfft_cl::Args a;
+	std::memset(&a, 0, sizeof a);
+	a.in = in;
+	a.out = out;
+	a.batch = (long long)batch;
+	plan_dists(p, inverse, a.in_dist, a.out_dist);
+	a.tw = p->main.tab.tw;
+	a.rtw = p->main.tab.rtw;
+	a.rot = p->main.tab.rot;
+	a.roots = p->main.tab.roots;
+	a.offs = d_offs;
+	const long long grid = ((long long)batch + sch.per_cta - 1) / sch.per_cta;
+	if (grid > 0x7fffffffLL) return SSFFT_ERR_INVALID_SIZE;
+	return jit_launch(inverse ? p->main.inv : p->main.fwd, (unsigned)grid, (unsigned)sch.cta_threads(),
+	                  sch.smem_bytes, s, &a);
 }
 
 ssfft_status launch_batch(const Plan *p, int inverse, const void *in, void *out, size_t batch, cudaStream_t s) {

@@ -105,6 +105,21 @@ ssfft_status ssfft_plan_error(ssfft_plan_t plan, unsigned *flags);
  * copy overlap on internal streams; returns when h_out is complete. */
 ssfft_status ssfft_exec_host(ssfft_plan_t plan, int inverse, const void *h_in, void *h_out);
 
+/* ---------------------------------------------------------------- uneven-size batches
+ * No single reference counterpart (the reference's FFT object has one size; a caller with many
+ * sizes loops over objects).  `count` independent complex transforms of sizes sizes[i] (each at
+ * most 16384 points FP32 / 8192 FP64), stored back to back: transform i starts at the sum of the
+ * sizes before it (complex elements).  ssfft_multi_exec runs them all as one CUDA graph launch
+ * (one size-specialised launch per distinct size, on parallel branches, captured once per
+ * input/output/direction); ssfft_multi_exec_plain runs the same launches one after another on
+ * `stream`. */
+typedef struct ssfft_multi_s *ssfft_multi_t;
+ssfft_status ssfft_multi_create(ssfft_multi_t *multi, const size_t *sizes, size_t count, ssfft_dtype dtype);
+ssfft_status ssfft_multi_exec(ssfft_multi_t multi, int inverse, const void *d_in, void *d_out, void *stream);
+ssfft_status ssfft_multi_exec_plain(ssfft_multi_t multi, int inverse, const void *d_in, void *d_out, void *stream);
+ssfft_status ssfft_multi_info(ssfft_multi_t multi, size_t *distinct_sizes, size_t *total_elements);
+ssfft_status ssfft_multi_destroy(ssfft_multi_t multi);
+
 /* ---------------------------------------------------------------- serving (continuous batching)
  * No reference counterpart: the reference transforms one buffer per call.  A server takes
  * fft/ifft requests of mixed sizes and kinds from many callers (e.g. audio blocks from many

@@ -44,7 +44,7 @@ int main(int argc, char **argv) {
 	const size_t sb = (size_t)std::atoi(argv[9]);
 	const uint64_t *cnt = reinterpret_cast<const uint64_t *>(tab.data());
 	const char *base = tab.data() + 4 * sizeof(uint64_t);
-	ssfft_cl::Args a;
+	ssfft_cl::Args a{};
 	a.in = in.data();
 	a.out = out.data();
 	a.batch = std::atoll(argv[6]);
