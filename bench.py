@@ -52,7 +52,7 @@ def parse():
                     help="realfft: the batched RealFFT<float> line (default); fp64: FFT<double> N=1024 x256; "
                          "large: single FP32 transforms of 2^24, 3^15, 2^12 3^4 5^2; serve: request serving sweep")
     ap.add_argument("--serve-duration", type=float, default=1.0)
-    ap.add_argument("--streams", type=int, default=1,
+    ap.add_argument("--streams", type=int, default=4,
                     help="run each size's forward->inverse chain on its own stream (1..4)")
     return ap.parse_args()
 
@@ -140,6 +140,26 @@ def measured_peak_hbm() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
+def max_over_ranks(seconds: float, dist=None, device: str = "cpu") -> float:
+    """The slowest rank's time (replicas: the job ends when the last rank does)."""
+    if dist is None:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def traffic_for(kernel: str):
+    """DRAM bytes per launch (read + write) of `kernel` from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f).get(kernel)
+    except Exception:
+        return None
+
+
 def cpu_leg(frames: int, threads: int, kind: str = "port", seed: int = 7) -> dict:
     """Time the reference algorithm on the host cores: forward + inverse of every size over
     `frames` frames, one plan instance per thread."""
@@ -218,14 +238,15 @@ def run_gpu(args, rank: int, world: int):
         plans.append(F.Plan(n, "f32", "real", frames))
     nl = len(SIZES) * 2
 
-    def step(evs=None):
+    def step(evs=None, ns=None):
+        ns = nstreams if ns is None else ns
         k = 0
-        if nstreams > 1:
+        if ns > 1:
             fork_ev.record(stream)
-            for st in side[1:]:
+            for st in side[1:ns]:
                 st.wait_event(fork_ev)
         for i, (p, x, s, b) in enumerate(zip(plans, xs, specs, backs)):
-            st = side[i % nstreams]
+            st = side[i % ns]
             h = int(st.cuda_stream)
             if evs is not None:
                 evs[k][0].record(st)
@@ -237,8 +258,8 @@ def run_gpu(args, rank: int, world: int):
             if evs is not None:
                 evs[k + 1][1].record(st)
             k += 2
-        if nstreams > 1:
-            for st, ev in zip(side[1:], join_ev[1:]):
+        if ns > 1:
+            for st, ev in zip(side[1:ns], join_ev[1:ns]):
                 ev.record(st)
                 stream.wait_event(ev)
 
@@ -246,9 +267,6 @@ def run_gpu(args, rank: int, world: int):
         step()
     torch.cuda.synchronize()
 
-    # per-launch CUDA events on the launching stream: one set per step, summed afterwards
-    evsets = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nl)]
-              for _ in range(args.steps)]
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.25)
@@ -259,25 +277,28 @@ def run_gpu(args, rank: int, world: int):
     t1 = torch.cuda.Event(enable_timing=True)
     t0.record(stream)
     for k in range(args.steps):
-        step(evsets[k])
+        step()
     t1.record(stream)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     clk = clocks.stop()
-    elapsed = t0.elapsed_time(t1) / 1e3
-    if dist:
-        tt = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        elapsed = float(tt.item())
+    elapsed = max_over_ranks(t0.elapsed_time(t1) / 1e3, dist, "cuda")
     value = flops_per_step(frames) * args.steps * world / elapsed / 1e9
 
-    # per-kernel durations
+    # per-kernel durations: a sequential pass (one stream, CUDA events around every launch), so
+    # that each kernel is timed alone for the roofline
+    rsteps = max(20, args.steps // 4)
+    evsets = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nl)]
+              for _ in range(rsteps)]
+    for k in range(rsteps):
+        step(evsets[k], ns=1)
+    torch.cuda.synchronize()
     kt = np.zeros(nl)
     for evs in evsets:
         for j, (a, b) in enumerate(evs):
             kt[j] += a.elapsed_time(b) / 1e3
-    kt /= args.steps
+    kt /= rsteps
     names, alg = [], []
     for n in SIZES:
         for d in ("r2c", "c2r"):
@@ -289,7 +310,7 @@ def run_gpu(args, rank: int, world: int):
     kernels = {names[j]: {"ms": round(kt[j] * 1e3, 4), "GB_s": round(alg[j] / kt[j] / 1e9, 1),
                           "frac": round(alg[j] / kt[j] / 1e9 / peak, 3)} for j in range(nl)}
     agg_bytes = sum(alg)
-    agg_gbs = agg_bytes / kt.sum() / 1e9
+    agg_gbs = agg_bytes / (elapsed / args.steps) / 1e9 / world
 
     # numerics spot check of what was timed
     import oracle
@@ -303,10 +324,17 @@ def run_gpu(args, rank: int, world: int):
     hback = [torch.empty(b.shape, dtype=b.dtype).pin_memory() for b in backs]
     lib = F.lib()
 
+    from concurrent.futures import ThreadPoolExecutor
+    pool = ThreadPoolExecutor(max_workers=len(SIZES))
+
+    def chain(p, a, s, b):
+        # one size: host frames -> bins -> host frames, through the C ABI's host-buffer entry point
+        F.check(lib.ssfft_exec_host(p.handle, 0, a.data_ptr(), s.data_ptr()), "exec_host")
+        F.check(lib.ssfft_exec_host(p.handle, 1, s.data_ptr(), b.data_ptr()), "exec_host")
+
     def e2e_step():
-        for p, a, s, b in zip(plans, hin, hspec, hback):
-            F.check(lib.ssfft_exec_host(p.handle, 0, a.data_ptr(), s.data_ptr()), "exec_host")
-            F.check(lib.ssfft_exec_host(p.handle, 1, s.data_ptr(), b.data_ptr()), "exec_host")
+        # the four sizes are independent jobs: one host thread each (distinct plans are thread-safe)
+        list(pool.map(lambda args: chain(*args), zip(plans, hin, hspec, hback)))
 
     for _ in range(2):
         e2e_step()
@@ -315,11 +343,8 @@ def run_gpu(args, rank: int, world: int):
     te = time.perf_counter()
     for _ in range(e2e_steps):
         e2e_step()
-    te = time.perf_counter() - te
-    if dist:
-        tt = torch.tensor([te], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        te = float(tt.item())
+    te = max_over_ranks(time.perf_counter() - te, dist, "cuda")
+    pool.shutdown()
     h2d = sum(a.numel() * 4 for a in hin) + sum(s.numel() * 8 for s in hspec)
     d2h = sum(s.numel() * 8 for s in hspec) + sum(b.numel() * 4 for b in hback)
     e2e = {"value": flops_per_step(frames) * e2e_steps * world / te / 1e9, "unit": "GFLOP/s",
@@ -346,10 +371,13 @@ def run_gpu(args, rank: int, world: int):
             "gpu_launches": nl * args.steps,
             "relL2_vs_fp64_oracle": rel,
             "roofline": {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": peak,
-                         "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                         "alg_bytes_per_launch": alg[top], "aggregate_GB_s": agg_gbs},
+                         "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic_for(names[top]), "alg_bytes_per_launch": alg[top],
+                         "timing": "kernel alone: sequential pass, CUDA events per launch",
+                         "aggregate_GB_s": agg_gbs, "aggregate_frac": agg_gbs / peak},
             "kernels": kernels,
             "e2e": e2e,
+            "gpu_launches_note": "per step: forward + inverse of each of the 4 sizes, one launch each",
             "cpu_baseline": cpu,
             "clocks": clk,
         }

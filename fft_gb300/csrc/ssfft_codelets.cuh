@@ -149,6 +149,30 @@ __device__ __forceinline__ void dft8(C *v) {
 	v[7] = sub(e3, o3);
 }
 
+// 9 = 3 x 3: DFT3 over n1 of x[3 n1 + n2], twiddle W9^{n2 k1}, DFT3 over n2, transpose.
+template <class C>
+__device__ __forceinline__ void dft9(C *v) {
+	using S = decltype(v[0].x);
+	const S c1 = S(0.76604444311897803520), s1 = S(0.64278760968653932632);  // cos, sin 2 pi/9
+	const S c2 = S(0.17364817766693034885), s2 = S(0.98480775301220805936);  // cos, sin 4 pi/9
+	const S c4 = S(-0.93969262078590838405), s4 = S(0.34202014332566873304); // cos, sin 8 pi/9
+#pragma unroll
+	for (int n2 = 0; n2 < 3; ++n2) dft3(v[n2], v[n2 + 3], v[n2 + 6]);
+	v[4] = mul(v[4], mkc(c1, -s1));  // W9^1
+	v[7] = mul(v[7], mkc(c2, -s2));  // W9^2
+	v[5] = mul(v[5], mkc(c2, -s2));  // W9^2
+	v[8] = mul(v[8], mkc(c4, -s4));  // W9^4
+#pragma unroll
+	for (int k1 = 0; k1 < 3; ++k1) dft3(v[3 * k1], v[3 * k1 + 1], v[3 * k1 + 2]);
+	C t[9];
+#pragma unroll
+	for (int k1 = 0; k1 < 3; ++k1)
+#pragma unroll
+		for (int k2 = 0; k2 < 3; ++k2) t[k1 + 3 * k2] = v[3 * k1 + k2];
+#pragma unroll
+	for (int k = 0; k < 9; ++k) v[k] = t[k];
+}
+
 // 16 = 4 x 4: DFT4 over n1 of x[4 n1 + n2], twiddle W16^{n2 k1}, DFT4 over n2, transpose.
 template <class C>
 __device__ __forceinline__ void dft16(C *v) {
@@ -228,8 +252,8 @@ __device__ __forceinline__ void dft_pfa(C *v) {
 
 template <int R>
 struct Specialised {
-	static constexpr bool value = R == 1 || R == 2 || R == 3 || R == 4 || R == 5 || R == 6 || R == 8 || R == 10 ||
-	                              R == 12 || R == 15 || R == 16;
+	static constexpr bool value = R == 1 || R == 2 || R == 3 || R == 4 || R == 5 || R == 6 || R == 8 || R == 9 ||
+	                              R == 10 || R == 12 || R == 15 || R == 16;
 };
 
 template <int R, class C>
@@ -240,6 +264,7 @@ __device__ __forceinline__ void dft(C *v) {
 	else if constexpr (R == 5) dft5(v[0], v[1], v[2], v[3], v[4]);
 	else if constexpr (R == 6) dft_pfa<2, 3, 3, 4>(v);     // 3 (3^-1 mod 2), 2 (2^-1 mod 3)
 	else if constexpr (R == 8) dft8(v);
+	else if constexpr (R == 9) dft9(v);
 	else if constexpr (R == 10) dft_pfa<2, 5, 5, 6>(v);    // 5 (5^-1 mod 2), 2 (2^-1 mod 5)
 	else if constexpr (R == 12) dft_pfa<4, 3, 9, 4>(v);    // 3 (3^-1 mod 4), 4 (4^-1 mod 3)
 	else if constexpr (R == 15) dft_pfa<3, 5, 10, 6>(v);   // 5 (5^-1 mod 3), 3 (3^-1 mod 5)

@@ -31,6 +31,7 @@ struct Schedule {
 	bool odd = false;         // real length is odd (scalar loads/stores)
 	bool staged = false;      // ssfft_cl::batch_staged (bulk-copy input staging, persistent CTAs)
 	int minb = 1;             // launch-bound CTAs per SM (register cap)
+	int emax = 16;            // complex values a thread holds in one pass
 	unsigned in_bytes = 0;    // staged: input bytes of one transform
 	size_t smem_bytes = 0;
 	int cta_threads() const { return threads * per_cta; }

@@ -57,7 +57,7 @@ std::string LargePass::name(bool inverse, bool first, bool last, int rot) const 
 	r += sub.dtype == SSFFT_F32 ? "float" : "double";
 	r += ", " + std::to_string(sub.n) + ", " + std::to_string(sub.threads) + ", " + std::to_string(sub.per_cta) + ", " +
 	     std::to_string(sub.smem_stride) + ", " + (cin ? "true" : "false") + ", " + (cout ? "true" : "false") + ", " +
-	     std::to_string(kElemsPerThread) + ", " + (sload ? "true" : "false") + ", " + (sstore ? "true" : "false") +
+	     std::to_string(sub.emax) + ", " + (sload ? "true" : "false") + ", " + (sstore ? "true" : "false") +
 	     ", " + std::to_string(twn) + "LL, " + std::to_string(lb) + ", " + std::to_string(rot);
 	for (int x : sub.radices) r += ", " + std::to_string(x);
 	r += ">";

@@ -156,6 +156,8 @@ ssfft_status ssfft_multi_create(ssfft_multi_t *out, const size_t *sizes, size_t 
 		});
 	for (auto &x : th) x.join();
 	if (bad) return SSFFT_ERR_UNSUPPORTED;
+	for (auto &g : m->groups)  // every size must run in one CTA (offset-table launches)
+		if (reinterpret_cast<const Plan *>(g.plan)->large) return SSFFT_ERR_UNSUPPORTED;
 	for (auto &g : m->groups) {
 		const auto &offs = by_size[g.n];
 		e = cudaMalloc(&g.d_offs, offs.size() * sizeof(long long));

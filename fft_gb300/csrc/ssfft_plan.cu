@@ -105,13 +105,14 @@ void unit_root(unsigned long long k, unsigned long long L, double *re, double *i
 // ------------------------------------------------------------------ schedules
 
 static bool specialised(int r) {
-	return r == 1 || r == 2 || r == 3 || r == 4 || r == 5 || r == 6 || r == 8 || r == 10 || r == 12 || r == 15 ||
-	       r == 16;
+	return r == 1 || r == 2 || r == 3 || r == 4 || r == 5 || r == 6 || r == 8 || r == 9 || r == 10 || r == 12 ||
+	       r == 15 || r == 16;
 }
 
 // Radices for n = 2^a 3^b 5^c * rest: 3 x 5 pairs become radix-15 prime-factor butterflies;
-// with `borrow`, leftover 5s and 3s also take factors of two (10, 12, 6); the remaining powers of
-// two run in ceil(a/4) balanced passes of 16/8/4/2; other primes run direct passes.
+// with `borrow`, leftover 5s and 3s also take factors of two (10, 12, 6); leftover 3s pair into
+// radix 9; the remaining powers of two run in ceil(a/4) balanced passes of 16/8/4/2; other primes
+// run direct passes.
 static void radices_for(int a, int b, int c, const std::vector<int> &rest, bool borrow, std::vector<int> &out) {
 	std::vector<int> comp;
 	const int k15 = std::min(b, c);
@@ -132,6 +133,7 @@ static void radices_for(int a, int b, int c, const std::vector<int> &rest, bool 
 	out = p2;
 	out.insert(out.end(), comp.begin(), comp.end());
 	for (; c > 0; --c) out.push_back(5);
+	for (; b >= 2; b -= 2) out.push_back(9);
 	for (; b > 0; --b) out.push_back(3);
 	out.insert(out.end(), rest.begin(), rest.end());
 }
@@ -182,13 +184,24 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	s.kind = kind;
 	s.odd = odd;
 	if (!choose_radices(n, s.radices)) return false;
-	int t = 1;
-	for (int r : s.radices) {
-		const int per = r == 1 ? 1 : kElemsPerThread / r;  // butterflies a thread holds
-		const int need = specialised(r) ? (n / r + per - 1) / per : (n + kElemsPerThread - 1) / kElemsPerThread;
-		t = std::max(t, need);
+	// threads per transform: every pass must fit its butterflies into `emax` values per thread;
+	// 16 normally, 32 when 16 would need more than one CTA's threads (long sizes whose composite
+	// radices hold a single butterfly per thread)
+	auto threads_for = [&](int emax) {
+		int t = 1;
+		for (int r : s.radices) {
+			const int per = r == 1 ? 1 : std::max(1, emax / r);  // butterflies a thread holds
+			const int need = specialised(r) ? (n / r + per - 1) / per : (n + emax - 1) / emax;
+			t = std::max(t, need);
+		}
+		return t;
+	};
+	s.emax = kElemsPerThread;
+	int t = threads_for(s.emax);
+	if (t > kMaxCtaThreads) {
+		s.emax = 2 * kElemsPerThread;
+		t = threads_for(s.emax);
 	}
-	// real transforms also split/merge h/2 pairs; keep at least a warp's worth of threads busy
 	if (t > kMaxCtaThreads) return false;
 	s.threads = t;
 	const size_t eb = dtype == SSFFT_F32 ? 8 : 16;
@@ -197,12 +210,12 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	if (s.smem_stride % 2 == 0) s.smem_stride += 1;  // neighbouring transforms start on other banks
 	const size_t per = (size_t)s.smem_stride * eb;
 	if (per > 227 * 1024) return false;
-	// about 256 threads per CTA (SSFFT_CTA_THREADS overrides), at most 48 KiB of shared memory
+	// about 128 threads per CTA (SSFFT_CTA_THREADS overrides), at most 48 KiB of shared memory
 	// unless one transform needs more
 	static const int cta_target = [] {
 		const char *e = std::getenv("SSFFT_CTA_THREADS");
 		const int v = e ? std::atoi(e) : 0;
-		return v > 0 ? v : 256;
+		return v > 0 ? v : 128;  // 128 measured best on GB300 (vs 256 / 512)
 	}();
 	int g = std::max(1, cta_target / t);
 	const size_t soft = std::max<size_t>(per, 48 * 1024);
@@ -251,7 +264,7 @@ std::string Schedule::name(bool inverse) const {
 	r += ", " + std::to_string(n) + ", " + std::to_string(threads) + ", " + std::to_string(per_cta) + ", " +
 	     std::to_string(smem_stride) + ", " + std::to_string(kind) + ", " + (inverse ? "true" : "false") + ", ";
 	if (!staged) r += std::string(odd ? "true" : "false") + ", ";
-	r += std::to_string(kElemsPerThread) + ", " + std::to_string(minb);
+	r += std::to_string(emax) + ", " + std::to_string(minb);
 	for (int x : radices) r += ", " + std::to_string(x);
 	r += ">";
 	return r;

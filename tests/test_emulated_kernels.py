@@ -25,6 +25,7 @@ CASES = [
     (240, "f32", "complex", 2, 2), (1024, "f64", "complex", 2, 2), (1920, "f32", "complex", 1, 1),
     (4096, "f32", "complex", 1, 1), (50, "f64", "complex", 3, 3), (36, "f32", "complex", 5, 5),
     (18, "f64", "complex", 2, 2), (2880, "f32", "complex", 3, 3), (200, "f64", "real", 3, 3),
+    (81, "f64", "complex", 3, 3), (2187, "f32", "complex", 2, 2), (486, "f64", "real", 2, 2),
     (2, "f64", "real", 1, 1), (3, "f64", "real", 2, 2), (7, "f32", "real", 1, 1), (10, "f64", "real", 4, 4),
     (98, "f32", "real", 3, 3), (480, "f32", "real", 5, 5), (3840, "f32", "real", 2, 2),
     (64, "f32", "complex", 300, 300), (1024, "f64", "complex", 7, 7), (480, "f32", "real", 40, 40),

@@ -154,7 +154,7 @@ def test_round_trip_is_n_times_input(F):
         assert rel_l2(back, n * x) <= 1e-13, n
 
 
-@pytest.mark.parametrize("n", [256, 768, 1000, 1024, 2048, 3072, 4096, 4800, 8192, 9216, 15360, 16384])
+@pytest.mark.parametrize("n", [256, 768, 1000, 1024, 2048, 3072, 4096, 4800, 8192, 9216, 15000, 15360, 16200, 16384, 2187, 6561])
 def test_complex_f32_vs_oracle(F, n):
     rng = np.random.default_rng(n)
     b = 6
