@@ -77,8 +77,9 @@ def _declare(l):
     dp = ctypes.POINTER(ctypes.c_double)
     szp = ctypes.POINTER(_sz)
     l.ssfft_schedule_tables.argtypes = [_sz, _int, _int, _sz, dp, szp, dp, szp, dp, szp, dp, szp]
+    l.ssfft_diag_staged_timeout.argtypes = [_sz, ctypes.c_uint, ctypes.POINTER(ctypes.c_uint)]
     for name in ("ssfft_plan_create", "ssfft_plan_destroy", "ssfft_plan_describe", "ssfft_exec", "ssfft_exec_batch",
-                 "ssfft_exec_host", "ssfft_plan_error", "ssfft_jit_check", "ssfft_schedule_info", "ssfft_schedule_name",
+                 "ssfft_exec_host", "ssfft_plan_error", "ssfft_diag_staged_timeout", "ssfft_jit_check", "ssfft_schedule_info", "ssfft_schedule_name",
                  "ssfft_schedule_tables"):
         getattr(l, name).restype = _int
     return l
@@ -179,6 +180,13 @@ def schedule_tables(n: int, dtype="f32", kind="complex", batch: int = 1) -> dict
         args += [a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(c)]
     check(lib().ssfft_schedule_tables(n, _dtype_code(dtype), _kind_code(kind), batch, *args), "schedule_tables")
     return dict(zip(("tw", "roots", "rtw", "rot"), arrs))
+
+
+def diag_staged_timeout(n: int = 1024, spin_limit: int = 1000) -> int:
+    """Run the staged kernel once with a lost input copy (GPU); returns the error flag it raised."""
+    flags = ctypes.c_uint(0)
+    check(lib().ssfft_diag_staged_timeout(n, spin_limit, ctypes.byref(flags)), "ssfft_diag_staged_timeout")
+    return flags.value
 
 
 def jit_check(n: int, dtype="f32", kind="complex", batch: int = 1, arch: str = "sm_103a") -> int:

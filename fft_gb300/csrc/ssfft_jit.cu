@@ -80,6 +80,7 @@ const Driver &driver() {
 struct Module {
 	CUmodule mod = nullptr;
 	std::vector<CUfunction> fns;
+	long long smem_set = -1;  // dynamic shared memory the functions' attributes allow so far
 };
 
 std::mutex g_jit_mutex;
@@ -213,8 +214,6 @@ ssfft_status jit_kernels(const std::vector<std::string> &names, size_t smem_byte
 	int device = 0;
 	cudaError_t ce = cudaGetDevice(&device);
 	if (ce != cudaSuccess) return cuda_fail(ce, "cudaGetDevice");
-	ce = cudaFree(nullptr);  // make the runtime's primary context current for the driver calls
-	if (ce != cudaSuccess) return cuda_fail(ce, "cudaFree(0)");
 	const Driver &drv = driver();
 	if (!drv.ok) {
 		g_jit_log = "CUDA driver entry points unavailable";
@@ -222,6 +221,7 @@ ssfft_status jit_kernels(const std::vector<std::string> &names, size_t smem_byte
 	}
 	const std::string arch = device_arch(device);
 	std::string key = std::to_string(device) + "|" + arch;
+	Module *mod = nullptr;
 	for (const auto &n : names) key += "|" + n;
 
 	{
@@ -229,6 +229,7 @@ ssfft_status jit_kernels(const std::vector<std::string> &names, size_t smem_byte
 		auto it = g_modules.find(key);
 		if (it != g_modules.end()) {
 			fns = it->second->fns;
+			mod = it->second.get();
 			goto loaded;
 		}
 	}
@@ -258,6 +259,8 @@ ssfft_status jit_kernels(const std::vector<std::string> &names, size_t smem_byte
 			write_file_atomic(img_path, image);
 			write_file_atomic(names_path, txt);
 		}
+		ce = cudaFree(nullptr);  // make the runtime's primary context current for the driver calls
+		if (ce != cudaSuccess) return cuda_fail(ce, "cudaFree(0)");
 		std::lock_guard<std::mutex> lock(g_jit_mutex);
 		auto it = g_modules.find(key);
 		if (it == g_modules.end()) {
@@ -276,15 +279,23 @@ ssfft_status jit_kernels(const std::vector<std::string> &names, size_t smem_byte
 			it = g_modules.emplace(key, std::move(m)).first;
 		}
 		fns = it->second->fns;
+		mod = it->second.get();
 	}
-loaded:
-	for (CUfunction f : fns) {
-		CUresult r = drv.funcSetAttribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem_bytes);
-		if (r != CUDA_SUCCESS) return cu_fail(r, "cuFuncSetAttribute");
-		// prefer the largest shared-memory carveout so smem, not the L1 split, bounds occupancy
-		r = drv.funcSetAttribute(f, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, 100);
-		if (r != CUDA_SUCCESS) return cu_fail(r, "cuFuncSetAttribute(carveout)");
+loaded: {
+	// attributes only when they change: a cached module needs no driver call at all, so plans
+	// can be launched inside a stream capture
+	std::lock_guard<std::mutex> lock(g_jit_mutex);
+	if ((long long)smem_bytes > mod->smem_set) {
+		for (CUfunction f : fns) {
+			CUresult r = drv.funcSetAttribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem_bytes);
+			if (r != CUDA_SUCCESS) return cu_fail(r, "cuFuncSetAttribute");
+			// prefer the largest shared-memory carveout so smem, not the L1 split, bounds occupancy
+			r = drv.funcSetAttribute(f, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, 100);
+			if (r != CUDA_SUCCESS) return cu_fail(r, "cuFuncSetAttribute(carveout)");
+		}
+		mod->smem_set = (long long)smem_bytes;
 	}
+}
 	return SSFFT_SUCCESS;
 }
 

@@ -26,6 +26,7 @@ namespace ssfft {
 
 ssfft_status launch_batch_offs(const Plan *p, int inverse, const void *in, void *out, size_t batch,
                                const long long *d_offs, cudaStream_t s);
+ssfft_status plan_prepare_launch(const Plan *p);
 
 namespace {
 
@@ -156,8 +157,13 @@ ssfft_status ssfft_multi_create(ssfft_multi_t *out, const size_t *sizes, size_t 
 		});
 	for (auto &x : th) x.join();
 	if (bad) return SSFFT_ERR_UNSUPPORTED;
-	for (auto &g : m->groups)  // every size must run in one CTA (offset-table launches)
-		if (reinterpret_cast<const Plan *>(g.plan)->large) return SSFFT_ERR_UNSUPPORTED;
+	for (auto &g : m->groups) {  // every size must run in one CTA (offset-table launches)
+		const Plan *p = reinterpret_cast<const Plan *>(g.plan);
+		if (p->large) return SSFFT_ERR_UNSUPPORTED;
+		// the graph capture must not load modules: compile every kernel a launch may use now
+		ssfft_status st = plan_prepare_launch(p);
+		if (st != SSFFT_SUCCESS) return st;
+	}
 	for (auto &g : m->groups) {
 		const auto &offs = by_size[g.n];
 		e = cudaMalloc(&g.d_offs, offs.size() * sizeof(long long));

@@ -177,7 +177,7 @@ size_t device_smem_limit(int dev) {
 }
 
 // Threads per transform, transforms per CTA and shared memory for n points.
-bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, Schedule &s, bool allow_staged) {
+bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, Schedule &s, int allow_staged) {
 	s = Schedule();
 	s.dtype = dtype;
 	s.n = n;
@@ -229,12 +229,11 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	// a whole number of 16-byte units and a group of them fits the copy and shared-memory limits.
 	const size_t sb = eb / 2;
 	const size_t in_bytes = kind == 0 ? (size_t)n * eb : (size_t)2 * n * sb;  // real: n_real = 2h reals or h bins
-	// Opt-in (SSFFT_STAGED=1): measured slower than the unstaged kernel on GB300 so far.
-	static const bool staged_enabled = [] {
-		const char *e = std::getenv("SSFFT_STAGED");
-		return e && e[0] == '1';
-	}();
-	if (allow_staged && staged_enabled && !odd && in_bytes % 16 == 0 && n >= 16) {
+	// Opt-in (SSFFT_STAGED=1, read when a plan is made): measured slower than the unstaged
+	// kernel on GB300 so far.
+	const char *staged_env = std::getenv("SSFFT_STAGED");
+	const bool staged_enabled = staged_env && staged_env[0] == '1';
+	if (((allow_staged == 1 && staged_enabled) || allow_staged == 2) && !odd && in_bytes % 16 == 0 && n >= 16) {
 		int gs = s.per_cta;
 		auto staged_smem = [&](int gg) { return (((size_t)gg * in_bytes + 127) & ~(size_t)127) + (size_t)gg * per; };
 		while (gs > 1 && staged_smem(gs) > 76 * 1024) --gs;
@@ -423,13 +422,26 @@ size_t plan_out_bytes(const Plan *p, int inverse, size_t batch) {
 
 // A staged plan given an input that is not 16-byte aligned runs the plain kernel of the same
 // schedule (compiled on first use).
+static ssfft_status unstaged_kernels(const Plan *p, Schedule &u, std::vector<CUfunction> &fns) {
+	const Schedule &st = p->main.sch;
+	if (!make_schedule(st.dtype, st.n, st.kind, st.odd, p->batch, u, 0)) return SSFFT_ERR_UNSUPPORTED;
+	return jit_kernels({u.name(false), u.name(true)}, u.smem_bytes, fns);
+}
+
+// Compiles (and loads) what a later launch of `p` may need beyond the plan's own kernels, so that
+// the launch makes no module-loading call (e.g. inside a stream capture).
+ssfft_status plan_prepare_launch(const Plan *p) {
+	if (!p->main.sch.staged) return SSFFT_SUCCESS;
+	Schedule u;
+	std::vector<CUfunction> fns;
+	return unstaged_kernels(p, u, fns);
+}
+
 static ssfft_status launch_unstaged(const Plan *p, int inverse, const void *in, void *out, size_t batch,
                                     cudaStream_t s, const long long *offs = nullptr) {
-	const Schedule &st = p->main.sch;
 	Schedule u;
-	if (!make_schedule(st.dtype, st.n, st.kind, st.odd, p->batch, u, false)) return SSFFT_ERR_UNSUPPORTED;
 	std::vector<CUfunction> fns;
-	ssfft_status rc = jit_kernels({u.name(false), u.name(true)}, u.smem_bytes, fns);
+	ssfft_status rc = unstaged_kernels(p, u, fns);
 	if (rc != SSFFT_SUCCESS) return rc;
 	ssfft_cl::Args a;
 	std::memset(&a, 0, sizeof a);
@@ -636,6 +648,60 @@ ssfft_status ssfft_plan_error(ssfft_plan_t plan, unsigned *flags) {
 ssfft_status ssfft_exec(ssfft_plan_t plan, int inverse, const void *d_in, void *d_out, void *stream) {
 	if (!plan) return SSFFT_ERR_INVALID_VALUE;
 	return ssfft_exec_batch(plan, inverse, d_in, d_out, reinterpret_cast<Plan *>(plan)->batch, stream);
+}
+
+// Failure-detection check of the staged kernel: one launch over four `n`-point complex FP32
+// transforms whose barrier expects each group's bytes while no copy is issued (a lost copy), with
+// `spin_limit` wait attempts.  The kernel must give up, raise the error flag (returned in *flags)
+// and return; nothing is in flight when it does, and the context stays usable.
+ssfft_status ssfft_diag_staged_timeout(size_t n, unsigned spin_limit, unsigned *flags) {
+	if (!flags || n < 16 || n > 4096) return SSFFT_ERR_INVALID_VALUE;
+	*flags = 0;
+	Schedule s;
+	if (!make_schedule(SSFFT_F32, (int)n, 0, false, 4, s, 2) || !s.staged) return SSFFT_ERR_UNSUPPORTED;
+	std::vector<double> tw, roots, rtw, rot;
+	single_tables(s, n, tw, roots, rtw, rot);
+	std::vector<float> blob(tw.begin(), tw.end());
+	blob.insert(blob.end(), roots.begin(), roots.end());
+	const size_t tab_bytes = std::max<size_t>(blob.size() * 4, 16), io_bytes = 4 * n * 8;
+	void *d_tab = nullptr, *d_in = nullptr, *d_out = nullptr;
+	unsigned *d_err = nullptr;
+	cudaError_t e = cudaMalloc(&d_tab, tab_bytes);
+	if (e == cudaSuccess) e = cudaMalloc(&d_err, sizeof(unsigned));
+	if (e == cudaSuccess) e = cudaMalloc(&d_in, io_bytes);
+	if (e == cudaSuccess) e = cudaMalloc(&d_out, io_bytes);
+	if (e == cudaSuccess && !blob.empty()) e = cudaMemcpy(d_tab, blob.data(), blob.size() * 4, cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) e = cudaMemset(d_err, 0, sizeof(unsigned));
+	if (e == cudaSuccess) e = cudaMemset(d_in, 0, io_bytes);
+	ssfft_status st = e == cudaSuccess ? SSFFT_SUCCESS : cuda_fail(e, "diag setup");
+	std::vector<CUfunction> fns;
+	if (st == SSFFT_SUCCESS) st = jit_kernels({s.name(false)}, s.smem_bytes, fns);
+	if (st == SSFFT_SUCCESS) {
+		ssfft_cl::Args a;
+		std::memset(&a, 0, sizeof a);
+		a.in = d_in;
+		a.out = d_out;
+		a.batch = 4;
+		a.in_dist = a.out_dist = 2 * (long long)n;
+		a.tw = d_tab;
+		a.roots = static_cast<const float *>(d_tab) + tw.size();
+		a.err = d_err;
+		a.spin_limit = spin_limit;
+		a.in_bytes = s.in_bytes;
+		a.drop_copy = 1;
+		const unsigned grid = (unsigned)((4 + s.per_cta - 1) / s.per_cta);
+		st = jit_launch(fns[0], grid, (unsigned)s.cta_threads(), s.smem_bytes, nullptr, &a);
+	}
+	if (st == SSFFT_SUCCESS) {
+		e = cudaDeviceSynchronize();
+		if (e == cudaSuccess) e = cudaMemcpy(flags, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+		if (e != cudaSuccess) st = cuda_fail(e, "diag sync");
+	}
+	cudaFree(d_tab);
+	cudaFree(d_err);
+	cudaFree(d_in);
+	cudaFree(d_out);
+	return st;
 }
 
 // ---------------------------------------------------------------- diagnostics (no GPU needed)

@@ -214,6 +214,11 @@ ssfft_status ssfft_schedule_info(size_t n, ssfft_dtype dtype, ssfft_kind kind, s
                                  int *npasses, int *threads, int *per_cta, size_t *smem_bytes);
 ssfft_status ssfft_schedule_name(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, int inverse, char *buf,
                                  size_t cap);
+/* Failure-detection check (GPU): one staged launch of four n-point complex FP32 transforms
+ * (16 <= n <= 4096) whose barrier waits for a copy that is never issued, bounded by spin_limit
+ * attempts; the kernel must set the error flag (returned in *flags) and return.  No reference
+ * counterpart. */
+ssfft_status ssfft_diag_staged_timeout(size_t n, unsigned spin_limit, unsigned *flags);
 ssfft_status ssfft_schedule_tables(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, double *tw,
                                    size_t *ntw, double *roots, size_t *nroots, double *rtw, size_t *nrtw, double *rot,
                                    size_t *nrot);

@@ -7,9 +7,6 @@ import os
 import shutil
 import subprocess
 
-# the emulator covers both the plain and the bulk-copy staged kernels
-os.environ.setdefault("SSFFT_STAGED", "1")
-
 import numpy as np
 import pytest
 
@@ -35,8 +32,21 @@ CASES = [
 ]
 
 
-@pytest.fixture(scope="session")
-def emulator(tmp_path_factory):
+@pytest.fixture(scope="module", autouse=True)
+def staged_schedules():
+    """The emulator covers both the plain and the bulk-copy staged kernels: plans made while this
+    module runs may pick the staged kernel (SSFFT_STAGED=1); the setting is restored afterwards."""
+    old = os.environ.get("SSFFT_STAGED")
+    os.environ["SSFFT_STAGED"] = "1"
+    yield
+    if old is None:
+        os.environ.pop("SSFFT_STAGED", None)
+    else:
+        os.environ["SSFFT_STAGED"] = old
+
+
+@pytest.fixture(scope="module")
+def emulator(staged_schedules, tmp_path_factory):
     if shutil.which("g++") is None:
         pytest.skip("g++ not available")
     d = tmp_path_factory.mktemp("emu")

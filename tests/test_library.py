@@ -62,6 +62,16 @@ def test_plan_kernels_compile_for_sm103a(n, dt, kind, batch):
     assert F.jit_check(n, dt, kind, batch, "sm_103a") > 0
 
 
+@pytest.mark.parametrize("n, dt, kind", [(1024, "f32", "complex"), (3840, "f32", "real"), (1024, "f64", "complex")])
+def test_staged_kernels_compile_for_sm103a(n, dt, kind, monkeypatch):
+    """The bulk-copy staged variant (opt-in) and the failure-detection launch use it."""
+    monkeypatch.setenv("SSFFT_STAGED", "1")
+    assert "batch_staged" in F.schedule_name(n, dt, kind, 64)
+    assert F.jit_check(n, dt, kind, 64, "sm_103a") > 0
+    monkeypatch.delenv("SSFFT_STAGED")
+    assert "batch_staged" not in F.schedule_name(n, dt, kind, 64)
+
+
 def test_schedules_respect_register_and_thread_budget():
     for n in list(range(1, 300)) + [480, 960, 1920, 3840, 4096, 8192, 16384, 15360, 3 ** 8]:
         info = F.schedule_info(n, "f32", "complex", 1000)
