@@ -52,6 +52,8 @@ def parse():
                     help="realfft: the batched RealFFT<float> line (default); fp64: FFT<double> N=1024 x256; "
                          "large: single FP32 transforms of 2^24, 3^15, 2^12 3^4 5^2; serve: request serving sweep")
     ap.add_argument("--serve-duration", type=float, default=1.0)
+    ap.add_argument("--tune", type=int, default=2, choices=[0, 1, 2],
+                    help="autotune level of the plans (0 planner defaults, 1 CTA shape, 2 also radix order)")
     ap.add_argument("--streams", type=int, default=4,
                     help="run each size's forward->inverse chain on its own stream (1..4)")
     return ap.parse_args()
@@ -151,13 +153,18 @@ def max_over_ranks(seconds: float, dist=None, device: str = "cpu") -> float:
 
 
 def traffic_for(kernel: str):
-    """DRAM bytes per launch (read + write) of `kernel` from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    """DRAM bytes per launch (read + write) of `kernel` from the committed ncu launch-list
+    summary (its table's last column), if the kernel is listed there."""
+    p = os.path.join(ROOT, "profiles", "realfft_f32_launches_16384frames.md")
     try:
         with open(p) as f:
-            return json.load(f).get(kernel)
-    except Exception:
-        return None
+            for line in f:
+                cells = [c.strip() for c in line.strip().strip("|").split("|")]
+                if cells and cells[0] == kernel:
+                    return float(cells[-1])
+    except (OSError, ValueError):
+        pass
+    return None
 
 
 def cpu_leg(frames: int, threads: int, kind: str = "port", seed: int = 7) -> dict:
@@ -235,7 +242,11 @@ def run_gpu(args, rank: int, world: int):
         xs.append(torch.from_numpy(x).cuda())
         specs.append(torch.empty((frames, n // 2), dtype=torch.complex64, device="cuda"))
         backs.append(torch.empty((frames, n), dtype=torch.float32, device="cuda"))
-        plans.append(F.Plan(n, "f32", "real", frames))
+        plans.append(F.Plan(n, "f32", "real", frames, autotune=args.tune))
+    schedules = {f"N{n}": p.tuning()["choice"] for n, p in zip(SIZES, plans)}
+    for n, p in zip(SIZES, plans):
+        for line in p.tuning()["log"]:
+            print(f"tune N={n}: {line}", file=sys.stderr)
     nl = len(SIZES) * 2
 
     def step(evs=None, ns=None):
@@ -367,7 +378,8 @@ def run_gpu(args, rank: int, world: int):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "RealFFT<float> N in {480,960,1920,3840}, 16384 frames each, fwd+inv",
                        "frames": frames, "parallelism": f"replicas x{world}", "streams": nstreams,
-                       "l2": "each step streams ~1.9 GB (> 129 MB L2), no flush"},
+                       "l2": "each step streams ~1.9 GB (> 129 MB L2), no flush",
+                       "autotune": args.tune, "schedules": schedules},
             "gpu_launches": nl * args.steps,
             "relL2_vs_fp64_oracle": rel,
             "roofline": {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": peak,
@@ -504,7 +516,7 @@ def run_uneven(args):
     x.imag.uniform_(-1, 1)
     y = torch.empty_like(x)
     t0 = time.perf_counter()
-    m = F.Multi(sizes, "f32")
+    m = F.Multi(sizes, "f32", autotune=min(args.tune, 1))
     build_s = time.perf_counter() - t0
     sh = int(torch.cuda.current_stream().cuda_stream)
     tg = _time_device(lambda: m.exec(False, x.data_ptr(), y.data_ptr(), sh), max(args.steps // 4, 50), 5)
@@ -523,6 +535,7 @@ def run_uneven(args):
     peak, kind = measured_peak_hbm()
     print(json.dumps({"workload": "32768 complex FP32 transforms, uneven sizes in [64,16384]",
                       "distinct_sizes": m.info()["distinct_sizes"], "alg_bytes": alg,
+                      "autotune": min(args.tune, 1),
                       "graph": {"ms": tg * 1e3, "GFLOP_s": flops / tg / 1e9, "alg_GB_s": alg / tg / 1e9,
                                 "frac_of_hbm": alg / tg / 1e9 / peak},
                       "plain_per_size": {"ms": tp * 1e3, "GFLOP_s": flops / tp / 1e9, "alg_GB_s": alg / tp / 1e9},

@@ -49,6 +49,21 @@ _int = ctypes.c_int
 _vp = ctypes.c_void_p
 
 
+class PlanOptions(ctypes.Structure):
+    """ssfft_plan_options (0 = planner default)."""
+    _fields_ = [("autotune", ctypes.c_int), ("cta_threads", ctypes.c_int), ("values_per_thread", ctypes.c_int),
+                ("min_ctas_per_sm", ctypes.c_int), ("radices", ctypes.c_int * 24)]
+
+
+def _options(autotune=0, radices=None, cta_threads=0, values_per_thread=0, min_ctas_per_sm=0):
+    o = PlanOptions()
+    o.autotune, o.cta_threads = int(autotune), int(cta_threads)
+    o.values_per_thread, o.min_ctas_per_sm = int(values_per_thread), int(min_ctas_per_sm)
+    for i, r in enumerate(radices or []):
+        o.radices[i] = int(r)
+    return o
+
+
 def _declare(l):
     l.ssfft_status_string.argtypes = [_int]
     l.ssfft_status_string.restype = ctypes.c_char_p
@@ -58,6 +73,8 @@ def _declare(l):
         getattr(l, name).restype = _sz
     l.ssfft_plan_create.argtypes = [ctypes.POINTER(_vp), _sz, _int, _int, _sz]
     l.ssfft_plan_destroy.argtypes = [_vp]
+    l.ssfft_plan_create_ex.argtypes = [ctypes.POINTER(_vp), _sz, _int, _int, _sz, ctypes.POINTER(PlanOptions)]
+    l.ssfft_plan_tuning.argtypes = [_vp, ctypes.c_char_p, _sz, ctypes.c_char_p, _sz]
     l.ssfft_plan_size.argtypes = [_vp]
     l.ssfft_plan_size.restype = _sz
     l.ssfft_plan_batch.argtypes = [_vp]
@@ -78,7 +95,7 @@ def _declare(l):
     szp = ctypes.POINTER(_sz)
     l.ssfft_schedule_tables.argtypes = [_sz, _int, _int, _sz, dp, szp, dp, szp, dp, szp, dp, szp]
     l.ssfft_diag_staged_timeout.argtypes = [_sz, ctypes.c_uint, ctypes.POINTER(ctypes.c_uint)]
-    for name in ("ssfft_plan_create", "ssfft_plan_destroy", "ssfft_plan_describe", "ssfft_exec", "ssfft_exec_batch",
+    for name in ("ssfft_plan_create", "ssfft_plan_create_ex", "ssfft_plan_tuning", "ssfft_plan_destroy", "ssfft_plan_describe", "ssfft_exec", "ssfft_exec_batch",
                  "ssfft_exec_host", "ssfft_plan_error", "ssfft_diag_staged_timeout", "ssfft_jit_check", "ssfft_schedule_info", "ssfft_schedule_name",
                  "ssfft_schedule_tables"):
         getattr(l, name).restype = _int
@@ -202,15 +219,25 @@ def jit_check(n: int, dtype="f32", kind="complex", batch: int = 1, arch: str = "
 class Plan:
     """One ``ssfft_plan_t``: ``batch`` transforms of size ``n`` (complex or real)."""
 
-    def __init__(self, n: int, dtype="f32", kind="complex", batch: int = 1):
+    def __init__(self, n: int, dtype="f32", kind="complex", batch: int = 1, *, autotune: int = 0, radices=None,
+                 cta_threads: int = 0, values_per_thread: int = 0, min_ctas_per_sm: int = 0):
         self.n = int(n)
         self.dtype = _dtype_code(dtype)
         self.kind = _kind_code(kind)
         self.batch = max(1, int(batch))
         h = _vp()
-        check(lib().ssfft_plan_create(ctypes.byref(h), self.n, self.dtype, self.kind, self.batch),
+        opt = _options(autotune, radices, cta_threads, values_per_thread, min_ctas_per_sm)
+        check(lib().ssfft_plan_create_ex(ctypes.byref(h), self.n, self.dtype, self.kind, self.batch,
+                                         ctypes.byref(opt)),
               f"plan_create(n={n}, kind={kind}, batch={batch})")
         self._h = h
+
+    def tuning(self) -> dict:
+        """Schedule options in force and the autotuner's candidate timings (if it ran)."""
+        a = ctypes.create_string_buffer(256)
+        b = ctypes.create_string_buffer(16384)
+        check(lib().ssfft_plan_tuning(self._h, a, 256, b, 16384), "plan_tuning")
+        return {"choice": a.value.decode(), "log": [x for x in b.value.decode().splitlines() if x]}
 
     @property
     def handle(self):
@@ -582,22 +609,26 @@ def fast_sizes(lo: int, hi: int) -> list:
 class Multi:
     """ssfft_multi_*: one submission of complex transforms of uneven sizes stored back to back."""
 
-    def __init__(self, sizes, dtype="f32"):
+    def __init__(self, sizes, dtype="f32", autotune: int = 0):
         l = lib()
         if not getattr(l, "_multi_declared", False):
             l.ssfft_multi_create.argtypes = [ctypes.POINTER(_vp), ctypes.POINTER(_sz), _sz, _int]
+            l.ssfft_multi_create_ex.argtypes = [ctypes.POINTER(_vp), ctypes.POINTER(_sz), _sz, _int,
+                                                ctypes.POINTER(PlanOptions)]
             l.ssfft_multi_exec.argtypes = [_vp, _int, _vp, _vp, _vp]
             l.ssfft_multi_exec_plain.argtypes = [_vp, _int, _vp, _vp, _vp]
             l.ssfft_multi_info.argtypes = [_vp, ctypes.POINTER(_sz), ctypes.POINTER(_sz)]
             l.ssfft_multi_destroy.argtypes = [_vp]
-            for name in ("ssfft_multi_create", "ssfft_multi_exec", "ssfft_multi_exec_plain", "ssfft_multi_info",
+            for name in ("ssfft_multi_create", "ssfft_multi_create_ex", "ssfft_multi_exec", "ssfft_multi_exec_plain", "ssfft_multi_info",
                          "ssfft_multi_destroy"):
                 getattr(l, name).restype = _int
             l._multi_declared = True
         self.sizes = [int(n) for n in sizes]
         arr = (_sz * len(self.sizes))(*self.sizes)
         h = _vp()
-        check(l.ssfft_multi_create(ctypes.byref(h), arr, len(self.sizes), _dtype_code(dtype)), "multi_create")
+        opt = _options(autotune)
+        check(l.ssfft_multi_create_ex(ctypes.byref(h), arr, len(self.sizes), _dtype_code(dtype), ctypes.byref(opt)),
+              "multi_create")
         self._h = h
 
     def exec(self, inverse: bool, d_in: int, d_out: int, stream: int = 0) -> None:

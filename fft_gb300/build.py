@@ -20,7 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libssfft.so")
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["ssfft_plan.cu", "ssfft_jit.cu", "ssfft_stage.cu", "ssfft_large.cu", "ssfft_serve.cu", "ssfft_multi.cu", "ssfft_noalloc.cu"]
+SOURCES = ["ssfft_plan.cu", "ssfft_jit.cu", "ssfft_stage.cu", "ssfft_large.cu", "ssfft_serve.cu", "ssfft_multi.cu", "ssfft_noalloc.cu", "ssfft_tune.cu"]
 
 
 def cuda_root() -> str:

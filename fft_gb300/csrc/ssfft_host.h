@@ -38,6 +38,17 @@ struct Schedule {
 	std::string name(bool inverse) const;
 };
 
+// Schedule choices that override the planner's defaults (0 / empty = default); set by the
+// caller (ssfft_plan_options) or by the autotuner.
+struct Knobs {
+	std::vector<int> radices;  // pass order, product = complex points
+	int cta_threads = 0;       // target threads per CTA
+	int emax = 0;              // complex values a thread holds in one pass
+	int minb = 0;              // launch-bound CTAs per SM
+	bool empty() const { return radices.empty() && !cta_threads && !emax && !minb; }
+	std::string str() const;
+};
+
 // Device tables of one schedule (all inside the plan's single table allocation).
 struct Tables {
 	const void *tw = nullptr, *roots = nullptr, *rtw = nullptr, *rot = nullptr;
@@ -78,6 +89,9 @@ struct Plan {
 	int launches_per_exec = 1;
 	LargePlan *large = nullptr;
 	HostStage *stage = nullptr;
+	Knobs knobs;              // schedule choices in force (explicit or tuned)
+	std::string tune_log;     // candidates the autotuner timed when this plan was made
+	int autotune = 0;         // 0 off, 1 quick (threads / CTA shape), 2 full (also radix order)
 	std::mutex stage_mutex;
 };
 
@@ -88,7 +102,15 @@ ssfft_status cuda_fail(cudaError_t e, const char *what);
 void unit_root(unsigned long long k, unsigned long long L, double *re, double *im);
 bool choose_radices(int n, std::vector<int> &radices);
 // allow_staged: 0 never, 1 when SSFFT_STAGED=1, 2 always (where the size allows it)
-bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, Schedule &s, int allow_staged = 1);
+bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, Schedule &s, int allow_staged = 1,
+                   const Knobs *knobs = nullptr);
+bool single_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, Schedule &s,
+                     const Knobs *knobs = nullptr, int allow_staged = 1);
+void single_tables(const Schedule &s, size_t n_real, std::vector<double> &tw, std::vector<double> &roots,
+                   std::vector<double> &rtw, std::vector<double> &rot);
+void radix_candidates(int n, std::vector<std::vector<int>> &out);
+// autotuner (ssfft_tune.cu): picks knobs for a single-CTA plan, cached per device and shape
+ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log);
 void schedule_twiddles(const Schedule &s, std::vector<double> &tw, std::vector<double> &roots);
 size_t device_smem_limit(int dev);
 
@@ -101,6 +123,10 @@ ssfft_status jit_launch_grid(CUfunction f, unsigned grid_x, unsigned grid_y, uns
                              cudaStream_t stream, void *args);
 int jit_occupancy(CUfunction f, int block, size_t smem);
 const char *jit_last_log();
+std::string jit_cache_dir();
+uint64_t codelet_hash();
+bool cache_read(const std::string &path, std::string &out);
+void cache_write(const std::string &path, const std::string &data);
 
 // plans
 void plan_dists(const Plan *p, int inverse, long long &in_dist, long long &out_dist);

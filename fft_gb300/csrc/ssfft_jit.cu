@@ -327,4 +327,12 @@ ssfft_status jit_launch(CUfunction f, unsigned grid, unsigned block, size_t smem
 	return jit_launch_grid(f, grid, 1, block, smem, stream, args);
 }
 
+std::string jit_cache_dir() { return cache_dir(); }
+uint64_t codelet_hash() { return fnv1a(kCodeletSource); }
+bool cache_read(const std::string &path, std::string &out) { return read_file(path, out); }
+void cache_write(const std::string &path, const std::string &data) {
+	mkdirs(cache_dir());
+	write_file_atomic(path, data);
+}
+
 }  // namespace ssfft

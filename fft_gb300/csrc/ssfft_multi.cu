@@ -116,7 +116,13 @@ using namespace ssfft;
 extern "C" {
 
 ssfft_status ssfft_multi_create(ssfft_multi_t *out, const size_t *sizes, size_t count, ssfft_dtype dtype) {
+	return ssfft_multi_create_ex(out, sizes, count, dtype, nullptr);
+}
+
+ssfft_status ssfft_multi_create_ex(ssfft_multi_t *out, const size_t *sizes, size_t count, ssfft_dtype dtype,
+                                   const ssfft_plan_options *opt) {
 	if (!out || !sizes || count == 0) return SSFFT_ERR_INVALID_VALUE;
+	if (opt && opt->radices[0] != 0) return SSFFT_ERR_INVALID_VALUE;  // one radix list cannot fit every size
 	if (dtype != SSFFT_F32 && dtype != SSFFT_F64) return SSFFT_ERR_INVALID_VALUE;
 	*out = nullptr;
 	std::unique_ptr<MultiPlan> m(new MultiPlan());
@@ -152,7 +158,7 @@ ssfft_status ssfft_multi_create(ssfft_multi_t *out, const size_t *sizes, size_t 
 			cudaSetDevice(dev);
 			for (size_t i = next++; i < mp->groups.size(); i = next++) {
 				Group &g = mp->groups[i];
-				if (ssfft_plan_create(&g.plan, g.n, mp->dtype, SSFFT_COMPLEX, g.count) != SSFFT_SUCCESS) bad = 1;
+				if (ssfft_plan_create_ex(&g.plan, g.n, mp->dtype, SSFFT_COMPLEX, g.count, opt) != SSFFT_SUCCESS) bad = 1;
 			}
 		});
 	for (auto &x : th) x.join();

@@ -177,13 +177,65 @@ size_t device_smem_limit(int dev) {
 }
 
 // Threads per transform, transforms per CTA and shared memory for n points.
-bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, Schedule &s, int allow_staged) {
+// Distinct radix lists worth timing for n complex points: the planner's choice and its pass
+// orders, and the list without borrowed composite radices and its orders (at most 8 in all).
+void radix_candidates(int n, std::vector<std::vector<int>> &out) {
+	out.clear();
+	std::vector<int> def;
+	if (!choose_radices(n, def)) return;
+	auto add_orders = [&](std::vector<int> r) {
+		std::vector<int> sorted = r;
+		std::sort(sorted.begin(), sorted.end());
+		std::vector<std::vector<int>> perms;
+		do perms.push_back(sorted);
+		while (std::next_permutation(sorted.begin(), sorted.end()) && perms.size() < 24);
+		// the given order first, then the others
+		if (std::find(out.begin(), out.end(), r) == out.end() && out.size() < 8) out.push_back(r);
+		for (auto &q : perms)
+			if (std::find(out.begin(), out.end(), q) == out.end() && out.size() < 8) out.push_back(q);
+	};
+	add_orders(def);
+	// the alternative grouping (with or without composite 10/12/6 radices)
+	int m = n, a = 0, b = 0, c = 0;
+	while (m % 2 == 0) m /= 2, ++a;
+	while (m % 3 == 0) m /= 3, ++b;
+	while (m % 5 == 0) m /= 5, ++c;
+	if (m == 1) {
+		std::vector<int> plain, borrowed;
+		radices_for(a, b, c, {}, false, plain);
+		radices_for(a, b, c, {}, true, borrowed);
+		if (plain != def && plain.size() <= def.size() + 1) add_orders(plain);
+		if (borrowed != def && borrowed.size() <= def.size() + 1) add_orders(borrowed);
+	}
+}
+
+std::string Knobs::str() const {
+	std::string r = "radices=";
+	for (size_t i = 0; i < radices.size(); ++i) r += (i ? "." : "") + std::to_string(radices[i]);
+	if (radices.empty()) r += "default";
+	r += " cta=" + std::to_string(cta_threads) + " emax=" + std::to_string(emax) + " minb=" + std::to_string(minb);
+	return r;
+}
+
+bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, Schedule &s, int allow_staged,
+                   const Knobs *knobs) {
 	s = Schedule();
 	s.dtype = dtype;
 	s.n = n;
 	s.kind = kind;
 	s.odd = odd;
-	if (!choose_radices(n, s.radices)) return false;
+	if (knobs && !knobs->radices.empty()) {
+		long long prod = 1;
+		for (int r : knobs->radices) {
+			if (r < 2 && n > 1) return false;
+			prod *= r;
+			if (prod > n) return false;
+		}
+		if (prod != n || knobs->radices.size() > 24) return false;
+		s.radices = knobs->radices;
+	} else if (!choose_radices(n, s.radices)) {
+		return false;
+	}
 	// threads per transform: every pass must fit its butterflies into `emax` values per thread;
 	// 16 normally, 32 when 16 would need more than one CTA's threads (long sizes whose composite
 	// radices hold a single butterfly per thread)
@@ -196,11 +248,18 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 		}
 		return t;
 	};
-	s.emax = kElemsPerThread;
-	int t = threads_for(s.emax);
-	if (t > kMaxCtaThreads) {
-		s.emax = 2 * kElemsPerThread;
+	int t;
+	if (knobs && knobs->emax > 0) {
+		if (knobs->emax > 2 * kElemsPerThread) return false;
+		s.emax = knobs->emax;
 		t = threads_for(s.emax);
+	} else {
+		s.emax = kElemsPerThread;
+		t = threads_for(s.emax);
+		if (t > kMaxCtaThreads) {
+			s.emax = 2 * kElemsPerThread;
+			t = threads_for(s.emax);
+		}
 	}
 	if (t > kMaxCtaThreads) return false;
 	s.threads = t;
@@ -217,7 +276,7 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 		const int v = e ? std::atoi(e) : 0;
 		return v > 0 ? v : 128;  // 128 measured best on GB300 (vs 256 / 512)
 	}();
-	int g = std::max(1, cta_target / t);
+	int g = std::max(1, (knobs && knobs->cta_threads > 0 ? knobs->cta_threads : cta_target) / t);
 	const size_t soft = std::max<size_t>(per, 48 * 1024);
 	while (g > 1 && (size_t)g * per > soft) --g;
 	if (batch > 0 && (size_t)g > batch) g = (int)batch;
@@ -253,6 +312,7 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	// cap of two CTAs.  SSFFT_MINB overrides for experiments.
 	int mb = s.staged ? 2 : 1;
 	if (minb_env > 0) mb = minb_env;
+	if (knobs && knobs->minb > 0) mb = knobs->minb;
 	s.minb = std::max(1, mb);
 	return true;
 }
@@ -308,17 +368,18 @@ static int kind_code(ssfft_kind kind) {
 }
 
 // The single-CTA schedule of (n, dtype, kind, batch), or false if n needs the multi-pass path.
-static bool single_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, Schedule &s) {
+bool single_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, Schedule &s, const Knobs *knobs,
+                     int allow_staged) {
 	const bool real = kind != SSFFT_COMPLEX;
 	const size_t cn = real ? n / 2 : n;
 	const int max_n = dtype == SSFFT_F32 ? kMaxSubTransform : kMaxSubTransform / 2;
 	if (cn == 0 || cn > (size_t)max_n) return false;
-	return make_schedule(dtype, (int)cn, kind_code(kind), real && (n & 1), batch, s, true);
+	return make_schedule(dtype, (int)cn, kind_code(kind), real && (n & 1), batch, s, allow_staged, knobs);
 }
 
 // FP64 tables of a single-CTA schedule: pass twiddles, direct-pass roots, and for real kinds
 // the split twiddles and half-shift rotations.
-static void single_tables(const Schedule &s, size_t n_real, std::vector<double> &tw, std::vector<double> &roots,
+void single_tables(const Schedule &s, size_t n_real, std::vector<double> &tw, std::vector<double> &roots,
                           std::vector<double> &rtw, std::vector<double> &rot) {
 	schedule_twiddles(s, tw, roots);
 	if (s.kind == ssfft_cl::kComplex) return;
@@ -343,7 +404,19 @@ static void single_tables(const Schedule &s, size_t n_real, std::vector<double> 
 
 static ssfft_status plan_build_single(Plan *p) {
 	Schedule &s = p->main.sch;
-	if (!single_schedule(p->n, p->dtype, p->kind, p->batch, s)) return SSFFT_ERR_UNSUPPORTED;
+	{
+		// the default schedule decides whether n runs in one CTA; explicit or tuned knobs refine it
+		Schedule d;
+		if (!single_schedule(p->n, p->dtype, p->kind, p->batch, d)) return SSFFT_ERR_UNSUPPORTED;
+	}
+	if (p->autotune > 0 && p->knobs.empty()) {
+		Knobs best;
+		ssfft_status st = autotune_single(p, p->autotune, best, p->tune_log);
+		if (st != SSFFT_SUCCESS) return st;
+		p->knobs = best;
+	}
+	if (!single_schedule(p->n, p->dtype, p->kind, p->batch, s, p->knobs.empty() ? nullptr : &p->knobs))
+		return SSFFT_ERR_INVALID_VALUE;  // explicit knobs that do not fit this size
 	if (s.smem_bytes > device_smem_limit(p->device)) return SSFFT_ERR_UNSUPPORTED;
 	std::vector<double> tw, roots, rtw, rot;
 	single_tables(s, p->n, tw, roots, rtw, rot);
@@ -544,6 +617,11 @@ size_t ssfft_real_size_minimum(size_t n) { return (size_minimum((n - 1) / 2) + 1
 size_t ssfft_real_size_maximum(size_t n) { return size_minimum(n / 2) * 2; }
 
 ssfft_status ssfft_plan_create(ssfft_plan_t *out, size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch) {
+	return ssfft_plan_create_ex(out, n, dtype, kind, batch, nullptr);
+}
+
+ssfft_status ssfft_plan_create_ex(ssfft_plan_t *out, size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch,
+                                  const ssfft_plan_options *opt) {
 	if (!out) return SSFFT_ERR_INVALID_VALUE;
 	*out = nullptr;
 	if (dtype != SSFFT_F32 && dtype != SSFFT_F64) return SSFFT_ERR_INVALID_VALUE;
@@ -557,6 +635,24 @@ ssfft_status ssfft_plan_create(ssfft_plan_t *out, size_t n, ssfft_dtype dtype, s
 	p->dtype = dtype;
 	p->kind = kind;
 	p->batch = batch;
+	static const int autotune_env = [] {
+		const char *e = std::getenv("SSFFT_AUTOTUNE");
+		return e ? std::max(0, std::min(2, std::atoi(e))) : 0;
+	}();
+	p->autotune = autotune_env;
+	if (opt) {
+		if (opt->autotune < 0 || opt->autotune > 2 || opt->cta_threads < 0 || opt->cta_threads > kMaxCtaThreads ||
+		    opt->values_per_thread < 0 || opt->values_per_thread > 2 * kElemsPerThread || opt->min_ctas_per_sm < 0 ||
+		    opt->min_ctas_per_sm > 32) {
+			delete p;
+			return SSFFT_ERR_INVALID_VALUE;
+		}
+		if (opt->autotune) p->autotune = opt->autotune;
+		p->knobs.cta_threads = opt->cta_threads;
+		p->knobs.emax = opt->values_per_thread;
+		p->knobs.minb = opt->min_ctas_per_sm;
+		for (int i = 0; i < 24 && opt->radices[i] > 0; ++i) p->knobs.radices.push_back(opt->radices[i]);
+	}
 	cudaError_t e = cudaGetDevice(&p->device);
 	ssfft_status st = e == cudaSuccess ? SSFFT_SUCCESS : cuda_fail(e, "cudaGetDevice");
 	if (st == SSFFT_SUCCESS) {
@@ -569,6 +665,20 @@ ssfft_status ssfft_plan_create(ssfft_plan_t *out, size_t n, ssfft_dtype dtype, s
 		return st;
 	}
 	*out = reinterpret_cast<ssfft_plan_t>(p);
+	return SSFFT_SUCCESS;
+}
+
+ssfft_status ssfft_plan_tuning(ssfft_plan_t plan, char *choice, size_t choice_len, char *log, size_t log_len) {
+	if (!plan) return SSFFT_ERR_INVALID_VALUE;
+	const Plan *p = reinterpret_cast<const Plan *>(plan);
+	auto put = [](const std::string &src, char *dst, size_t len) {
+		if (!dst || !len) return;
+		const size_t k = std::min(len - 1, src.size());
+		std::memcpy(dst, src.data(), k);
+		dst[k] = 0;
+	};
+	put(p->large ? std::string("multi-pass") : p->knobs.str(), choice, choice_len);
+	put(p->tune_log, log, log_len);
 	return SSFFT_SUCCESS;
 }
 

@@ -1,0 +1,316 @@
+// ssfft_tune.cu -- autotuner for single-CTA plans.
+//
+// The planner's defaults (radix order, ~128 threads per CTA, 16 complex values per thread) were
+// measured on the headline sizes; other sizes and batch counts can prefer other shapes.  When a
+// plan asks for it, the tuner times candidate schedules on the plan's own batch (zero-filled
+// scratch buffers, CUDA events on a private stream) by coordinate descent:
+//   level 2: radix order (the planner's list, its permutations, the alternative grouping);
+//   level 1 and 2: values per thread {8, 16, 32}, then CTA size {64, 128, 256, 512}.
+// Candidates of one stage compile concurrently (NVRTC), and are timed one at a time under a
+// process-wide lock so concurrent plan creations do not disturb each other's timings.  The
+// winner is cached per (device name, kernel source, n, dtype, kind, batch range, level) in memory
+// and in a text file under the kernel cache directory.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "ssfft_host.h"
+
+namespace ssfft {
+
+namespace {
+
+std::mutex g_cache_mu;      // in-memory and on-disk results
+std::mutex g_time_mu;       // one candidate timed at a time in the process
+std::map<std::string, Knobs> g_cache;
+bool g_loaded = false;
+
+std::string cache_file() {
+	char h[32];
+	std::snprintf(h, sizeof h, "%016llx", (unsigned long long)codelet_hash());
+	return jit_cache_dir() + "/tune-" + h + ".txt";
+}
+
+// "r=16.8.15 c=128 e=16 m=1"
+std::string encode(const Knobs &k) {
+	std::string r = "r=";
+	for (size_t i = 0; i < k.radices.size(); ++i) r += (i ? "." : "") + std::to_string(k.radices[i]);
+	r += " c=" + std::to_string(k.cta_threads) + " e=" + std::to_string(k.emax) + " m=" + std::to_string(k.minb);
+	return r;
+}
+
+bool decode(const std::string &txt, Knobs &k) {
+	k = Knobs();
+	std::stringstream ss(txt);
+	std::string tok;
+	while (ss >> tok) {
+		if (tok.size() < 2 || tok[1] != '=') return false;
+		const std::string v = tok.substr(2);
+		if (tok[0] == 'r') {
+			std::stringstream rs(v);
+			std::string part;
+			while (std::getline(rs, part, '.'))
+				if (!part.empty()) k.radices.push_back(std::atoi(part.c_str()));
+		} else if (tok[0] == 'c') {
+			k.cta_threads = std::atoi(v.c_str());
+		} else if (tok[0] == 'e') {
+			k.emax = std::atoi(v.c_str());
+		} else if (tok[0] == 'm') {
+			k.minb = std::atoi(v.c_str());
+		}
+	}
+	return true;
+}
+
+void load_locked() {
+	if (g_loaded) return;
+	g_loaded = true;
+	std::string txt;
+	if (!cache_read(cache_file(), txt)) return;
+	std::stringstream ss(txt);
+	std::string line;
+	while (std::getline(ss, line)) {
+		const size_t tab = line.find('\t');
+		if (tab == std::string::npos) continue;
+		Knobs k;
+		if (decode(line.substr(tab + 1), k)) g_cache[line.substr(0, tab)] = k;
+	}
+}
+
+void store_locked(const std::string &key, const Knobs &k) {
+	g_cache[key] = k;
+	std::string txt;
+	for (const auto &kv : g_cache) txt += kv.first + "\t" + encode(kv.second) + "\n";
+	cache_write(cache_file(), txt);
+}
+
+struct Candidate {
+	Knobs knobs;
+	Schedule sch;
+	std::vector<CUfunction> fns;
+	ssfft_status st = SSFFT_ERR_UNSUPPORTED;
+	double fwd_us = 0, inv_us = 0;
+	double total() const { return fwd_us + inv_us; }
+};
+
+// Scratch of the timing runs: input and output large enough for `tb` transforms either way.
+struct Scratch {
+	void *in = nullptr, *out = nullptr, *tab = nullptr;
+	size_t tab_bytes = 0;
+	cudaStream_t stream = nullptr;
+	cudaEvent_t ev[2] = {};
+	~Scratch() {
+		if (in) cudaFree(in);
+		if (out) cudaFree(out);
+		if (tab) cudaFree(tab);
+		for (auto e : ev)
+			if (e) cudaEventDestroy(e);
+		if (stream) cudaStreamDestroy(stream);
+	}
+};
+
+void compile_all(const Plan *p, size_t tb, std::vector<Candidate> &cs) {
+	std::atomic<size_t> next{0};
+	const int nt = (int)std::max<size_t>(1, std::min<size_t>(cs.size(), 4));
+	std::vector<std::thread> th;
+	const size_t limit = device_smem_limit(p->device);
+	for (int t = 0; t < nt; ++t)
+		th.emplace_back([&] {
+			cudaSetDevice(p->device);
+			for (size_t i = next++; i < cs.size(); i = next++) {
+				Candidate &c = cs[i];
+				if (!single_schedule(p->n, p->dtype, p->kind, tb, c.sch, &c.knobs, 0) || c.sch.smem_bytes > limit) {
+					c.st = SSFFT_ERR_UNSUPPORTED;
+					continue;
+				}
+				c.st = jit_kernels({c.sch.name(false), c.sch.name(true)}, c.sch.smem_bytes, c.fns);
+			}
+		});
+	for (auto &x : th) x.join();
+}
+
+ssfft_status time_one(const Plan *p, size_t tb, Scratch &sc, Candidate &c) {
+	std::vector<double> tw, roots, rtw, rot;
+	single_tables(c.sch, p->n, tw, roots, rtw, rot);
+	const size_t sb = p->dtype == SSFFT_F32 ? 4 : 8;
+	const size_t o_roots = (tw.size() * sb + 255) & ~(size_t)255;
+	const size_t o_rtw = (o_roots + roots.size() * sb + 255) & ~(size_t)255;
+	const size_t o_rot = (o_rtw + rtw.size() * sb + 255) & ~(size_t)255;
+	const size_t total = std::max<size_t>((o_rot + rot.size() * sb + 255) & ~(size_t)255, 256);
+	std::vector<unsigned char> blob(total, 0);
+	auto put = [&](size_t off, const std::vector<double> &v) {
+		for (size_t i = 0; i < v.size(); ++i) {
+			if (sb == 4) {
+				const float f = (float)v[i];
+				std::memcpy(blob.data() + off + i * 4, &f, 4);
+			} else {
+				std::memcpy(blob.data() + off + i * 8, &v[i], 8);
+			}
+		}
+	};
+	put(0, tw);
+	put(o_roots, roots);
+	put(o_rtw, rtw);
+	put(o_rot, rot);
+	if (total > sc.tab_bytes) {
+		if (sc.tab) cudaFree(sc.tab);
+		sc.tab = nullptr;
+		sc.tab_bytes = 0;
+		cudaError_t e = cudaMalloc(&sc.tab, total);
+		if (e != cudaSuccess) return cuda_fail(e, "tune tables");
+		sc.tab_bytes = total;
+	}
+	cudaError_t e = cudaMemcpy(sc.tab, blob.data(), total, cudaMemcpyHostToDevice);
+	if (e != cudaSuccess) return cuda_fail(e, "tune tables copy");
+	const unsigned char *base = static_cast<const unsigned char *>(sc.tab);
+	const long long grid = ((long long)tb + c.sch.per_cta - 1) / c.sch.per_cta;
+	for (int inv = 0; inv < 2; ++inv) {
+		ssfft_cl::Args a;
+		std::memset(&a, 0, sizeof a);
+		a.in = sc.in;
+		a.out = sc.out;
+		a.batch = (long long)tb;
+		plan_dists(p, inv, a.in_dist, a.out_dist);
+		a.tw = base;
+		a.roots = base + o_roots;
+		a.rtw = base + o_rtw;
+		a.rot = base + o_rot;
+		CUfunction f = c.fns[inv];
+		ssfft_status st = jit_launch(f, (unsigned)grid, (unsigned)c.sch.cta_threads(), c.sch.smem_bytes, sc.stream, &a);
+		if (st != SSFFT_SUCCESS) return st;
+		// repeats scale with the work so that each measurement spans ~0.3 ms or more
+		const double work = (double)tb * (double)p->n;
+		const int reps = (int)std::min(20.0, std::max(3.0, std::ceil(3e7 / std::max(work, 1.0))));
+		cudaEventRecord(sc.ev[0], sc.stream);
+		for (int r = 0; r < reps && st == SSFFT_SUCCESS; ++r)
+			st = jit_launch(f, (unsigned)grid, (unsigned)c.sch.cta_threads(), c.sch.smem_bytes, sc.stream, &a);
+		cudaEventRecord(sc.ev[1], sc.stream);
+		if (st != SSFFT_SUCCESS) return st;
+		e = cudaEventSynchronize(sc.ev[1]);
+		if (e != cudaSuccess) return cuda_fail(e, "tune timing");
+		float ms = 0;
+		cudaEventElapsedTime(&ms, sc.ev[0], sc.ev[1]);
+		(inv ? c.inv_us : c.fwd_us) = 1e3 * ms / reps;
+	}
+	return SSFFT_SUCCESS;
+}
+
+}  // namespace
+
+ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log) {
+	best = Knobs();
+	log.clear();
+	const bool real = p->kind != SSFFT_COMPLEX;
+	const int cn = (int)(real ? p->n / 2 : p->n);
+	if (cn < 8) return SSFFT_SUCCESS;  // nothing to choose
+	cudaDeviceProp prop;
+	cudaError_t e = cudaGetDeviceProperties(&prop, p->device);
+	if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceProperties");
+	int bb = 0;
+	while (bb < 40 && ((size_t)1 << (bb + 1)) <= p->batch) ++bb;
+	const std::string key = std::string(prop.name) + "|" + std::to_string(p->n) + "|" +
+	                        (p->dtype == SSFFT_F32 ? "f32" : "f64") + "|" + std::to_string((int)p->kind) + "|b" +
+	                        std::to_string(bb) + "|L" + std::to_string(level);
+	{
+		std::lock_guard<std::mutex> lock(g_cache_mu);
+		load_locked();
+		auto it = g_cache.find(key);
+		if (it != g_cache.end()) {
+			best = it->second;
+			return SSFFT_SUCCESS;
+		}
+	}
+	// timing batch: the plan's batch, capped so each scratch buffer stays within 256 MiB
+	const size_t sb = p->dtype == SSFFT_F32 ? 4 : 8;
+	const size_t per = (real ? 2 * (size_t)cn + 2 : 2 * (size_t)cn) * sb;
+	const size_t tb = std::max<size_t>(1, std::min(p->batch, ((size_t)256 << 20) / per));
+	Scratch sc;
+	e = cudaMalloc(&sc.in, tb * per);
+	if (e == cudaSuccess) e = cudaMalloc(&sc.out, tb * per);
+	if (e == cudaSuccess) e = cudaMemset(sc.in, 0, tb * per);
+	if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sc.stream, cudaStreamNonBlocking);
+	if (e == cudaSuccess) e = cudaEventCreate(&sc.ev[0]);
+	if (e == cudaSuccess) e = cudaEventCreate(&sc.ev[1]);
+	if (e != cudaSuccess) return cuda_fail(e, "tune scratch");
+
+	std::map<std::string, double> timed;  // kernel name -> total us (identical schedules are timed once)
+	auto run_stage = [&](std::vector<Candidate> &cs) -> ssfft_status {
+		compile_all(p, tb, cs);
+		std::lock_guard<std::mutex> lock(g_time_mu);
+		for (auto &c : cs) {
+			if (c.st != SSFFT_SUCCESS) continue;
+			const std::string nm = c.sch.name(false);
+			auto it = timed.find(nm);
+			if (it != timed.end()) {
+				c.fwd_us = it->second;
+				c.inv_us = 0;
+				continue;
+			}
+			ssfft_status st = time_one(p, tb, sc, c);
+			if (st != SSFFT_SUCCESS) return st;
+			timed[nm] = c.total();
+			char line[256];
+			std::snprintf(line, sizeof line, "%s threads=%dx%d fwd=%.2fus inv=%.2fus\n", c.knobs.str().c_str(),
+			              c.sch.threads, c.sch.per_cta, c.fwd_us, c.inv_us);
+			log += line;
+		}
+		const Candidate *w = nullptr;
+		for (auto &c : cs)
+			if (c.st == SSFFT_SUCCESS && (!w || c.total() < w->total())) w = &c;
+		if (w) best = w->knobs;
+		return SSFFT_SUCCESS;
+	};
+
+	if (level >= 2) {
+		std::vector<std::vector<int>> lists;
+		radix_candidates(cn, lists);
+		std::vector<Candidate> cs;
+		for (auto &l : lists) {
+			Candidate c;
+			c.knobs.radices = l;
+			cs.push_back(c);
+		}
+		if (cs.size() > 1) {
+			ssfft_status st = run_stage(cs);
+			if (st != SSFFT_SUCCESS) return st;
+		}
+	}
+	{
+		std::vector<Candidate> cs;
+		for (int em : {8, 16, 32}) {
+			Candidate c;
+			c.knobs = best;
+			c.knobs.emax = em;
+			cs.push_back(c);
+		}
+		ssfft_status st = run_stage(cs);
+		if (st != SSFFT_SUCCESS) return st;
+	}
+	{
+		std::vector<Candidate> cs;
+		for (int ct : {64, 128, 256, 512}) {
+			Candidate c;
+			c.knobs = best;
+			c.knobs.cta_threads = ct;
+			cs.push_back(c);
+		}
+		ssfft_status st = run_stage(cs);
+		if (st != SSFFT_SUCCESS) return st;
+	}
+	std::lock_guard<std::mutex> lock(g_cache_mu);
+	store_locked(key, best);
+	return SSFFT_SUCCESS;
+}
+
+}  // namespace ssfft

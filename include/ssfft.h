@@ -77,6 +77,27 @@ size_t ssfft_real_size_maximum(size_t n);  /* RealFFT<V>::sizeMaximum  signalsmi
  * real kinds).  Plans are bound to the device that was current at creation. */
 ssfft_status ssfft_plan_create(ssfft_plan_t *plan, size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch);
 ssfft_status ssfft_plan_destroy(ssfft_plan_t plan);
+
+/* Schedule options for ssfft_plan_create_ex (zero-initialise; 0 = planner default).  No reference
+ * counterpart: the reference's plan is fixed by its factorisation (setPlan :139-185). */
+typedef struct ssfft_plan_options {
+    int autotune;          /* 0 off; 1 time candidate CTA shapes and values per thread; 2 also radix
+                            * orders.  Results are cached per (device, n, dtype, kind, batch range) in
+                            * memory and under $SSFFT_CACHE_DIR.  SSFFT_AUTOTUNE=1|2 sets a default. */
+    int cta_threads;       /* target threads per CTA */
+    int values_per_thread; /* complex values a thread holds in one pass (<= 32) */
+    int min_ctas_per_sm;   /* launch bound (register cap) */
+    int radices[24];       /* explicit pass order, 0-terminated; product must equal the complex
+                            * length (n, or n/2 for real kinds) */
+} ssfft_plan_options;
+/* ssfft_plan_create with options (options may be NULL).  Options apply to transforms that run in
+ * one CTA; longer ones use the multi-pass schedule regardless. */
+ssfft_status ssfft_plan_create_ex(ssfft_plan_t *plan, size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch,
+                                  const ssfft_plan_options *options);
+/* The schedule options in force ("radices=16.8.15 cta=128 emax=16 minb=1", 0 = default) and the
+ * autotuner's timings of the candidates it measured for this plan (one line each; empty when
+ * the choice came from the cache).  Text is truncated to len-1 bytes. */
+ssfft_status ssfft_plan_tuning(ssfft_plan_t plan, char *choice, size_t choice_len, char *log, size_t log_len);
 /* Transform size the plan was created for (FFT::size :370-372 / RealFFT::size :442-444). */
 size_t ssfft_plan_size(ssfft_plan_t plan);
 /* Plan's batch, and the device bytes its tables and scratch hold. */
@@ -115,6 +136,9 @@ ssfft_status ssfft_exec_host(ssfft_plan_t plan, int inverse, const void *h_in, v
  * `stream`. */
 typedef struct ssfft_multi_s *ssfft_multi_t;
 ssfft_status ssfft_multi_create(ssfft_multi_t *multi, const size_t *sizes, size_t count, ssfft_dtype dtype);
+/* ssfft_multi_create with plan options for every size (e.g. autotune; radices must be empty). */
+ssfft_status ssfft_multi_create_ex(ssfft_multi_t *multi, const size_t *sizes, size_t count, ssfft_dtype dtype,
+                                   const ssfft_plan_options *options);
 ssfft_status ssfft_multi_exec(ssfft_multi_t multi, int inverse, const void *d_in, void *d_out, void *stream);
 ssfft_status ssfft_multi_exec_plain(ssfft_multi_t multi, int inverse, const void *d_in, void *d_out, void *stream);
 ssfft_status ssfft_multi_info(ssfft_multi_t multi, size_t *distinct_sizes, size_t *total_elements);
