@@ -52,16 +52,43 @@ _vp = ctypes.c_void_p
 class PlanOptions(ctypes.Structure):
     """ssfft_plan_options (0 = planner default)."""
     _fields_ = [("autotune", ctypes.c_int), ("cta_threads", ctypes.c_int), ("values_per_thread", ctypes.c_int),
-                ("min_ctas_per_sm", ctypes.c_int), ("radices", ctypes.c_int * 24)]
+                ("min_ctas_per_sm", ctypes.c_int), ("radices", ctypes.c_int * 24), ("precision", ctypes.c_int)]
 
 
-def _options(autotune=0, radices=None, cta_threads=0, values_per_thread=0, min_ctas_per_sm=0):
+PRECISION = {"fp32": 0, "split_bf16": 1}
+
+
+def _options(autotune=0, radices=None, cta_threads=0, values_per_thread=0, min_ctas_per_sm=0, precision="fp32"):
     o = PlanOptions()
     o.autotune, o.cta_threads = int(autotune), int(cta_threads)
     o.values_per_thread, o.min_ctas_per_sm = int(values_per_thread), int(min_ctas_per_sm)
     for i, r in enumerate(radices or []):
         o.radices[i] = int(r)
+    o.precision = PRECISION[precision] if isinstance(precision, str) else int(precision)
     return o
+
+
+def schedule_options(**opts) -> None:
+    """Options (as for Plan) that schedule_info / schedule_name / schedule_tables / jit_check
+    apply in this thread; no arguments restores the planner defaults."""
+    if opts:
+        o = _options(**opts)
+        check(lib().ssfft_schedule_options(ctypes.byref(o)), "schedule_options")
+    else:
+        check(lib().ssfft_schedule_options(None), "schedule_options")
+
+
+def diag_tc_tile(a: np.ndarray, bt: np.ndarray) -> tuple:
+    """D = A B for one 128 x 32 x 32 FP32 tile through the split-BF16 tensor-core path (GPU).
+    ``bt`` is B transposed.  Returns (D, error flag)."""
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    bt = np.ascontiguousarray(bt, dtype=np.float32)
+    assert a.shape == (128, 32) and bt.shape == (32, 32)
+    d = np.zeros((128, 32), dtype=np.float32)
+    flags = ctypes.c_uint(0)
+    check(lib().ssfft_diag_tc_tile(_vp(a.ctypes.data), _vp(bt.ctypes.data), _vp(d.ctypes.data), ctypes.byref(flags)),
+          "diag_tc_tile")
+    return d, flags.value
 
 
 def _declare(l):
@@ -95,8 +122,11 @@ def _declare(l):
     szp = ctypes.POINTER(_sz)
     l.ssfft_schedule_tables.argtypes = [_sz, _int, _int, _sz, dp, szp, dp, szp, dp, szp, dp, szp]
     l.ssfft_diag_staged_timeout.argtypes = [_sz, ctypes.c_uint, ctypes.POINTER(ctypes.c_uint)]
+    l.ssfft_schedule_options.argtypes = [ctypes.POINTER(PlanOptions)]
+    l.ssfft_diag_tc_tile.argtypes = [_vp, _vp, _vp, ctypes.POINTER(ctypes.c_uint)]
     for name in ("ssfft_plan_create", "ssfft_plan_create_ex", "ssfft_plan_tuning", "ssfft_plan_destroy", "ssfft_plan_describe", "ssfft_exec", "ssfft_exec_batch",
-                 "ssfft_exec_host", "ssfft_plan_error", "ssfft_diag_staged_timeout", "ssfft_jit_check", "ssfft_schedule_info", "ssfft_schedule_name",
+                 "ssfft_exec_host", "ssfft_plan_error", "ssfft_diag_staged_timeout", "ssfft_schedule_options",
+                 "ssfft_diag_tc_tile", "ssfft_jit_check", "ssfft_schedule_info", "ssfft_schedule_name",
                  "ssfft_schedule_tables"):
         getattr(l, name).restype = _int
     return l
@@ -220,13 +250,13 @@ class Plan:
     """One ``ssfft_plan_t``: ``batch`` transforms of size ``n`` (complex or real)."""
 
     def __init__(self, n: int, dtype="f32", kind="complex", batch: int = 1, *, autotune: int = 0, radices=None,
-                 cta_threads: int = 0, values_per_thread: int = 0, min_ctas_per_sm: int = 0):
+                 cta_threads: int = 0, values_per_thread: int = 0, min_ctas_per_sm: int = 0, precision="fp32"):
         self.n = int(n)
         self.dtype = _dtype_code(dtype)
         self.kind = _kind_code(kind)
         self.batch = max(1, int(batch))
         h = _vp()
-        opt = _options(autotune, radices, cta_threads, values_per_thread, min_ctas_per_sm)
+        opt = _options(autotune, radices, cta_threads, values_per_thread, min_ctas_per_sm, precision)
         check(lib().ssfft_plan_create_ex(ctypes.byref(h), self.n, self.dtype, self.kind, self.batch,
                                          ctypes.byref(opt)),
               f"plan_create(n={n}, kind={kind}, batch={batch})")
@@ -609,7 +639,7 @@ def fast_sizes(lo: int, hi: int) -> list:
 class Multi:
     """ssfft_multi_*: one submission of complex transforms of uneven sizes stored back to back."""
 
-    def __init__(self, sizes, dtype="f32", autotune: int = 0):
+    def __init__(self, sizes, dtype="f32", autotune: int = 0, precision="fp32"):
         l = lib()
         if not getattr(l, "_multi_declared", False):
             l.ssfft_multi_create.argtypes = [ctypes.POINTER(_vp), ctypes.POINTER(_sz), _sz, _int]
@@ -626,7 +656,7 @@ class Multi:
         self.sizes = [int(n) for n in sizes]
         arr = (_sz * len(self.sizes))(*self.sizes)
         h = _vp()
-        opt = _options(autotune)
+        opt = _options(autotune, precision=precision)
         check(l.ssfft_multi_create_ex(ctypes.byref(h), arr, len(self.sizes), _dtype_code(dtype), ctypes.byref(opt)),
               "multi_create")
         self._h = h

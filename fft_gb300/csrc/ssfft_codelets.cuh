@@ -39,6 +39,8 @@ struct Args {
 	const long long *offs;    // batch kernel: if set, transform g starts offs[g] scalars into in and out
 	unsigned int drop_copy;   // staged kernels, failure-detection check only: the barrier expects each
 	                          // group's bytes but no copy is issued, so every wait runs out (0 normally)
+	const float *tcb;         // tensor-core kernels: the first pass's DFT as a 32 x 32 real matrix
+	                          // [output column][input column] (FP32 values of FP64-built roots)
 };
 
 enum : int { kComplex = 0, kReal = 1, kRealHalfShift = 2 };
@@ -692,6 +694,367 @@ __global__ void __launch_bounds__(THREADS *PER_CTA, MINB) batch_staged(const Arg
 		}
 		if constexpr (R2C) real_post<T, N, THREADS, KIND, INV, INV>(c, rtw);
 		__syncthreads();  // the work buffer is reused by the next group
+	}
+}
+
+
+// ------------------------------------------------------------------ split-BF16 tensor-core pass
+
+// The first pass (radix R0 <= 16, no twiddles) as a matrix product on the tensor cores.  Each
+// butterfly j of transform g is one row of A: [Re x_r | Im x_r] for r < R0 (x_r = element
+// j + r*NB), zero-padded to 32 columns; B is the radix-R0 DFT in the same real form, so row
+// [Re y_k | Im y_k] of D = A B holds the butterfly's outputs.  FP32 operands do not feed the
+// tensor cores, so each is split into three BF16 parts, x = x0 + x1 + x2 (8 significant bits
+// each, exact to ~2^-24 |x|), and the six products x_a w_b with a + b <= 2 accumulate in FP32
+// in tensor memory (the three dropped products are below 2^-24 relative).  128 rows form one
+// M=128, N=32, K=16 tcgen05.mma tile; 6 products x 2 K-steps = 12 MMAs per tile, issued by one
+// thread, completed on an mbarrier (bounded wait), read back with tcgen05.ld (one row per lane
+// of warps 0-3) and written to shared memory in the Stockham order the next pass expects.
+//
+// Operand layout in shared memory: the no-swizzle K-major canonical layout, 8-row x 16-byte
+// core matrices stored as 128 contiguous bytes; core matrices adjacent in K are kTcLbo bytes
+// apart, 8-row groups kTcSbo bytes apart.  One A part is 128 x 32 BF16 = 8 KiB, one B part
+// 32 x 32 BF16 = 2 KiB.
+constexpr unsigned kTcLbo = 128, kTcSbo = 512;
+constexpr unsigned kTcAPart = 8192, kTcBPart = 2048;
+__host__ __device__ constexpr unsigned tc_off_a(int per_cta, int stride) {
+	return ((unsigned)per_cta * (unsigned)stride * 8u + 1023u) & ~1023u;
+}
+__host__ __device__ constexpr unsigned tc_smem_bytes(int per_cta, int stride) {
+	return tc_off_a(per_cta, stride) + 3 * kTcAPart + 3 * kTcBPart + 16;
+}
+__host__ __device__ constexpr unsigned tc_core_off(int row, int k) {
+	return (unsigned)(row >> 3) * kTcSbo + (unsigned)(k >> 3) * kTcLbo + (unsigned)(row & 7) * 16u + (unsigned)(k & 7) * 2u;
+}
+// instruction descriptor (kind::f16): D FP32 (bits 4-5 = 1), A and B BF16 (bits 7-9 = 1,
+// 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28
+constexpr unsigned kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
+
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ unsigned short f2bf(float x) {
+	unsigned short r;
+	asm("cvt.rn.bf16.f32 %0, %1;" : "=h"(r) : "f"(x));
+	return r;
+}
+__device__ __forceinline__ float bf2f(unsigned short h) { return __uint_as_float((unsigned)h << 16); }
+// shared-memory matrix descriptor: start >> 4 (bits 0-13), LBO >> 4 (16-29), SBO >> 4 (32-45),
+// fixed 0b001 at bits 46-48, no swizzle (bits 61-63 = 0)
+__device__ __forceinline__ unsigned long long tc_desc(const void *p) {
+	return (unsigned long long)((smem_u32(p) & 0x3FFFFu) >> 4) | ((unsigned long long)(kTcLbo >> 4) << 16) |
+	       ((unsigned long long)(kTcSbo >> 4) << 32) | (1ull << 46);
+}
+__device__ __forceinline__ void tmem_alloc32(unsigned *slot) {
+	asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(smem_u32(slot)) : "memory");
+	asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc32(unsigned taddr) {
+	asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(taddr) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_mma(unsigned d, unsigned long long a, unsigned long long b, int acc) {
+	asm volatile(
+	    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+	    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+	    "l"(a), "l"(b), "r"(kTcIdesc), "r"(acc)
+	    : "memory");
+}
+__device__ __forceinline__ void tc_commit(unsigned long long *bar) {
+	asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+	             : "memory");
+}
+// 32 consecutive FP32 columns of this thread's lane; the wait is inside the same statement so
+// the values are complete when they are used
+__device__ __forceinline__ void tc_ld32(unsigned taddr, float (&v)[32]) {
+	unsigned r[32];
+	asm volatile(
+	    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+	    "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n\t"
+	    "tcgen05.wait::ld.sync.aligned;"
+	    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+	      "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+	      "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+	      "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+	    : "r"(taddr)
+	    : "memory");
+#pragma unroll
+	for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+#elif defined(SSFFT_EMULATION)
+// Host emulation: tensor memory is one 128-lane x 32-column array (the emulator runs one CTA at
+// a time), the MMA decodes the same descriptors the device would and computes in FP32.
+unsigned short f2bf(float x);
+float bf2f(unsigned short h);
+extern float emu_tmem[128][32];
+inline unsigned long long tc_desc(const void *p) {
+	const unsigned off = (unsigned)(static_cast<const unsigned char *>(p) - smem_raw);
+	return (unsigned long long)((off & 0x3FFFFu) >> 4) | ((unsigned long long)(kTcLbo >> 4) << 16) |
+	       ((unsigned long long)(kTcSbo >> 4) << 32) | (1ull << 46);
+}
+inline void tmem_alloc32(unsigned *slot) {
+	if (threadIdx.x == 0) *slot = 0;
+}
+inline void tmem_dealloc32(unsigned) {}
+inline void tc_fence_before() {}
+inline void tc_fence_after() {}
+inline void tc_mma(unsigned d, unsigned long long a, unsigned long long b, int acc) {
+	const unsigned m_dim = ((kTcIdesc >> 24) & 31u) << 4, n_dim = ((kTcIdesc >> 17) & 63u) << 3;
+	auto elem = [](unsigned long long desc, unsigned row, unsigned k) {
+		const unsigned start = (unsigned)(desc & 0x3FFFu) << 4;
+		const unsigned lbo = (unsigned)((desc >> 16) & 0x3FFFu) << 4, sbo = (unsigned)((desc >> 32) & 0x3FFFu) << 4;
+		const unsigned off = start + (row >> 3) * sbo + (k >> 3) * lbo + (row & 7) * 16 + (k & 7) * 2;
+		unsigned short h;
+		std::memcpy(&h, smem_raw + off, 2);
+		return bf2f(h);
+	};
+	const unsigned lane0 = d >> 16, col0 = d & 0xFFFFu;
+	for (unsigned m = 0; m < m_dim; ++m)
+		for (unsigned n = 0; n < n_dim; ++n) {
+			float sum = 0;
+			for (unsigned k = 0; k < 16; ++k) sum += elem(a, m, k) * elem(b, n, k);
+			float &dst = emu_tmem[lane0 + m][col0 + n];
+			dst = acc ? dst + sum : sum;
+		}
+}
+inline void tc_commit(unsigned long long *) {}
+inline void tc_ld32(unsigned taddr, float (&v)[32]) {
+	const unsigned lane = (taddr >> 16) + (threadIdx.x & 31u), col = taddr & 0xFFFFu;
+	for (int i = 0; i < 32; ++i) v[i] = emu_tmem[lane][col + i];
+}
+#else
+// host pass of the library build: declarations only (the kernels are device code)
+unsigned short f2bf(float x);
+float bf2f(unsigned short h);
+unsigned long long tc_desc(const void *p);
+void tmem_alloc32(unsigned *slot);
+void tmem_dealloc32(unsigned taddr);
+void tc_fence_before();
+void tc_fence_after();
+void tc_mma(unsigned d, unsigned long long a, unsigned long long b, int acc);
+void tc_commit(unsigned long long *bar);
+void tc_ld32(unsigned taddr, float (&v)[32]);
+#endif
+
+// x = x0 + x1 + x2 in BF16 parts
+__device__ __forceinline__ void split3(float x, unsigned short &h0, unsigned short &h1, unsigned short &h2) {
+	h0 = f2bf(x);
+	float r = x - bf2f(h0);
+	h1 = f2bf(r);
+	r -= bf2f(h1);
+	h2 = f2bf(r);
+}
+
+// Complex FP32 transforms whose first pass (radix R0 <= 16) runs on the tensor cores and whose
+// remaining passes (Rest...) are the FP32 passes of the batch kernel.  At least 128 threads per
+// CTA (rows of a tile are built and read back by threads 0-127).  A bounded wait that runs out
+// sets *err, waits once more (bounded) for the MMAs in flight, frees the tensor memory and
+// returns without writing.
+template <int N, int THREADS, int PER_CTA, int SMEM_STRIDE, bool INV, int EMAX, int MINB, int R0, int... Rest>
+__global__ void __launch_bounds__(THREADS *PER_CTA, MINB) batch_tc(const Args a) {
+	using T = float;
+	using C = float2;
+	constexpr int CT = THREADS * PER_CTA;
+	static_assert(CT >= 128, "the tensor-core pass reads 128 accumulator lanes");
+	static_assert(R0 >= 2 && R0 <= 16 && N % R0 == 0, "first radix must fit the 32-column tile");
+	constexpr int NB = N / R0;
+	constexpr int ROWS = NB * PER_CTA;
+	constexpr int TILES = (ROWS + 127) / 128;
+	constexpr int PS = Cx<T>::kPadShift;
+	constexpr bool LAST = sizeof...(Rest) == 0;
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	constexpr unsigned OFF_A = tc_off_a(PER_CTA, SMEM_STRIDE);
+	constexpr unsigned OFF_B = OFF_A + 3 * kTcAPart;
+	constexpr unsigned OFF_BAR = OFF_B + 3 * kTcBPart;
+	unsigned char *tile_a = smem_raw + OFF_A;
+	unsigned char *tile_b = smem_raw + OFF_B;
+	unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem_raw + OFF_BAR);
+	unsigned *slot = reinterpret_cast<unsigned *>(smem_raw + OFF_BAR + 8);
+	const int tid = threadIdx.x;
+	const int warp = tid >> 5;
+
+	if (tid == 0) mbar_init(bar, 1);
+	if (warp == 0) tmem_alloc32(slot);
+	// B parts: the split DFT matrix (K-major: row n = output column, k = input column)
+	for (int idx = tid; idx < 32 * 32; idx += CT) {
+		const int n = idx >> 5, k = idx & 31;
+		unsigned short h0, h1, h2;
+		split3(__ldg(a.tcb + idx), h0, h1, h2);
+		const unsigned o = tc_core_off(n, k);
+		*reinterpret_cast<unsigned short *>(tile_b + o) = h0;
+		*reinterpret_cast<unsigned short *>(tile_b + kTcBPart + o) = h1;
+		*reinterpret_cast<unsigned short *>(tile_b + 2 * kTcBPart + o) = h2;
+	}
+	fence_async_smem();
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+	const unsigned taddr = *slot;
+	const float2 *in = reinterpret_cast<const float2 *>(a.in);
+	unsigned phase = 0;
+	bool failed = false;
+
+	for (int tile = 0; tile < TILES; ++tile) {
+		const int row = tile * 128 + tid;
+		const int g = row / NB, j = row - (row / NB) * NB;
+		const long long gi = (long long)blockIdx.x * PER_CTA + g;
+		const bool live = tid < 128 && row < ROWS && gi < a.batch;
+		if (tid < 128) {
+			// this row of the three A parts, packed two BF16 per word: columns 0-15 real parts,
+			// 16-31 imaginary parts (zero beyond R0)
+			unsigned w[3][16];
+#pragma unroll
+			for (int q = 0; q < 16; ++q) w[0][q] = w[1][q] = w[2][q] = 0;
+			if (live) {
+				const float2 *src = in + (a.offs ? a.offs[gi] : gi * a.in_dist) / 2;
+#pragma unroll
+				for (int r = 0; r < R0; ++r) {
+					float2 v = __ldcs(src + j + r * NB);
+					if (INV) v.y = -v.y;
+					unsigned short h[2][3];
+					split3(v.x, h[0][0], h[0][1], h[0][2]);
+					split3(v.y, h[1][0], h[1][1], h[1][2]);
+#pragma unroll
+					for (int part = 0; part < 2; ++part) {
+						const int k = part * 16 + r;
+#pragma unroll
+						for (int sp = 0; sp < 3; ++sp) w[sp][k >> 1] |= (unsigned)h[part][sp] << ((k & 1) * 16);
+					}
+				}
+			}
+#pragma unroll
+			for (int sp = 0; sp < 3; ++sp)
+#pragma unroll
+				for (int kb = 0; kb < 4; ++kb) {
+					unsigned *dst = reinterpret_cast<unsigned *>(tile_a + sp * kTcAPart + tc_core_off(tid, kb * 8));
+					dst[0] = w[sp][kb * 4];
+					dst[1] = w[sp][kb * 4 + 1];
+					dst[2] = w[sp][kb * 4 + 2];
+					dst[3] = w[sp][kb * 4 + 3];
+				}
+		}
+		fence_async_smem();
+		tc_fence_before();
+		__syncthreads();
+		if (tid == 0) {
+			tc_fence_after();
+			// smallest products first: (x2 w0), (x1 w1), (x0 w2), (x1 w0), (x0 w1), (x0 w0)
+			const int pa[6] = {2, 1, 0, 1, 0, 0}, pb[6] = {0, 1, 2, 0, 1, 0};
+#pragma unroll
+			for (int q = 0; q < 6; ++q)
+#pragma unroll
+				for (int ks = 0; ks < 2; ++ks)
+					tc_mma(taddr, tc_desc(tile_a + pa[q] * kTcAPart + ks * 2 * kTcLbo),
+					       tc_desc(tile_b + pb[q] * kTcBPart + ks * 2 * kTcLbo), q + ks > 0);
+			tc_commit(bar);
+		}
+		const bool ok = mbar_wait_bounded(bar, phase, a.spin_limit);
+		phase ^= 1u;
+		if (__syncthreads_or(!ok)) {
+			if (tid == 0) atomicOr(a.err, 1u);
+			mbar_wait_bounded(bar, phase ^ 1u, a.spin_limit);  // let the MMAs in flight finish
+			failed = true;
+			break;
+		}
+		tc_fence_after();
+		if (tid < 128) {
+			float v[32];
+			tc_ld32(taddr + ((unsigned)(warp * 32) << 16), v);
+			if (live) {
+				if constexpr (LAST) {
+					C *dst = reinterpret_cast<C *>(a.out) + (a.offs ? a.offs[gi] : gi * a.out_dist) / 2;
+#pragma unroll
+					for (int k = 0; k < R0; ++k) __stcs(dst + j * R0 + k, make_float2(v[k], INV ? -v[16 + k] : v[16 + k]));
+				} else {
+					C *sm = reinterpret_cast<C *>(smem_raw) + g * SMEM_STRIDE;
+#pragma unroll
+					for (int k = 0; k < R0; ++k) sm[pidx<PS>(j * R0 + k)] = make_float2(v[k], v[16 + k]);
+				}
+			}
+		}
+		tc_fence_before();
+		__syncthreads();
+	}
+	if (warp == 0) {
+		tc_fence_after();
+		tmem_dealloc32(taddr);
+	}
+	if (failed) return;
+	if constexpr (!LAST) {
+		const int g = tid / THREADS;
+		const long long gi = (long long)blockIdx.x * PER_CTA + g;
+		Ctx<T, kComplex, INV, INV> c;
+		c.t = tid - g * THREADS;
+		c.valid = gi < a.batch;
+		c.sm = reinterpret_cast<C *>(smem_raw) + g * SMEM_STRIDE;
+		long long oout = 0;
+		if (c.valid) oout = a.offs ? a.offs[gi] : gi * a.out_dist;
+		c.gin = nullptr;
+		c.gout = reinterpret_cast<T *>(a.out) + oout;
+		c.rot = nullptr;
+		passes<T, N, THREADS, R0, 0, RootCount<R0>::value, kSmem, kGlobal, kComplex, INV, INV, false, EMAX, Rest...>(
+		    c, reinterpret_cast<const C *>(a.tw), reinterpret_cast<const C *>(a.roots));
+	}
+}
+
+// Failure-free check of the tensor-core tile on its own: D = A B for one 128 x 32 x 32 tile of
+// FP32 inputs (A row-major 128 x 32, B given as its transpose 32 x 32 in a.tcb, D row-major
+// 128 x 32 to a.out), through the same split, layout, MMA and read-back as batch_tc.
+template <int UNUSED = 0>
+__global__ void __launch_bounds__(128, 1) tc_tile_check(const Args a) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	unsigned char *tile_a = smem_raw;
+	unsigned char *tile_b = smem_raw + 3 * kTcAPart;
+	unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem_raw + 3 * kTcAPart + 3 * kTcBPart);
+	unsigned *slot = reinterpret_cast<unsigned *>(smem_raw + 3 * kTcAPart + 3 * kTcBPart + 8);
+	const int tid = threadIdx.x, warp = tid >> 5;
+	const float *A = static_cast<const float *>(a.in);
+	if (tid == 0) mbar_init(bar, 1);
+	if (warp == 0) tmem_alloc32(slot);
+	for (int idx = tid; idx < 32 * 32; idx += 128) {
+		unsigned short h0, h1, h2;
+		split3(__ldg(a.tcb + idx), h0, h1, h2);
+		const unsigned o = tc_core_off(idx >> 5, idx & 31);
+		*reinterpret_cast<unsigned short *>(tile_b + o) = h0;
+		*reinterpret_cast<unsigned short *>(tile_b + kTcBPart + o) = h1;
+		*reinterpret_cast<unsigned short *>(tile_b + 2 * kTcBPart + o) = h2;
+	}
+	for (int k = 0; k < 32; ++k) {
+		unsigned short h0, h1, h2;
+		split3(A[tid * 32 + k], h0, h1, h2);
+		const unsigned o = tc_core_off(tid, k);
+		*reinterpret_cast<unsigned short *>(tile_a + o) = h0;
+		*reinterpret_cast<unsigned short *>(tile_a + kTcAPart + o) = h1;
+		*reinterpret_cast<unsigned short *>(tile_a + 2 * kTcAPart + o) = h2;
+	}
+	fence_async_smem();
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+	const unsigned taddr = *slot;
+	if (tid == 0) {
+		const int pa[6] = {2, 1, 0, 1, 0, 0}, pb[6] = {0, 1, 2, 0, 1, 0};
+		for (int q = 0; q < 6; ++q)
+			for (int ks = 0; ks < 2; ++ks)
+				tc_mma(taddr, tc_desc(tile_a + pa[q] * kTcAPart + ks * 2 * kTcLbo),
+				       tc_desc(tile_b + pb[q] * kTcBPart + ks * 2 * kTcLbo), q + ks > 0);
+		tc_commit(bar);
+	}
+	const bool ok = mbar_wait_bounded(bar, 0, a.spin_limit);
+	if (__syncthreads_or(!ok)) {
+		if (tid == 0) atomicOr(a.err, 1u);
+		mbar_wait_bounded(bar, 0, a.spin_limit);
+	} else {
+		tc_fence_after();
+		float v[32];
+		tc_ld32(taddr + ((unsigned)(warp * 32) << 16), v);
+		float *D = static_cast<float *>(a.out);
+		for (int k = 0; k < 32; ++k) D[tid * 32 + k] = v[k];
+	}
+	tc_fence_before();
+	__syncthreads();
+	if (warp == 0) {
+		tc_fence_after();
+		tmem_dealloc32(taddr);
 	}
 }
 

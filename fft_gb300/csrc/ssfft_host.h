@@ -30,6 +30,7 @@ struct Schedule {
 	int kind = 0;             // ssfft_cl::kComplex / kReal / kRealHalfShift
 	bool odd = false;         // real length is odd (scalar loads/stores)
 	bool staged = false;      // ssfft_cl::batch_staged (bulk-copy input staging, persistent CTAs)
+	bool tc = false;          // ssfft_cl::batch_tc (first pass as split-BF16 tensor-core products)
 	int minb = 1;             // launch-bound CTAs per SM (register cap)
 	int emax = 16;            // complex values a thread holds in one pass
 	unsigned in_bytes = 0;    // staged: input bytes of one transform
@@ -45,6 +46,8 @@ struct Knobs {
 	int cta_threads = 0;       // target threads per CTA
 	int emax = 0;              // complex values a thread holds in one pass
 	int minb = 0;              // launch-bound CTAs per SM
+	int precision = 0;         // SSFFT_PRECISION_*: 1 = first pass on the tensor cores (split BF16)
+	// no shape choice made (precision is not a shape choice)
 	bool empty() const { return radices.empty() && !cta_threads && !emax && !minb; }
 	std::string str() const;
 };
@@ -52,6 +55,7 @@ struct Knobs {
 // Device tables of one schedule (all inside the plan's single table allocation).
 struct Tables {
 	const void *tw = nullptr, *roots = nullptr, *rtw = nullptr, *rot = nullptr;
+	const float *tcb = nullptr;  // tensor-core schedules: the first pass's DFT, 32 x 32 FP32
 };
 
 struct SubPlan {
@@ -109,6 +113,7 @@ bool single_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch,
 void single_tables(const Schedule &s, size_t n_real, std::vector<double> &tw, std::vector<double> &roots,
                    std::vector<double> &rtw, std::vector<double> &rot);
 void radix_candidates(int n, std::vector<std::vector<int>> &out);
+void tc_matrix(int r0, std::vector<float> &bt);
 // autotuner (ssfft_tune.cu): picks knobs for a single-CTA plan, cached per device and shape
 ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log);
 void schedule_twiddles(const Schedule &s, std::vector<double> &tw, std::vector<double> &roots);

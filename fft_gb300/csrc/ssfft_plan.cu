@@ -214,6 +214,7 @@ std::string Knobs::str() const {
 	for (size_t i = 0; i < radices.size(); ++i) r += (i ? "." : "") + std::to_string(radices[i]);
 	if (radices.empty()) r += "default";
 	r += " cta=" + std::to_string(cta_threads) + " emax=" + std::to_string(emax) + " minb=" + std::to_string(minb);
+	if (precision == 1) r += " precision=split_bf16";
 	return r;
 }
 
@@ -236,6 +237,13 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	} else if (!choose_radices(n, s.radices)) {
 		return false;
 	}
+	// split-BF16 tensor-core first pass: complex FP32, first radix <= 16 (moved to the front)
+	const bool want_tc = knobs && knobs->precision == 1 && kind == 0 && dtype == SSFFT_F32 && n >= 2;
+	if (want_tc && s.radices[0] > 16) {
+		auto it = std::find_if(s.radices.begin(), s.radices.end(), [](int r) { return r >= 2 && r <= 16; });
+		if (it != s.radices.end()) std::rotate(s.radices.begin(), it, it + 1);
+	}
+	s.tc = want_tc && s.radices[0] >= 2 && s.radices[0] <= 16;
 	// threads per transform: every pass must fit its butterflies into `emax` values per thread;
 	// 16 normally, 32 when 16 would need more than one CTA's threads (long sizes whose composite
 	// radices hold a single butterfly per thread)
@@ -281,9 +289,15 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	while (g > 1 && (size_t)g * per > soft) --g;
 	if (batch > 0 && (size_t)g > batch) g = (int)batch;
 	s.per_cta = std::max(1, g);
+	if (s.tc) {
+		// the tensor-core pass needs 128 threads (one accumulator lane per row)
+		while (s.per_cta * t < 128) ++s.per_cta;
+		if (s.per_cta * t > kMaxCtaThreads) s.tc = false, s.per_cta = std::max(1, g);
+	}
 	s.smem_bytes = (size_t)s.per_cta * per;
 	// a single-pass complex transform never touches shared memory
 	if (kind == 0 && s.radices.size() == 1) s.smem_bytes = 0;
+	if (s.tc) s.smem_bytes = ssfft_cl::tc_smem_bytes(s.per_cta, s.smem_stride);
 	// Staged input (bulk copies into shared memory, persistent CTAs) when one transform's input is
 	// a whole number of 16-byte units and a group of them fits the copy and shared-memory limits.
 	const size_t sb = eb / 2;
@@ -292,7 +306,7 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	// kernel on GB300 so far.
 	const char *staged_env = std::getenv("SSFFT_STAGED");
 	const bool staged_enabled = staged_env && staged_env[0] == '1';
-	if (((allow_staged == 1 && staged_enabled) || allow_staged == 2) && !odd && in_bytes % 16 == 0 && n >= 16) {
+	if (((allow_staged == 1 && staged_enabled) || allow_staged == 2) && !s.tc && !odd && in_bytes % 16 == 0 && n >= 16) {
 		int gs = s.per_cta;
 		auto staged_smem = [&](int gg) { return (((size_t)gg * in_bytes + 127) & ~(size_t)127) + (size_t)gg * per; };
 		while (gs > 1 && staged_smem(gs) > 76 * 1024) --gs;
@@ -318,6 +332,13 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 }
 
 std::string Schedule::name(bool inverse) const {
+	if (tc) {
+		std::string r = "ssfft_cl::batch_tc<" + std::to_string(n) + ", " + std::to_string(threads) + ", " +
+		                std::to_string(per_cta) + ", " + std::to_string(smem_stride) + ", " +
+		                (inverse ? "true" : "false") + ", " + std::to_string(emax) + ", " + std::to_string(minb);
+		for (int x : radices) r += ", " + std::to_string(x);
+		return r + ">";
+	}
 	std::string r = staged ? "ssfft_cl::batch_staged<" : "ssfft_cl::batch<";
 	r += dtype == SSFFT_F32 ? "float" : "double";
 	r += ", " + std::to_string(n) + ", " + std::to_string(threads) + ", " + std::to_string(per_cta) + ", " +
@@ -402,6 +423,23 @@ void single_tables(const Schedule &s, size_t n_real, std::vector<double> &tw, st
 		}
 }
 
+// The radix-r0 DFT (r0 <= 16) as the 32 x 32 real matrix of the tensor-core pass, transposed
+// (row = output column): inputs [Re x_r | Im x_r], outputs [Re y_k | Im y_k] in 16-column halves,
+// y_k = sum_r x_r e^{-2 pi i r k / r0}; zero outside r, k < r0.  FP64 roots, rounded to FP32.
+void tc_matrix(int r0, std::vector<float> &bt) {
+	bt.assign(32 * 32, 0.0f);
+	for (int k = 0; k < r0; ++k)
+		for (int r = 0; r < r0; ++r) {
+			double re, im;  // e^{-2 pi i rk/r0} = c - i s
+			unit_root((unsigned long long)r * k, (unsigned long long)r0, &re, &im);
+			const float c = (float)re, sn = (float)-im;
+			bt[k * 32 + r] = c;             // Re y_k += Re x_r c
+			bt[k * 32 + 16 + r] = sn;       // Re y_k += Im x_r s
+			bt[(16 + k) * 32 + r] = -sn;    // Im y_k -= Re x_r s
+			bt[(16 + k) * 32 + 16 + r] = c; // Im y_k += Im x_r c
+		}
+}
+
 static ssfft_status plan_build_single(Plan *p) {
 	Schedule &s = p->main.sch;
 	{
@@ -415,7 +453,7 @@ static ssfft_status plan_build_single(Plan *p) {
 		if (st != SSFFT_SUCCESS) return st;
 		p->knobs = best;
 	}
-	if (!single_schedule(p->n, p->dtype, p->kind, p->batch, s, p->knobs.empty() ? nullptr : &p->knobs))
+	if (!single_schedule(p->n, p->dtype, p->kind, p->batch, s, &p->knobs))
 		return SSFFT_ERR_INVALID_VALUE;  // explicit knobs that do not fit this size
 	if (s.smem_bytes > device_smem_limit(p->device)) return SSFFT_ERR_UNSUPPORTED;
 	std::vector<double> tw, roots, rtw, rot;
@@ -425,7 +463,10 @@ static ssfft_status plan_build_single(Plan *p) {
 	const size_t off_roots = align_up(off_tw + tw.size() * sb, 256);
 	const size_t off_rtw = align_up(off_roots + roots.size() * sb, 256);
 	const size_t off_rot = align_up(off_rtw + rtw.size() * sb, 256);
-	const size_t off_err = align_up(off_rot + rot.size() * sb, 256);
+	std::vector<float> tcb;
+	if (s.tc) tc_matrix(s.radices[0], tcb);
+	const size_t off_tcb = align_up(off_rot + rot.size() * sb, 256);
+	const size_t off_err = align_up(off_tcb + tcb.size() * 4, 256);
 	const size_t total = align_up(off_err + 16, 256);
 	std::vector<unsigned char> blob(total, 0);
 	if (sb == 4) {
@@ -439,6 +480,7 @@ static ssfft_status plan_build_single(Plan *p) {
 		put_table<double>(blob, off_rtw, rtw);
 		put_table<double>(blob, off_rot, rot);
 	}
+	if (!tcb.empty()) std::memcpy(blob.data() + off_tcb, tcb.data(), tcb.size() * 4);
 	cudaError_t e = cudaMalloc(&p->d_tables, total);
 	if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(tables)");
 	p->table_bytes = total;
@@ -449,6 +491,7 @@ static ssfft_status plan_build_single(Plan *p) {
 	p->main.tab.roots = base + off_roots;
 	p->main.tab.rtw = base + off_rtw;
 	p->main.tab.rot = base + off_rot;
+	p->main.tab.tcb = tcb.empty() ? nullptr : reinterpret_cast<const float *>(base + off_tcb);
 	p->main.err = reinterpret_cast<unsigned *>(static_cast<unsigned char *>(p->d_tables) + off_err);
 
 	std::vector<CUfunction> fns;
@@ -497,7 +540,8 @@ size_t plan_out_bytes(const Plan *p, int inverse, size_t batch) {
 // schedule (compiled on first use).
 static ssfft_status unstaged_kernels(const Plan *p, Schedule &u, std::vector<CUfunction> &fns) {
 	const Schedule &st = p->main.sch;
-	if (!make_schedule(st.dtype, st.n, st.kind, st.odd, p->batch, u, 0)) return SSFFT_ERR_UNSUPPORTED;
+	if (!make_schedule(st.dtype, st.n, st.kind, st.odd, p->batch, u, 0, p->knobs.empty() ? nullptr : &p->knobs))
+		return SSFFT_ERR_UNSUPPORTED;
 	return jit_kernels({u.name(false), u.name(true)}, u.smem_bytes, fns);
 }
 
@@ -549,6 +593,9 @@ ssfft_status launch_batch_offs(const Plan *p, int inverse, const void *in, void 
 	a.rtw = p->main.tab.rtw;
 	a.rot = p->main.tab.rot;
 	a.roots = p->main.tab.roots;
+	a.tcb = p->main.tab.tcb;
+	a.err = p->main.err;
+	a.spin_limit = 1u << 22;
 	a.offs = d_offs;
 	const long long grid = ((long long)batch + sch.per_cta - 1) / sch.per_cta;
 	if (grid > 0x7fffffffLL) return SSFFT_ERR_INVALID_SIZE;
@@ -572,6 +619,7 @@ ssfft_status launch_batch(const Plan *p, int inverse, const void *in, void *out,
 	a.err = p->main.err;
 	a.spin_limit = 1u << 22;
 	a.in_bytes = sch.in_bytes;
+	a.tcb = p->main.tab.tcb;
 	long long grid = ((long long)batch + sch.per_cta - 1) / sch.per_cta;
 	if (sch.staged) {
 		if ((uintptr_t)in % 16) return launch_unstaged(p, inverse, in, out, batch, s);
@@ -651,6 +699,11 @@ ssfft_status ssfft_plan_create_ex(ssfft_plan_t *out, size_t n, ssfft_dtype dtype
 		p->knobs.cta_threads = opt->cta_threads;
 		p->knobs.emax = opt->values_per_thread;
 		p->knobs.minb = opt->min_ctas_per_sm;
+		if (opt->precision != SSFFT_PRECISION_FP32 && opt->precision != SSFFT_PRECISION_SPLIT_BF16) {
+			delete p;
+			return SSFFT_ERR_INVALID_VALUE;
+		}
+		p->knobs.precision = opt->precision;
 		for (int i = 0; i < 24 && opt->radices[i] > 0; ++i) p->knobs.radices.push_back(opt->radices[i]);
 	}
 	cudaError_t e = cudaGetDevice(&p->device);
@@ -817,17 +870,72 @@ ssfft_status ssfft_diag_staged_timeout(size_t n, unsigned spin_limit, unsigned *
 // ---------------------------------------------------------------- diagnostics (no GPU needed)
 
 // Compile the kernels a plan of this shape would use (build-time check).
+static thread_local Knobs g_diag_knobs;  // options of the schedule diagnostics in this thread
+
+ssfft_status ssfft_schedule_options(const ssfft_plan_options *opt) {
+	g_diag_knobs = Knobs();
+	if (!opt) return SSFFT_SUCCESS;
+	if (opt->precision != SSFFT_PRECISION_FP32 && opt->precision != SSFFT_PRECISION_SPLIT_BF16)
+		return SSFFT_ERR_INVALID_VALUE;
+	g_diag_knobs.cta_threads = opt->cta_threads;
+	g_diag_knobs.emax = opt->values_per_thread;
+	g_diag_knobs.minb = opt->min_ctas_per_sm;
+	g_diag_knobs.precision = opt->precision;
+	for (int i = 0; i < 24 && opt->radices[i] > 0; ++i) g_diag_knobs.radices.push_back(opt->radices[i]);
+	return SSFFT_SUCCESS;
+}
+
+ssfft_status ssfft_diag_tc_tile(const float *h_a, const float *h_bt, float *h_d, unsigned *flags) {
+	if (!h_a || !h_bt || !h_d || !flags) return SSFFT_ERR_INVALID_VALUE;
+	*flags = 0;
+	float *d_a = nullptr, *d_b = nullptr, *d_d = nullptr;
+	unsigned *d_err = nullptr;
+	cudaError_t e = cudaMalloc(&d_a, 128 * 32 * 4);
+	if (e == cudaSuccess) e = cudaMalloc(&d_b, 32 * 32 * 4);
+	if (e == cudaSuccess) e = cudaMalloc(&d_d, 128 * 32 * 4);
+	if (e == cudaSuccess) e = cudaMalloc(&d_err, sizeof(unsigned));
+	if (e == cudaSuccess) e = cudaMemcpy(d_a, h_a, 128 * 32 * 4, cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) e = cudaMemcpy(d_b, h_bt, 32 * 32 * 4, cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) e = cudaMemset(d_d, 0, 128 * 32 * 4);
+	if (e == cudaSuccess) e = cudaMemset(d_err, 0, sizeof(unsigned));
+	ssfft_status st = e == cudaSuccess ? SSFFT_SUCCESS : cuda_fail(e, "tc tile setup");
+	const size_t smem = 3 * ssfft_cl::kTcAPart + 3 * ssfft_cl::kTcBPart + 16;
+	std::vector<CUfunction> fns;
+	if (st == SSFFT_SUCCESS) st = jit_kernels({"ssfft_cl::tc_tile_check<0>"}, smem, fns);
+	if (st == SSFFT_SUCCESS) {
+		ssfft_cl::Args a;
+		std::memset(&a, 0, sizeof a);
+		a.in = d_a;
+		a.out = d_d;
+		a.tcb = d_b;
+		a.err = d_err;
+		a.spin_limit = 1u << 20;
+		st = jit_launch(fns[0], 1, 128, smem, nullptr, &a);
+	}
+	if (st == SSFFT_SUCCESS) {
+		e = cudaDeviceSynchronize();
+		if (e == cudaSuccess) e = cudaMemcpy(h_d, d_d, 128 * 32 * 4, cudaMemcpyDeviceToHost);
+		if (e == cudaSuccess) e = cudaMemcpy(flags, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+		if (e != cudaSuccess) st = cuda_fail(e, "tc tile");
+	}
+	cudaFree(d_a);
+	cudaFree(d_b);
+	cudaFree(d_d);
+	cudaFree(d_err);
+	return st;
+}
+
 ssfft_status ssfft_jit_check(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, const char *arch,
                              size_t *image_bytes) {
 	Schedule s;
-	if (!single_schedule(n, dtype, kind, batch, s)) return large_jit_check(n, dtype, kind, arch ? arch : "sm_103a", image_bytes);
+	if (!single_schedule(n, dtype, kind, batch, s, &g_diag_knobs)) return large_jit_check(n, dtype, kind, arch ? arch : "sm_103a", image_bytes);
 	return jit_compile_only({s.name(false), s.name(true)}, arch ? arch : "sm_103a", image_bytes);
 }
 
 ssfft_status ssfft_schedule_info(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, int *radices, int cap,
                                  int *npasses, int *threads, int *per_cta, size_t *smem_bytes) {
 	Schedule s;
-	if (!single_schedule(n, dtype, kind, batch, s)) return SSFFT_ERR_UNSUPPORTED;
+	if (!single_schedule(n, dtype, kind, batch, s, &g_diag_knobs)) return SSFFT_ERR_UNSUPPORTED;
 	if (npasses) *npasses = (int)s.radices.size();
 	if (radices)
 		for (int i = 0; i < (int)s.radices.size() && i < cap; ++i) radices[i] = s.radices[i];
@@ -840,7 +948,7 @@ ssfft_status ssfft_schedule_info(size_t n, ssfft_dtype dtype, ssfft_kind kind, s
 ssfft_status ssfft_schedule_name(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, int inverse, char *buf,
                                  size_t cap) {
 	Schedule s;
-	if (!single_schedule(n, dtype, kind, batch, s)) return SSFFT_ERR_UNSUPPORTED;
+	if (!single_schedule(n, dtype, kind, batch, s, &g_diag_knobs)) return SSFFT_ERR_UNSUPPORTED;
 	const std::string name = s.name(inverse != 0);
 	if (!buf || cap < name.size() + 1) return SSFFT_ERR_INVALID_VALUE;
 	std::memcpy(buf, name.c_str(), name.size() + 1);
@@ -851,7 +959,7 @@ ssfft_status ssfft_schedule_tables(size_t n, ssfft_dtype dtype, ssfft_kind kind,
                                    size_t *ntw, double *roots, size_t *nroots, double *rtw, size_t *nrtw, double *rot,
                                    size_t *nrot) {
 	Schedule s;
-	if (!single_schedule(n, dtype, kind, batch, s)) return SSFFT_ERR_UNSUPPORTED;
+	if (!single_schedule(n, dtype, kind, batch, s, &g_diag_knobs)) return SSFFT_ERR_UNSUPPORTED;
 	std::vector<double> vtw, vroots, vrtw, vrot;
 	single_tables(s, n, vtw, vroots, vrtw, vrot);
 	const std::vector<double> *src[4] = {&vtw, &vroots, &vrtw, &vrot};

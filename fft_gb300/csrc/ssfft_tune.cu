@@ -5,7 +5,8 @@
 // plan asks for it, the tuner times candidate schedules on the plan's own batch (zero-filled
 // scratch buffers, CUDA events on a private stream) by coordinate descent:
 //   level 2: radix order (the planner's list, its permutations, the alternative grouping);
-//   level 1 and 2: values per thread {8, 16, 32}, then CTA size {64, 128, 256, 512}.
+//   level 1 and 2: values per thread {8, 16, 32}, then CTA size {64, 128, 256, 512};
+//   level 2: register caps (launch bounds for at most 48 or 40 registers a thread).
 // Candidates of one stage compile concurrently (NVRTC), and are timed one at a time under a
 // process-wide lock so concurrent plan creations do not disturb each other's timings.  The
 // winner is cached per (device name, kernel source, n, dtype, kind, batch range, level) in memory
@@ -46,7 +47,8 @@ std::string cache_file() {
 std::string encode(const Knobs &k) {
 	std::string r = "r=";
 	for (size_t i = 0; i < k.radices.size(); ++i) r += (i ? "." : "") + std::to_string(k.radices[i]);
-	r += " c=" + std::to_string(k.cta_threads) + " e=" + std::to_string(k.emax) + " m=" + std::to_string(k.minb);
+	r += " c=" + std::to_string(k.cta_threads) + " e=" + std::to_string(k.emax) + " m=" + std::to_string(k.minb) +
+	     " p=" + std::to_string(k.precision);
 	return r;
 }
 
@@ -68,6 +70,8 @@ bool decode(const std::string &txt, Knobs &k) {
 			k.emax = std::atoi(v.c_str());
 		} else if (tok[0] == 'm') {
 			k.minb = std::atoi(v.c_str());
+		} else if (tok[0] == 'p') {
+			k.precision = std::atoi(v.c_str());
 		}
 	}
 	return true;
@@ -143,11 +147,15 @@ void compile_all(const Plan *p, size_t tb, std::vector<Candidate> &cs) {
 ssfft_status time_one(const Plan *p, size_t tb, Scratch &sc, Candidate &c) {
 	std::vector<double> tw, roots, rtw, rot;
 	single_tables(c.sch, p->n, tw, roots, rtw, rot);
+	std::vector<float> tcb;
+	if (c.sch.tc) tc_matrix(c.sch.radices[0], tcb);
 	const size_t sb = p->dtype == SSFFT_F32 ? 4 : 8;
 	const size_t o_roots = (tw.size() * sb + 255) & ~(size_t)255;
 	const size_t o_rtw = (o_roots + roots.size() * sb + 255) & ~(size_t)255;
 	const size_t o_rot = (o_rtw + rtw.size() * sb + 255) & ~(size_t)255;
-	const size_t total = std::max<size_t>((o_rot + rot.size() * sb + 255) & ~(size_t)255, 256);
+	const size_t o_tcb = (o_rot + rot.size() * sb + 255) & ~(size_t)255;
+	const size_t o_err = (o_tcb + tcb.size() * 4 + 255) & ~(size_t)255;
+	const size_t total = o_err + 256;
 	std::vector<unsigned char> blob(total, 0);
 	auto put = [&](size_t off, const std::vector<double> &v) {
 		for (size_t i = 0; i < v.size(); ++i) {
@@ -163,6 +171,7 @@ ssfft_status time_one(const Plan *p, size_t tb, Scratch &sc, Candidate &c) {
 	put(o_roots, roots);
 	put(o_rtw, rtw);
 	put(o_rot, rot);
+	if (!tcb.empty()) std::memcpy(blob.data() + o_tcb, tcb.data(), tcb.size() * 4);
 	if (total > sc.tab_bytes) {
 		if (sc.tab) cudaFree(sc.tab);
 		sc.tab = nullptr;
@@ -186,6 +195,9 @@ ssfft_status time_one(const Plan *p, size_t tb, Scratch &sc, Candidate &c) {
 		a.roots = base + o_roots;
 		a.rtw = base + o_rtw;
 		a.rot = base + o_rot;
+		a.tcb = tcb.empty() ? nullptr : reinterpret_cast<const float *>(base + o_tcb);
+		a.err = reinterpret_cast<unsigned *>(static_cast<unsigned char *>(sc.tab) + o_err);
+		a.spin_limit = 1u << 22;
 		CUfunction f = c.fns[inv];
 		ssfft_status st = jit_launch(f, (unsigned)grid, (unsigned)c.sch.cta_threads(), c.sch.smem_bytes, sc.stream, &a);
 		if (st != SSFFT_SUCCESS) return st;
@@ -210,6 +222,7 @@ ssfft_status time_one(const Plan *p, size_t tb, Scratch &sc, Candidate &c) {
 
 ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log) {
 	best = Knobs();
+	best.precision = p->knobs.precision;
 	log.clear();
 	const bool real = p->kind != SSFFT_COMPLEX;
 	const int cn = (int)(real ? p->n / 2 : p->n);
@@ -221,7 +234,8 @@ ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log) 
 	while (bb < 40 && ((size_t)1 << (bb + 1)) <= p->batch) ++bb;
 	const std::string key = std::string(prop.name) + "|" + std::to_string(p->n) + "|" +
 	                        (p->dtype == SSFFT_F32 ? "f32" : "f64") + "|" + std::to_string((int)p->kind) + "|b" +
-	                        std::to_string(bb) + "|L" + std::to_string(level);
+	                        std::to_string(bb) + "|L" + std::to_string(level) + "|P" +
+	                        std::to_string(p->knobs.precision);
 	{
 		std::lock_guard<std::mutex> lock(g_cache_mu);
 		load_locked();
@@ -278,6 +292,7 @@ ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log) 
 		std::vector<Candidate> cs;
 		for (auto &l : lists) {
 			Candidate c;
+			c.knobs = best;
 			c.knobs.radices = l;
 			cs.push_back(c);
 		}
@@ -307,6 +322,29 @@ ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log) 
 		}
 		ssfft_status st = run_stage(cs);
 		if (st != SSFFT_SUCCESS) return st;
+	}
+	if (level >= 2) {
+		// register caps: enough CTAs per SM for at most 48 or 40 registers a thread (more warps
+		// in flight hide the first pass's HBM latency, if the caps do not force spills)
+		Schedule cur;
+		if (single_schedule(p->n, p->dtype, p->kind, tb, cur, &best, 0)) {
+			std::vector<Candidate> cs;
+			for (int regs : {48, 40}) {
+				const int m = 65536 / (cur.cta_threads() * regs);
+				if (m < 2 || m > 32) continue;
+				Candidate c;
+				c.knobs = best;
+				c.knobs.minb = m;
+				cs.push_back(c);
+			}
+			if (!cs.empty()) {
+				Candidate keep;
+				keep.knobs = best;
+				cs.insert(cs.begin(), keep);
+				ssfft_status st = run_stage(cs);
+				if (st != SSFFT_SUCCESS) return st;
+			}
+		}
 	}
 	std::lock_guard<std::mutex> lock(g_cache_mu);
 	store_locked(key, best);

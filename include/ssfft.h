@@ -89,7 +89,12 @@ typedef struct ssfft_plan_options {
     int min_ctas_per_sm;   /* launch bound (register cap) */
     int radices[24];       /* explicit pass order, 0-terminated; product must equal the complex
                             * length (n, or n/2 for real kinds) */
+    int precision;         /* SSFFT_PRECISION_FP32 or SSFFT_PRECISION_SPLIT_BF16 */
 } ssfft_plan_options;
+/* SSFFT_PRECISION_SPLIT_BF16 (complex FP32 plans that run in one CTA): the first radix pass
+ * (radix <= 16) runs as tensor-core matrix products (tcgen05) on FP32 values split into three
+ * BF16 parts, accumulated in FP32; later passes are FP32.  Other plans ignore it. */
+enum { SSFFT_PRECISION_FP32 = 0, SSFFT_PRECISION_SPLIT_BF16 = 1 };
 /* ssfft_plan_create with options (options may be NULL).  Options apply to transforms that run in
  * one CTA; longer ones use the multi-pass schedule regardless. */
 ssfft_status ssfft_plan_create_ex(ssfft_plan_t *plan, size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch,
@@ -232,6 +237,13 @@ ssfft_status ssfft_fft_noalloc_f32(const void *d_in, void *d_out, size_t n, int 
  * (e.g. "sm_103a") and returns the image size; ssfft_schedule_name returns the kernel template
  * the plan runs; ssfft_schedule_tables returns its FP64 tables (pass with NULL arrays first to
  * get the counts). */
+/* Options the diagnostics below apply in the calling thread (NULL: planner defaults). */
+ssfft_status ssfft_schedule_options(const ssfft_plan_options *options);
+/* Tensor-core tile check (GPU): D = A B for one 128 x 32 x 32 FP32 tile through the split-BF16
+ * tcgen05 path (A row-major 128 x 32, bt = B transposed, 32 x 32 row-major, D row-major
+ * 128 x 32, all host memory); *flags receives the kernel's error flag.  No reference
+ * counterpart. */
+ssfft_status ssfft_diag_tc_tile(const float *a, const float *bt, float *d, unsigned *flags);
 ssfft_status ssfft_jit_check(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, const char *arch,
                              size_t *image_bytes);
 ssfft_status ssfft_schedule_info(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, int *radices, int cap,

@@ -7,8 +7,11 @@
 #include <barrier>
 #include <cstddef>
 #include <cstdint>
+#include <cstring>
 
+#define SSFFT_EMULATION 1
 #define __device__
+#define __host__
 #define __global__
 #define __forceinline__ inline
 #define __launch_bounds__(...)

@@ -18,7 +18,21 @@ thread_local EmuIdx threadIdx, blockIdx, gridDim;
 thread_local std::barrier<> *emu_barrier;
 std::atomic<int> emu_or_acc{0};
 namespace ssfft_cl {
-alignas(16) unsigned char smem_raw[232 * 1024];
+alignas(1024) unsigned char smem_raw[232 * 1024];
+float emu_tmem[128][32];
+// BF16 round to nearest even (finite inputs) and widening
+unsigned short f2bf(float x) {
+	uint32_t b;
+	std::memcpy(&b, &x, 4);
+	b += 0x7FFFu + ((b >> 16) & 1u);
+	return (unsigned short)(b >> 16);
+}
+float bf2f(unsigned short h) {
+	const uint32_t b = (uint32_t)h << 16;
+	float x;
+	std::memcpy(&x, &b, 4);
+	return x;
+}
 }
 
 struct Case {
@@ -58,6 +72,8 @@ int main(int argc, char **argv) {
 	a.err = &err;
 	a.spin_limit = 1;
 	a.in_bytes = (unsigned)std::atoi(argv[10]);
+	// tensor-core kernels: the first pass's DFT matrix follows the four tables when present
+	a.tcb = reinterpret_cast<const float *>(base + (cnt[0] + cnt[1] + cnt[2] + cnt[3]) * sb);
 	for (int b = 0; b < grid; ++b) {
 		std::barrier<> bar(c.cta_threads);
 		std::vector<std::thread> th;

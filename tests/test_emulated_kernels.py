@@ -30,6 +30,24 @@ CASES = [
     (2, "f64", "real_halfshift", 1, 1), (4, "f64", "real_halfshift", 2, 2), (9, "f64", "real_halfshift", 1, 1),
     (12, "f32", "real_halfshift", 2, 2), (98, "f64", "real_halfshift", 1, 1), (960, "f32", "real_halfshift", 2, 2),
 ]
+# split-BF16 tensor-core first pass (complex FP32): the emulated MMA decodes the same shared-memory
+# descriptors and core-matrix layout the device reads
+TC_CASES = [(64, "f32", "complex", 40, 40), (1920, "f32", "complex", 3, 3), (16, "f32", "complex", 200, 200),
+            (112, "f32", "complex", 5, 5), (7, "f32", "complex", 130, 130), (4096, "f32", "complex", 1, 1),
+            (480, "f32", "complex", 9, 9), (3, "f32", "complex", 1, 1)]
+TC_TOL = 2e-6
+
+
+def tc_matrix(r0):
+    """The radix-r0 DFT as the tensor-core pass's 32 x 32 real matrix, transposed (row = output
+    column): [Re y_k | Im y_k] from [Re x_r | Im x_r], y_k = sum_r x_r exp(-2 pi i r k / r0)."""
+    bt = np.zeros((32, 32))
+    for k in range(r0):
+        for r in range(r0):
+            c, s = np.cos(2 * np.pi * r * k / r0), np.sin(2 * np.pi * r * k / r0)
+            bt[k, r], bt[k, 16 + r], bt[16 + k, r], bt[16 + k, 16 + r] = c, s, -s, c
+    return bt.astype(np.float32)
+
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -52,13 +70,16 @@ def emulator(staged_schedules, tmp_path_factory):
     d = tmp_path_factory.mktemp("emu")
     lines = []
     index = {}
-    for (n, dt, kind, pb, _) in CASES:
+    for case, tc in [(c, False) for c in CASES] + [(c, True) for c in TC_CASES]:
+        (n, dt, kind, pb, _) = case
+        F.schedule_options(**({"precision": "split_bf16"} if tc else {}))
         info = F.schedule_info(n, dt, kind, pb)
         for inv in (False, True):
             name = F.schedule_name(n, dt, kind, pb, inv)
-            index[(n, dt, kind, pb, inv)] = (len(lines), info)
+            index[(n, dt, kind, pb, inv, tc)] = (len(lines), info)
             lines.append(f'{{"{n}-{dt}-{kind}-{int(inv)}", &{name}, {info["threads"] * info["per_cta"]}, '
                          f'{info["smem_bytes"]}}},')
+        F.schedule_options()
     (d / "emu_cases.inc").write_text("\n".join(lines) + "\n")
     exe = d / "emu"
     cmd = ["g++", "-std=c++20", "-O1", "-pthread", "-w", "-I", str(d), "-I", os.path.join(ROOT, "tests", "emu"),
@@ -68,9 +89,10 @@ def emulator(staged_schedules, tmp_path_factory):
     return exe, index, d
 
 
-def _run(emulator, n, dt, kind, pb, eb, inv, x):
+def _run(emulator, n, dt, kind, pb, eb, inv, x, tc=False):
     exe, index, d = emulator
-    ci, info = index[(n, dt, kind, pb, inv)]
+    ci, info = index[(n, dt, kind, pb, inv, tc)]
+    F.schedule_options(**({"precision": "split_bf16"} if tc else {}))
     sdt = np.float32 if dt == "f32" else np.float64
     real = kind != "complex"
     h2 = 2 * (n // 2)
@@ -85,12 +107,15 @@ def _run(emulator, n, dt, kind, pb, eb, inv, x):
     tabs = F.schedule_tables(n, dt, kind, pb)
     blob = np.array([tabs[k].size for k in ("tw", "roots", "rtw", "rot")], dtype=np.uint64).tobytes()
     blob += b"".join(tabs[k].astype(sdt).tobytes() for k in ("tw", "roots", "rtw", "rot"))
+    name = F.schedule_name(n, dt, kind, pb, inv)
+    if "batch_tc" in name:
+        blob += tc_matrix(info["radices"][0]).tobytes()
+    F.schedule_options()
     fi, fo, ft = d / f"in{ci}", d / f"out{ci}", d / f"tab{ci}"
     fi.write_bytes(xin.tobytes())
     fo.write_bytes(out.tobytes())
     ft.write_bytes(blob)
     groups = -(-eb // info["per_cta"])
-    name = F.schedule_name(n, dt, kind, pb, inv)
     # persistent (staged) kernels: fewer CTAs than groups, so each CTA walks several groups
     grid = max(1, groups // 2) if "batch_staged" in name else groups
     in_bytes = in_dist * np.dtype(sdt).itemsize
@@ -126,3 +151,18 @@ def test_emulated_kernel_matches_oracle(emulator, case):
         assert rel_l2(got[:, :2 * h], ref) <= tol, rel_l2(got[:, :2 * h], ref)
         if n % 2:
             assert np.all(np.isnan(got[:, 2 * h:])), "odd real length: last sample must be left alone"
+
+
+@pytest.mark.parametrize("case", TC_CASES, ids=lambda c: f"tc-{c[0]}")
+def test_emulated_tensor_core_kernel_matches_oracle(emulator, case):
+    n, dt, kind, pb, eb = case
+    F.schedule_options(precision="split_bf16")
+    name = F.schedule_name(n, dt, kind, pb)
+    F.schedule_options()
+    assert "batch_tc" in name
+    rng = np.random.default_rng(n * 11)
+    x = (rng.uniform(-1, 1, (eb, n)) + 1j * rng.uniform(-1, 1, (eb, n))).astype(np.complex64)
+    for inv in (False, True):
+        got = _run(emulator, n, dt, kind, pb, eb, inv, x, tc=True).view(np.complex64)
+        ref = np.stack([oracle.fft(r.astype(np.complex128), inv) for r in x])
+        assert rel_l2(got, ref) <= TC_TOL, (inv, rel_l2(got, ref))
