@@ -618,12 +618,39 @@ inline bool mbar_try_wait(unsigned long long *, unsigned) { return true; }
 #endif
 
 // Wait for phase `phase` of `bar`, giving up after `limit` attempts (each try_wait itself
-// suspends for a bounded, hardware-defined time).
+// suspends for a bounded, hardware-defined time).  On the device the polling loop is one asm
+// statement: as a C++ loop, the compiler moved address arithmetic of the code after it above
+// it and kept the results live (the staged kernel went from ~69 to 93+ registers).
+#if defined(__CUDA_ARCH__)
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned phase, unsigned limit) {
+	unsigned ok;
+	asm volatile(
+	    "{\n\t"
+	    ".reg .pred p, q;\n\t"
+	    ".reg .u32 i;\n\t"
+	    "mov.u32 i, 0;\n\t"
+	    "mov.u32 %0, 0;\n"
+	    "LAB_WAIT:\n\t"
+	    "setp.ge.u32 q, i, %3;\n\t"
+	    "@q bra LAB_DONE;\n\t"
+	    "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+	    "add.u32 i, i, 1;\n\t"
+	    "@!p bra LAB_WAIT;\n\t"
+	    "mov.u32 %0, 1;\n"
+	    "LAB_DONE:\n\t"
+	    "}"
+	    : "=r"(ok)
+	    : "r"(smem_u32(bar)), "r"(phase), "r"(limit)
+	    : "memory");
+	return ok != 0;
+}
+#else
+inline bool mbar_wait_bounded(unsigned long long *bar, unsigned phase, unsigned limit) {
 	for (unsigned i = 0; i < limit; ++i)
 		if (mbar_try_wait(bar, phase)) return true;
 	return false;
 }
+#endif
 
 // The batch kernel with asynchronous input staging: persistent CTAs walk the groups of PER_CTA
 // transforms; each group's input (contiguous in HBM) arrives in an unpadded staging buffer by
