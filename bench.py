@@ -461,8 +461,14 @@ def run_large(args):
         p = F.Plan(n, "f32", "complex", 1)
         t = _time_device(lambda: p.exec(False, xi.data_ptr(), y.data_ptr(), sh), 20, 3)
         alg = 16 * n
+        p.exec(False, xi.data_ptr(), y.data_ptr(), sh)
+        torch.cuda.synchronize()
+        import oracle
+        ref = oracle.fft(x.astype(np.complex128))
+        rel = float(np.linalg.norm(y.cpu().numpy() - ref) / np.linalg.norm(ref))
         out.append({"n": n, "ms": t * 1e3, "GFLOP_s": 5 * n * math.log2(n) / t / 1e9, "alg_GB_s": alg / t / 1e9,
-                    "passes": p.describe()["radices"], "launches": p.describe()["launches"]})
+                    "passes": p.describe()["radices"], "launches": p.describe()["launches"],
+                    "relL2_vs_fp64_oracle": rel})
         del xi, y, p
         torch.cuda.empty_cache()
     peak, kind = measured_peak_hbm()

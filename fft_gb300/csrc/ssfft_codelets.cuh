@@ -41,6 +41,8 @@ struct Args {
 	                          // group's bytes but no copy is issued, so every wait runs out (0 normally)
 	const float *tcb;         // tensor-core kernels: the first pass's DFT as a 32 x 32 real matrix
 	                          // [output column][input column] (FP32 values of FP64-built roots)
+	long long pf_dist;        // batch kernel: CTA b prefetches into L2 the input of CTA b + pf_dist
+	                          // (about one wave of resident CTAs ahead; 0 = off)
 };
 
 enum : int { kComplex = 0, kReal = 1, kRealHalfShift = 2 };
@@ -301,6 +303,39 @@ __device__ __forceinline__ typename Cx<T>::C sload(const Ctx<T, KIND, CIN, COUT>
 	} else {
 		if constexpr (KIND == kRealHalfShift) v = mul(v, __ldg(c.rot + e));
 		return v;
+	}
+}
+
+// L2 prefetch of one line (a hint: no data returns, nothing waits on it).
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+#else
+inline void prefetch_l2(const void *) {}
+#endif
+
+// The input of the CTA pf_dist blocks ahead (transforms stored back to back), one 128-byte
+// line per thread per step: by the time that CTA starts, about one wave later, its loads hit L2,
+// and the HBM read stream keeps going while resident CTAs compute.
+template <typename T, int PER_CTA, int CTA_THREADS>
+__device__ __forceinline__ void prefetch_ahead(const Args &a) {
+	if (a.pf_dist <= 0) return;
+	const long long first = ((long long)blockIdx.x + a.pf_dist) * PER_CTA;
+	if (first >= a.batch) return;
+	const long long cnt = a.batch - first < PER_CTA ? a.batch - first : PER_CTA;
+	const unsigned char *in = reinterpret_cast<const unsigned char *>(a.in);
+	const long long per = a.in_dist * (long long)sizeof(T);  // input bytes of one transform
+	if (!a.offs) {
+		const unsigned char *base = in + first * per;
+		const long long bytes = cnt * per;
+		for (long long off = (long long)threadIdx.x * 128; off < bytes; off += (long long)CTA_THREADS * 128)
+			prefetch_l2(base + off);
+	} else {
+		// scattered transforms (offset table): line k of transform g = k / lines
+		const long long lines = (per + 127) / 128;
+		for (long long k = threadIdx.x; k < cnt * lines; k += CTA_THREADS) {
+			const long long g = k / lines;
+			prefetch_l2(in + a.offs[first + g] * (long long)sizeof(T) + (k - g * lines) * 128);
+		}
 	}
 }
 
@@ -566,6 +601,7 @@ __global__ void __launch_bounds__(THREADS *PER_CTA, MINB) batch(const Args a) {
 	const C *tw = reinterpret_cast<const C *>(a.tw);
 	const C *roots = reinterpret_cast<const C *>(a.roots);
 	const C *rtw = reinterpret_cast<const C *>(a.rtw);
+	prefetch_ahead<T, PER_CTA, THREADS * PER_CTA>(a);
 	if constexpr (C2R) real_pre<T, N, THREADS, KIND, INV, INV>(c, rtw);
 	passes<T, N, THREADS, 1, 0, 0, C2R ? kSmem : kGlobal, R2C ? kSmem : kGlobal, KIND, INV, INV, ODD, EMAX, Rs...>(
 	    c, tw, roots);

@@ -47,8 +47,9 @@ struct Knobs {
 	int emax = 0;              // complex values a thread holds in one pass
 	int minb = 0;              // launch-bound CTAs per SM
 	int precision = 0;         // SSFFT_PRECISION_*: 1 = first pass on the tensor cores (split BF16)
+	int prefetch = -1;         // L2 prefetch distance in quarter waves of resident CTAs (-1 default)
 	// no shape choice made (precision is not a shape choice)
-	bool empty() const { return radices.empty() && !cta_threads && !emax && !minb; }
+	bool empty() const { return radices.empty() && !cta_threads && !emax && !minb && prefetch < 0; }
 	std::string str() const;
 };
 
@@ -63,6 +64,7 @@ struct SubPlan {
 	Tables tab;
 	CUfunction fwd = nullptr, inv = nullptr;
 	int grid_cap = 0;        // staged: resident CTAs (persistent grid)
+	long long pf_dist = 0;   // plain batch kernel: L2 prefetch distance in CTAs (resident CTAs)
 	unsigned *err = nullptr; // staged: device error word
 };
 
@@ -116,6 +118,9 @@ void radix_candidates(int n, std::vector<std::vector<int>> &out);
 void tc_matrix(int r0, std::vector<float> &bt);
 // autotuner (ssfft_tune.cu): picks knobs for a single-CTA plan, cached per device and shape
 ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log);
+// prefetch distance in CTAs for a schedule with `resident` CTAs on the GPU at once
+long long prefetch_distance(const Schedule &s, const Knobs &k, long long resident);
+long long resident_ctas(CUfunction fwd, CUfunction inv, const Schedule &s, int device);
 void schedule_twiddles(const Schedule &s, std::vector<double> &tw, std::vector<double> &roots);
 size_t device_smem_limit(int dev);
 

@@ -214,6 +214,7 @@ std::string Knobs::str() const {
 	for (size_t i = 0; i < radices.size(); ++i) r += (i ? "." : "") + std::to_string(radices[i]);
 	if (radices.empty()) r += "default";
 	r += " cta=" + std::to_string(cta_threads) + " emax=" + std::to_string(emax) + " minb=" + std::to_string(minb);
+	if (prefetch >= 0) r += " prefetch=" + std::to_string(prefetch) + "/4";
 	if (precision == 1) r += " precision=split_bf16";
 	return r;
 }
@@ -440,6 +441,26 @@ void tc_matrix(int r0, std::vector<float> &bt) {
 		}
 }
 
+long long resident_ctas(CUfunction fwd, CUfunction inv, const Schedule &s, int device) {
+	int sms = 0;
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+	const int occ = std::min(jit_occupancy(fwd, s.cta_threads(), s.smem_bytes),
+	                         jit_occupancy(inv, s.cta_threads(), s.smem_bytes));
+	return (long long)std::max(1, occ) * std::max(1, sms);
+}
+
+// The plain batch kernel prefetches into L2 the input of the CTA this many blocks ahead: by
+// default one wave of resident CTAs (measured on GB300: complex N=1024 77% -> 92% of the copy
+// bandwidth, RealFFT N=3840 62% -> 70%).  Knob: quarter waves (0 = off); SSFFT_PREFETCH=0 turns
+// it off for plans made while it is set.
+long long prefetch_distance(const Schedule &s, const Knobs &k, long long resident) {
+	if (s.staged || s.tc) return 0;
+	const char *env = std::getenv("SSFFT_PREFETCH");
+	if (env && env[0] == '0') return 0;
+	const int quarters = k.prefetch >= 0 ? k.prefetch : 4;
+	return resident * quarters / 4;
+}
+
 static ssfft_status plan_build_single(Plan *p) {
 	Schedule &s = p->main.sch;
 	{
@@ -499,12 +520,10 @@ static ssfft_status plan_build_single(Plan *p) {
 	if (st != SSFFT_SUCCESS) return st;
 	p->main.fwd = fns[0];
 	p->main.inv = fns[1];
-	if (s.staged) {
-		int sms = 0;
-		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
-		const int occ = std::min(jit_occupancy(fns[0], s.cta_threads(), s.smem_bytes),
-		                         jit_occupancy(fns[1], s.cta_threads(), s.smem_bytes));
-		p->main.grid_cap = std::max(1, occ) * std::max(1, sms);
+	{
+		const long long resident = resident_ctas(fns[0], fns[1], s, p->device);
+		if (s.staged) p->main.grid_cap = (int)resident;
+		p->main.pf_dist = prefetch_distance(s, p->knobs, resident);
 	}
 	p->launches_per_exec = 1;
 	return SSFFT_SUCCESS;
@@ -597,6 +616,7 @@ ssfft_status launch_batch_offs(const Plan *p, int inverse, const void *in, void 
 	a.err = p->main.err;
 	a.spin_limit = 1u << 22;
 	a.offs = d_offs;
+	a.pf_dist = p->main.pf_dist;
 	const long long grid = ((long long)batch + sch.per_cta - 1) / sch.per_cta;
 	if (grid > 0x7fffffffLL) return SSFFT_ERR_INVALID_SIZE;
 	return jit_launch(inverse ? p->main.inv : p->main.fwd, (unsigned)grid, (unsigned)sch.cta_threads(),
@@ -620,6 +640,7 @@ ssfft_status launch_batch(const Plan *p, int inverse, const void *in, void *out,
 	a.spin_limit = 1u << 22;
 	a.in_bytes = sch.in_bytes;
 	a.tcb = p->main.tab.tcb;
+	a.pf_dist = p->main.pf_dist;
 	long long grid = ((long long)batch + sch.per_cta - 1) / sch.per_cta;
 	if (sch.staged) {
 		if ((uintptr_t)in % 16) return launch_unstaged(p, inverse, in, out, batch, s);
@@ -704,6 +725,11 @@ ssfft_status ssfft_plan_create_ex(ssfft_plan_t *out, size_t n, ssfft_dtype dtype
 			return SSFFT_ERR_INVALID_VALUE;
 		}
 		p->knobs.precision = opt->precision;
+		if (opt->prefetch_quarter_waves < -1 || opt->prefetch_quarter_waves > 64) {
+			delete p;
+			return SSFFT_ERR_INVALID_VALUE;
+		}
+		if (opt->prefetch_quarter_waves != 0) p->knobs.prefetch = std::max(0, opt->prefetch_quarter_waves);
 		for (int i = 0; i < 24 && opt->radices[i] > 0; ++i) p->knobs.radices.push_back(opt->radices[i]);
 	}
 	cudaError_t e = cudaGetDevice(&p->device);

@@ -6,7 +6,8 @@
 // scratch buffers, CUDA events on a private stream) by coordinate descent:
 //   level 2: radix order (the planner's list, its permutations, the alternative grouping);
 //   level 1 and 2: values per thread {8, 16, 32}, then CTA size {64, 128, 256, 512};
-//   level 2: register caps (launch bounds for at most 48 or 40 registers a thread).
+//   level 2: L2 prefetch distance (1/2, 1, 2 waves of resident CTAs), then register caps
+//   (launch bounds for at most 48 or 40 registers a thread).
 // Candidates of one stage compile concurrently (NVRTC), and are timed one at a time under a
 // process-wide lock so concurrent plan creations do not disturb each other's timings.  The
 // winner is cached per (device name, kernel source, n, dtype, kind, batch range, level) in memory
@@ -48,7 +49,7 @@ std::string encode(const Knobs &k) {
 	std::string r = "r=";
 	for (size_t i = 0; i < k.radices.size(); ++i) r += (i ? "." : "") + std::to_string(k.radices[i]);
 	r += " c=" + std::to_string(k.cta_threads) + " e=" + std::to_string(k.emax) + " m=" + std::to_string(k.minb) +
-	     " p=" + std::to_string(k.precision);
+	     " p=" + std::to_string(k.precision) + " f=" + std::to_string(k.prefetch);
 	return r;
 }
 
@@ -72,6 +73,8 @@ bool decode(const std::string &txt, Knobs &k) {
 			k.minb = std::atoi(v.c_str());
 		} else if (tok[0] == 'p') {
 			k.precision = std::atoi(v.c_str());
+		} else if (tok[0] == 'f') {
+			k.prefetch = std::atoi(v.c_str());
 		}
 	}
 	return true;
@@ -198,6 +201,7 @@ ssfft_status time_one(const Plan *p, size_t tb, Scratch &sc, Candidate &c) {
 		a.tcb = tcb.empty() ? nullptr : reinterpret_cast<const float *>(base + o_tcb);
 		a.err = reinterpret_cast<unsigned *>(static_cast<unsigned char *>(sc.tab) + o_err);
 		a.spin_limit = 1u << 22;
+		a.pf_dist = prefetch_distance(c.sch, c.knobs, resident_ctas(c.fns[0], c.fns[1], c.sch, p->device));
 		CUfunction f = c.fns[inv];
 		ssfft_status st = jit_launch(f, (unsigned)grid, (unsigned)c.sch.cta_threads(), c.sch.smem_bytes, sc.stream, &a);
 		if (st != SSFFT_SUCCESS) return st;
@@ -264,7 +268,7 @@ ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log) 
 		std::lock_guard<std::mutex> lock(g_time_mu);
 		for (auto &c : cs) {
 			if (c.st != SSFFT_SUCCESS) continue;
-			const std::string nm = c.sch.name(false);
+			const std::string nm = c.sch.name(false) + "|pf" + std::to_string(c.knobs.prefetch);
 			auto it = timed.find(nm);
 			if (it != timed.end()) {
 				c.fwd_us = it->second;
@@ -318,6 +322,18 @@ ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log) 
 			Candidate c;
 			c.knobs = best;
 			c.knobs.cta_threads = ct;
+			cs.push_back(c);
+		}
+		ssfft_status st = run_stage(cs);
+		if (st != SSFFT_SUCCESS) return st;
+	}
+	if (level >= 2) {
+		// L2 prefetch distance: half, one or two waves of resident CTAs ahead
+		std::vector<Candidate> cs;
+		for (int q : {2, 4, 8}) {
+			Candidate c;
+			c.knobs = best;
+			c.knobs.prefetch = q;
 			cs.push_back(c);
 		}
 		ssfft_status st = run_stage(cs);

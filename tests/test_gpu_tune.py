@@ -43,7 +43,8 @@ def test_explicit_radix_orders(F, radices):
 
 
 @pytest.mark.parametrize("opts", [dict(cta_threads=64), dict(cta_threads=512), dict(values_per_thread=8),
-                                  dict(values_per_thread=32), dict(min_ctas_per_sm=4)])
+                                  dict(values_per_thread=32), dict(min_ctas_per_sm=4),
+                                  dict(prefetch_quarter_waves=-1), dict(prefetch_quarter_waves=8)])
 def test_explicit_shapes(F, opts):
     for n in (480, 1920):
         _real_case(F, n, 100, **opts)
