@@ -1144,6 +1144,7 @@ struct StridedArgs {
 	const void *twhi;
 	const void *rot;    // half-shift rotations (ROT)
 	long long rot_in_stride2, rot_out_stride2;  // u2 stride of the index j inside the whole transform
+	long long pf_dist;  // CTA b prefetches into L2 the input of CTA b + pf_dist (0 = off)
 };
 
 template <typename T, int N, int THREADS, int G, int STRIDE, bool CIN, bool COUT, int EMAX, bool SLOAD, bool SSTORE,
@@ -1171,6 +1172,29 @@ __global__ void __launch_bounds__(THREADS *G) strided(const StridedArgs a) {
 	c.gin = reinterpret_cast<const T *>(in + (c.valid ? ib + (u00 + g) * a.is0 : 0));
 	c.gout = reinterpret_cast<T *>(out + (c.valid ? ob + (u00 + g) * a.os0 : 0));
 	c.rot = reinterpret_cast<const C *>(a.rot);
+	if (a.pf_dist > 0 && (long long)blockIdx.x + a.pf_dist < (long long)gridDim.x) {
+		// the input the CTA pf_dist blocks ahead will read, one 128-byte line per prefetch
+		long long pc = (long long)blockIdx.x + a.pf_dist;
+		const long long pu00 = (pc % blocks0) * G;
+		pc /= blocks0;
+		const long long pib = (pc / a.U1) * a.is2 + (pc % a.U1) * a.is1;
+		constexpr int PER_LINE = 128 / (int)sizeof(C);
+		if constexpr (SLOAD) {
+			// G-element segments (is0 == 1), one per element e
+			constexpr int SEG_LINES = (G + PER_LINE - 1) / PER_LINE;
+			for (int k = threadIdx.x; k < N * SEG_LINES; k += CTA) {
+				const int e = k / SEG_LINES, l = k - e * SEG_LINES;
+				if (pu00 + l * PER_LINE < a.U0) prefetch_l2(in + pib + (pu00 + l * PER_LINE) * a.is0 + (long long)e * a.in_es);
+			}
+		} else {
+			// G contiguous rows of N elements (in_es == 1)
+			constexpr int ROW_LINES = (N + PER_LINE - 1) / PER_LINE;
+			for (int k = threadIdx.x; k < G * ROW_LINES; k += CTA) {
+				const int gg = k / ROW_LINES, l = k - gg * ROW_LINES;
+				if (pu00 + gg < a.U0) prefetch_l2(in + pib + (pu00 + gg) * a.is0 + (long long)l * PER_LINE * a.in_es);
+			}
+		}
+	}
 	if constexpr (SLOAD) {
 		// G-element segments: consecutive threads take consecutive u0 of the same element
 #pragma unroll 4

@@ -15,6 +15,7 @@
 // h = n/2 > 16384 points add the even/odd split (forward) or pre-twiddle (inverse) as one
 // element-wise kernel (ssfft_cl::real_split).
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -36,6 +37,7 @@ struct LargePass {
 	long long is0 = 0, is1 = 0, in_es = 1, os0 = 0, os1 = 0, out_es = 1;
 	size_t off_tw = 0, off_roots = 0, off_twlo = 0, off_twhi = 0;
 	CUfunction fwd = nullptr, inv = nullptr;
+	long long pf_dist = 0;     // L2 prefetch distance in CTAs (one wave of resident CTAs)
 	std::string name(bool inverse, bool first, bool last, int rot) const;
 };
 
@@ -313,9 +315,14 @@ ssfft_status plan_build_large(Plan *p) {
 	std::vector<CUfunction> fns;
 	ssfft_status st = jit_kernels(names, smem_max, fns);
 	if (st != SSFFT_SUCCESS) return st;
+	const char *pf_env = std::getenv("SSFFT_PREFETCH");
+	const bool prefetch = !(pf_env && pf_env[0] == '0');
 	for (int i = 0; i < P; ++i) {
-		lp->pass[i].fwd = fns[2 * i];
-		lp->pass[i].inv = fns[2 * i + 1];
+		LargePass &ps = lp->pass[i];
+		ps.fwd = fns[2 * i];
+		ps.inv = fns[2 * i + 1];
+		// prefetch one wave of resident CTAs ahead (as the batch kernel does)
+		if (prefetch) ps.pf_dist = resident_ctas(ps.fwd, ps.inv, ps.sub, p->device);
 	}
 	if (real) {
 		lp->split_fwd = fns[2 * P];
@@ -372,6 +379,7 @@ ssfft_status launch_large(Plan *p, int inverse, const void *in, void *out, size_
 			a.rot = tab + lp->off_rot;
 			a.rot_in_stride2 = N;
 			a.rot_out_stride2 = N;
+			a.pf_dist = ps.pf_dist;
 			const long long G = ps.sub.per_cta;
 			const long long grid = nb * ps.U1 * ((ps.U0 + G - 1) / G);
 			if (grid > 0x7fffffffLL) return SSFFT_ERR_INVALID_SIZE;
