@@ -378,6 +378,13 @@ __device__ __forceinline__ void gstore(const Ctx<T, KIND, CIN, COUT> &c, int e, 
 
 // ------------------------------------------------------------------ one pass
 
+// Twiddle rows stored for a pass of radix R: exponents 1, 2, 4, 8 (< R) for the register
+// butterflies, 1..R-1 for the direct passes.
+template <int R>
+struct TwRows {
+	static constexpr int value = Specialised<R>::value ? (R > 8 ? 4 : R > 4 ? 3 : R > 2 ? 2 : 1) : R - 1;
+};
+
 template <typename T, int N, int THREADS, int R, int NS, int TWO, int ROOTS, int SRC, int DST, int KIND, bool CIN,
           bool COUT, bool ODD, int EMAX>
 __device__ __forceinline__ void pass(const Ctx<T, KIND, CIN, COUT> &c, const typename Cx<T>::C *tw,
@@ -406,9 +413,21 @@ __device__ __forceinline__ void pass(const Ctx<T, KIND, CIN, COUT> &c, const typ
 			const int j = c.t + i * THREADS;
 			if (c.valid && (!GUARD || j < NB)) {
 				if constexpr (NS > 1) {
+					// W^{mr}: rows W^{m}, W^{2m}, W^{4m}, W^{8m} are loaded, the other powers are
+					// products w_r = w_{r - lowbit(r)} * w_{lowbit(r)} (at most 3 products deep);
+					// a quarter to a half of the twiddle loads, which were most of the L1 traffic
 					const int m = j % NS;
+					C pw[TwRows<R>::value];
 #pragma unroll
-					for (int r = 1; r < R; ++r) v[i][r] = mul(v[i][r], __ldg(tw + TWO + (r - 1) * NS + m));
+					for (int b = 0; b < TwRows<R>::value; ++b) pw[b] = __ldg(tw + TWO + b * NS + m);
+					C w[R];
+#pragma unroll
+					for (int r = 1; r < R; ++r) {
+						const int lb = r & -r;
+						const int b = lb == 1 ? 0 : lb == 2 ? 1 : lb == 4 ? 2 : 3;
+						w[r] = r == lb ? pw[b] : mul(w[r - lb], pw[b]);
+						v[i][r] = mul(v[i][r], w[r]);
+					}
 				}
 				dft<R>(v[i]);
 			}
@@ -471,10 +490,12 @@ __device__ __forceinline__ void pass(const Ctx<T, KIND, CIN, COUT> &c, const typ
 	if constexpr (DST == kSmem) __syncthreads();
 }
 
-// Twiddle slots used by a pass of radix R after NS points (none for the first pass).
+// Twiddle slots used by a pass of radix R after NS points (none for the first pass): rows of
+// the exponents 1, 2, 4, 8 below R for register butterflies, every exponent 1..R-1 for direct
+// passes.
 template <int R, int NS>
 struct TwCount {
-	static constexpr int value = NS > 1 ? NS * (R - 1) : 0;
+	static constexpr int value = NS > 1 ? NS * TwRows<R>::value : 0;
 };
 template <int R>
 struct RootCount {

@@ -356,8 +356,15 @@ std::string Schedule::name(bool inverse) const {
 void schedule_twiddles(const Schedule &s, std::vector<double> &tw, std::vector<double> &roots) {
 	long long ns = 1;
 	for (int R : s.radices) {
+		// register butterflies store the rows of exponents 1, 2, 4, 8 (< R) and form the other
+		// powers by products; direct passes store every exponent 1..R-1
+		std::vector<int> exps;
+		if (specialised(R))
+			for (int e = 1; e < R; e *= 2) exps.push_back(e);
+		else
+			for (int r = 1; r < R; ++r) exps.push_back(r);
 		if (ns > 1)
-			for (int r = 1; r < R; ++r)
+			for (int r : exps)
 				for (long long m = 0; m < ns; ++m) {
 					double re, im;
 					unit_root((unsigned long long)(m * r), (unsigned long long)(ns * R), &re, &im);
