@@ -81,6 +81,11 @@ def schedule_options(**opts) -> None:
         check(lib().ssfft_schedule_options(None), "schedule_options")
 
 
+def schedule_direction(inverse: bool) -> None:
+    """Direction whose schedule schedule_info / schedule_tables report in this thread."""
+    check(lib().ssfft_schedule_direction(int(bool(inverse))), "schedule_direction")
+
+
 def diag_tc_tile(a: np.ndarray, bt: np.ndarray) -> tuple:
     """D = A B for one 128 x 32 x 32 FP32 tile through the split-BF16 tensor-core path (GPU).
     ``bt`` is B transposed.  Returns (D, error flag)."""
@@ -126,9 +131,10 @@ def _declare(l):
     l.ssfft_schedule_tables.argtypes = [_sz, _int, _int, _sz, dp, szp, dp, szp, dp, szp, dp, szp]
     l.ssfft_diag_staged_timeout.argtypes = [_sz, ctypes.c_uint, ctypes.POINTER(ctypes.c_uint)]
     l.ssfft_schedule_options.argtypes = [ctypes.POINTER(PlanOptions)]
+    l.ssfft_schedule_direction.argtypes = [_int]
     l.ssfft_diag_tc_tile.argtypes = [_vp, _vp, _vp, ctypes.POINTER(ctypes.c_uint)]
     for name in ("ssfft_plan_create", "ssfft_plan_create_ex", "ssfft_plan_tuning", "ssfft_plan_destroy", "ssfft_plan_describe", "ssfft_exec", "ssfft_exec_batch",
-                 "ssfft_exec_host", "ssfft_plan_error", "ssfft_diag_staged_timeout", "ssfft_schedule_options",
+                 "ssfft_exec_host", "ssfft_plan_error", "ssfft_diag_staged_timeout", "ssfft_schedule_options", "ssfft_schedule_direction",
                  "ssfft_diag_tc_tile", "ssfft_jit_check", "ssfft_schedule_info", "ssfft_schedule_name",
                  "ssfft_schedule_tables"):
         getattr(l, name).restype = _int

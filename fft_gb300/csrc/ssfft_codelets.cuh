@@ -49,6 +49,9 @@ enum : int { kComplex = 0, kReal = 1, kRealHalfShift = 2 };
 // element sources / destinations of a pass: padded shared memory, HBM, or the unpadded staging
 // buffer a bulk copy filled
 enum : int { kSmem = 0, kGlobal = 1, kStage = 2 };
+// fused real split: the last pass of a RealFFT forward writes the bins (kFusedR2C), the first pass
+// of its inverse reads the bins and pre-twiddles them (kFusedC2R)
+enum : int { kFusedR2C = 3, kFusedC2R = 4 };
 
 template <typename T>
 struct Cx;
@@ -289,6 +292,7 @@ struct Ctx {
 	T *gout;       // this transform's output, in scalars
 	const C *rot;  // half-shift rotations
 	const C *st;   // staged kernels: this transform's input in the unpadded staging buffer
+	const C *rtw;  // real split twiddles (fused split passes)
 	int t;         // thread index inside the transform
 	bool valid;    // the transform exists (the last CTA may be partial)
 };
@@ -385,6 +389,25 @@ struct TwRows {
 	static constexpr int value = Specialised<R>::value ? (R > 8 ? 4 : R > 4 ? 3 : R > 2 ? 2 : 1) : R - 1;
 };
 
+// v[r] *= W_{NS R}^{m r}: rows W^{m}, W^{2m}, W^{4m}, W^{8m} are loaded, the other powers are
+// products w_r = w_{r - lowbit(r)} * w_{lowbit(r)} (at most 3 products deep); a quarter to a half
+// of the twiddle loads, which were most of the L1 traffic.
+template <typename T, int R, int NS, int TWO>
+__device__ __forceinline__ void apply_twiddles(typename Cx<T>::C (&v)[R], const typename Cx<T>::C *tw, int m) {
+	using C = typename Cx<T>::C;
+	C pw[TwRows<R>::value];
+#pragma unroll
+	for (int b = 0; b < TwRows<R>::value; ++b) pw[b] = __ldg(tw + TWO + b * NS + m);
+	C w[R];
+#pragma unroll
+	for (int r = 1; r < R; ++r) {
+		const int lb = r & -r;
+		const int b = lb == 1 ? 0 : lb == 2 ? 1 : lb == 4 ? 2 : 3;
+		w[r] = r == lb ? pw[b] : mul(w[r - lb], pw[b]);
+		v[r] = mul(v[r], w[r]);
+	}
+}
+
 template <typename T, int N, int THREADS, int R, int NS, int TWO, int ROOTS, int SRC, int DST, int KIND, bool CIN,
           bool COUT, bool ODD, int EMAX>
 __device__ __forceinline__ void pass(const Ctx<T, KIND, CIN, COUT> &c, const typename Cx<T>::C *tw,
@@ -412,23 +435,7 @@ __device__ __forceinline__ void pass(const Ctx<T, KIND, CIN, COUT> &c, const typ
 		for (int i = 0; i < NBPT; ++i) {
 			const int j = c.t + i * THREADS;
 			if (c.valid && (!GUARD || j < NB)) {
-				if constexpr (NS > 1) {
-					// W^{mr}: rows W^{m}, W^{2m}, W^{4m}, W^{8m} are loaded, the other powers are
-					// products w_r = w_{r - lowbit(r)} * w_{lowbit(r)} (at most 3 products deep);
-					// a quarter to a half of the twiddle loads, which were most of the L1 traffic
-					const int m = j % NS;
-					C pw[TwRows<R>::value];
-#pragma unroll
-					for (int b = 0; b < TwRows<R>::value; ++b) pw[b] = __ldg(tw + TWO + b * NS + m);
-					C w[R];
-#pragma unroll
-					for (int r = 1; r < R; ++r) {
-						const int lb = r & -r;
-						const int b = lb == 1 ? 0 : lb == 2 ? 1 : lb == 4 ? 2 : 3;
-						w[r] = r == lb ? pw[b] : mul(w[r - lb], pw[b]);
-						v[i][r] = mul(v[i][r], w[r]);
-					}
-				}
+				if constexpr (NS > 1) apply_twiddles<T, R, NS, TWO>(v[i], tw, j % NS);
 				dft<R>(v[i]);
 			}
 		}
@@ -506,6 +513,144 @@ struct NoHook {
 	__device__ __forceinline__ void operator()() const {}
 };
 
+// ------------------------------------------------------------------ real split fused into a pass
+//
+// RealFFT (not the half-shift variant) pairs bin k with bin H - k in its forward split and input k
+// with H - k in its inverse pre-twiddle (signalsmith-fft.h:459-472, :477-492).  In the last pass
+// (radix R, NS = H/R) butterfly j produces X[j + r NS] and butterfly NS - j produces the mirrors
+// X[H - j - r NS] = X[(NS - j) + (R - 1 - r) NS]; in the first pass butterfly j reads z[j + r NB]
+// and butterfly NB - j reads the mirrors.  A thread that runs both butterflies of such a pair (a
+// unit: j and M - j, M = NS or NB; j = 0 and j = M/2 are their own mirrors) has both ends of
+// every pair in registers, so the split or pre-twiddle needs no shared-memory round trip.  A unit
+// holds 2R values; the planner uses these passes for R <= 8.  Each output pair is computed once,
+// with the reference's formulas; the self-paired bin H/2 gets the reference's surviving write.
+
+// Forward split of the pair (i, H - i), 1 <= i <= H/2, from Z[i] and Z[H - i].
+template <typename T, int H>
+__device__ __forceinline__ void split_pair(typename Cx<T>::C *out, const typename Cx<T>::C *rtw, int i,
+                                           typename Cx<T>::C zi, typename Cx<T>::C zci) {
+	using C = typename Cx<T>::C;
+	const C zc = conj(zci);
+	const C odd = scale(add(zi, zc), T(0.5));
+	const C even = scale(sub(zi, zc), T(0.5));
+	const C e = mul(even, __ldg(rtw + i));
+	if (2 * i != H) __stcs(out + i, add(odd, e));
+	__stcs(out + (H - i), conj(sub(odd, e)));
+}
+
+// Inverse pre-twiddle of the pair (i, H - i), 1 <= i <= H/2: the (conjugated) first-pass inputs
+// z[i] and z[H - i] from bins B[i], B[H - i].
+template <typename T, int H>
+__device__ __forceinline__ void pretwiddle_pair(const typename Cx<T>::C *in, const typename Cx<T>::C *rtw, int i,
+                                                typename Cx<T>::C &zi, typename Cx<T>::C &zci) {
+	using C = typename Cx<T>::C;
+	const C v = __ldcs(in + i);
+	const C v2c = conj(__ldcs(in + (H - i)));
+	const C odd = add(v, v2c);
+	const C even = mulc(sub(v, v2c), __ldg(rtw + i));
+	zi = conj(add(odd, even));
+	zci = sub(odd, even);
+}
+
+// Last pass of a RealFFT forward with the split fused: shared memory -> H bins in HBM.
+template <typename T, int H, int THREADS, int R, int NS, int TWO, int KIND, bool CIN, bool COUT>
+__device__ __forceinline__ void pass_last_r2c(const Ctx<T, KIND, CIN, COUT> &c, const typename Cx<T>::C *tw) {
+	using C = typename Cx<T>::C;
+	constexpr int PS = Cx<T>::kPadShift;
+	constexpr int U = NS / 2 + 1, UPT = (U + THREADS - 1) / THREADS;
+	static_assert(Specialised<R>::value && NS * R == H, "fused split needs a register butterfly as the last pass");
+	C *out = reinterpret_cast<C *>(c.gout);
+#pragma unroll
+	for (int q = 0; q < UPT; ++q) {
+		const int u = c.t + q * THREADS;
+		if (c.valid && u < U) {
+			const int j1 = u, j2 = NS - u;
+			const bool two = u != 0 && 2 * u != NS;
+			C v1[R], v2[R];
+#pragma unroll
+			for (int r = 0; r < R; ++r) {
+				v1[r] = c.sm[pidx<PS>(j1 + r * NS)];
+				v2[r] = two ? c.sm[pidx<PS>(j2 + r * NS)] : v1[r];
+			}
+			if constexpr (NS > 1) {
+				apply_twiddles<T, R, NS, TWO>(v1, tw, j1);
+				if (two) apply_twiddles<T, R, NS, TWO>(v2, tw, j2);
+			}
+			dft<R>(v1);
+			if (two) dft<R>(v2);
+			if (two) {
+#pragma unroll
+				for (int r = 0; r < R; ++r) {
+					const int k = j1 + r * NS, mk = H - k;
+					if (k < mk) split_pair<T, H>(out, c.rtw, k, v1[r], v2[R - 1 - r]);
+					else split_pair<T, H>(out, c.rtw, mk, v2[R - 1 - r], v1[r]);
+				}
+			} else if (j1 == 0) {
+				__stcs(out, mkc(v1[0].x + v1[0].y, v1[0].x - v1[0].y));
+#pragma unroll
+				for (int r = 1; r < R; ++r)
+					if (r <= R - r) split_pair<T, H>(out, c.rtw, r * NS, v1[r], v1[R - r]);
+			} else {
+#pragma unroll
+				for (int r = 0; r < R; ++r)
+					if (r <= R - 1 - r) split_pair<T, H>(out, c.rtw, j1 + r * NS, v1[r], v1[R - 1 - r]);
+			}
+		}
+	}
+}
+
+// First pass of a RealFFT inverse with the pre-twiddle fused: H bins in HBM -> shared memory.
+template <typename T, int H, int THREADS, int R, int KIND, bool CIN, bool COUT>
+__device__ __forceinline__ void pass_first_c2r(const Ctx<T, KIND, CIN, COUT> &c) {
+	using C = typename Cx<T>::C;
+	constexpr int PS = Cx<T>::kPadShift;
+	constexpr int NB = H / R, U = NB / 2 + 1, UPT = (U + THREADS - 1) / THREADS;
+	static_assert(Specialised<R>::value && NB * R == H, "fused pre-twiddle needs a register butterfly first");
+	const C *in = reinterpret_cast<const C *>(c.gin);
+#pragma unroll
+	for (int q = 0; q < UPT; ++q) {
+		const int u = c.t + q * THREADS;
+		if (c.valid && u < U) {
+			const int j1 = u, j2 = NB - u;
+			const bool two = u != 0 && 2 * u != NB;
+			C v1[R], v2[R];
+			if (two) {
+#pragma unroll
+				for (int r = 0; r < R; ++r) {
+					const int k = j1 + r * NB, mk = H - k;
+					if (k < mk) pretwiddle_pair<T, H>(in, c.rtw, k, v1[r], v2[R - 1 - r]);
+					else pretwiddle_pair<T, H>(in, c.rtw, mk, v2[R - 1 - r], v1[r]);
+				}
+			} else if (j1 == 0) {
+				const C v = __ldcs(in);
+				v1[0] = conj(mkc(v.x + v.y, v.x - v.y));
+#pragma unroll
+				for (int r = 1; r < R; ++r) {
+					C unused;
+					if (r < R - r) pretwiddle_pair<T, H>(in, c.rtw, r * NB, v1[r], v1[R - r]);
+					else if (r == R - r) pretwiddle_pair<T, H>(in, c.rtw, r * NB, unused, v1[r]);
+				}
+			} else {
+#pragma unroll
+				for (int r = 0; r < R; ++r) {
+					C unused;
+					if (r < R - 1 - r) pretwiddle_pair<T, H>(in, c.rtw, j1 + r * NB, v1[r], v1[R - 1 - r]);
+					else if (r == R - 1 - r) pretwiddle_pair<T, H>(in, c.rtw, j1 + r * NB, unused, v1[r]);
+				}
+			}
+			dft<R>(v1);
+#pragma unroll
+			for (int r = 0; r < R; ++r) c.sm[pidx<PS>(j1 * R + r)] = v1[r];
+			if (two) {
+				dft<R>(v2);
+#pragma unroll
+				for (int r = 0; r < R; ++r) c.sm[pidx<PS>(j2 * R + r)] = v2[r];
+			}
+		}
+	}
+	__syncthreads();
+}
+
 // All passes of the transform; `after_first` runs (on every thread) once the first pass has
 // consumed its input.
 template <typename T, int N, int THREADS, int NS, int TWO, int ROOTS, int FIRST_SRC, int LAST_DST, int KIND, bool CIN,
@@ -515,7 +660,10 @@ __device__ __forceinline__ void passes(const Ctx<T, KIND, CIN, COUT> &c, const t
 	constexpr bool last = sizeof...(Rest) == 0;
 	constexpr int SRC = NS == 1 ? FIRST_SRC : kSmem;
 	constexpr int DST = last ? LAST_DST : kSmem;
-	pass<T, N, THREADS, R, NS, TWO, ROOTS, SRC, DST, KIND, CIN, COUT, ODD, EMAX>(c, tw, roots);
+	static_assert(!(SRC == kFusedC2R && last) && !(DST == kFusedR2C && NS == 1), "fused split needs two passes or more");
+	if constexpr (SRC == kFusedC2R) pass_first_c2r<T, N, THREADS, R, KIND, CIN, COUT>(c);
+	else if constexpr (DST == kFusedR2C) pass_last_r2c<T, N, THREADS, R, NS, TWO, KIND, CIN, COUT>(c, tw);
+	else pass<T, N, THREADS, R, NS, TWO, ROOTS, SRC, DST, KIND, CIN, COUT, ODD, EMAX>(c, tw, roots);
 	if constexpr (NS == 1) after_first();
 	if constexpr (!last)
 		passes<T, N, THREADS, NS * R, TWO + TwCount<R, NS>::value, ROOTS + RootCount<R>::value, FIRST_SRC, LAST_DST,
@@ -599,7 +747,7 @@ __device__ __forceinline__ void real_pre(const Ctx<T, KIND, CIN, COUT> &c, const
 // one pass.  MINB: CTAs the compiler must fit per SM (caps registers; more resident warps hide the
 // first pass's HBM latency).
 template <typename T, int N, int THREADS, int PER_CTA, int SMEM_STRIDE, int KIND, bool INV, bool ODD, int EMAX,
-          int MINB, int... Rs>
+          int MINB, bool FUSE, int... Rs>
 __global__ void __launch_bounds__(THREADS *PER_CTA, MINB) batch(const Args a) {
 	using C = typename Cx<T>::C;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -622,11 +770,19 @@ __global__ void __launch_bounds__(THREADS *PER_CTA, MINB) batch(const Args a) {
 	const C *tw = reinterpret_cast<const C *>(a.tw);
 	const C *roots = reinterpret_cast<const C *>(a.roots);
 	const C *rtw = reinterpret_cast<const C *>(a.rtw);
+	c.rtw = rtw;
 	prefetch_ahead<T, PER_CTA, THREADS * PER_CTA>(a);
-	if constexpr (C2R) real_pre<T, N, THREADS, KIND, INV, INV>(c, rtw);
-	passes<T, N, THREADS, 1, 0, 0, C2R ? kSmem : kGlobal, R2C ? kSmem : kGlobal, KIND, INV, INV, ODD, EMAX, Rs...>(
-	    c, tw, roots);
-	if constexpr (R2C) real_post<T, N, THREADS, KIND, INV, INV>(c, rtw);
+	if constexpr (FUSE) {
+		// real split / pre-twiddle inside the last / first pass (KIND == kReal, even length)
+		static_assert(KIND == kReal && !ODD, "fused split is for RealFFT of even length");
+		passes<T, N, THREADS, 1, 0, 0, C2R ? kFusedC2R : kGlobal, R2C ? kFusedR2C : kGlobal, KIND, INV, INV, ODD, EMAX,
+		       Rs...>(c, tw, roots);
+	} else {
+		if constexpr (C2R) real_pre<T, N, THREADS, KIND, INV, INV>(c, rtw);
+		passes<T, N, THREADS, 1, 0, 0, C2R ? kSmem : kGlobal, R2C ? kSmem : kGlobal, KIND, INV, INV, ODD, EMAX, Rs...>(
+		    c, tw, roots);
+		if constexpr (R2C) real_post<T, N, THREADS, KIND, INV, INV>(c, rtw);
+	}
 }
 
 // ------------------------------------------------------------------ asynchronous staging

@@ -31,6 +31,7 @@ struct Schedule {
 	bool odd = false;         // real length is odd (scalar loads/stores)
 	bool staged = false;      // ssfft_cl::batch_staged (bulk-copy input staging, persistent CTAs)
 	bool tc = false;          // ssfft_cl::batch_tc (first pass as split-BF16 tensor-core products)
+	int fuse = 0;             // RealFFT split fused into a pass: 1 forward (last pass), 2 inverse (first)
 	int minb = 1;             // launch-bound CTAs per SM (register cap)
 	int emax = 16;            // complex values a thread holds in one pass
 	unsigned in_bytes = 0;    // staged: input bytes of one transform
@@ -48,6 +49,8 @@ struct Knobs {
 	int minb = 0;              // launch-bound CTAs per SM
 	int precision = 0;         // SSFFT_PRECISION_*: 1 = first pass on the tensor cores (split BF16)
 	int prefetch = -1;         // L2 prefetch distance in quarter waves of resident CTAs (-1 default)
+	int fuse = -1;             // RealFFT split fused into a pass: -1 where possible, 0 never (an explicit
+	                           // radix order from the caller is kept as given)
 	// no shape choice made (precision is not a shape choice)
 	bool empty() const { return radices.empty() && !cta_threads && !emax && !minb && prefetch < 0; }
 	std::string str() const;
@@ -59,12 +62,14 @@ struct Tables {
 	const float *tcb = nullptr;  // tensor-core schedules: the first pass's DFT, 32 x 32 FP32
 };
 
+// Forward and inverse may differ (a RealFFT with the split fused runs the radix list rotated
+// differently per direction); otherwise sch_inv / tab_inv equal sch / tab.
 struct SubPlan {
-	Schedule sch;
-	Tables tab;
+	Schedule sch, sch_inv;
+	Tables tab, tab_inv;
 	CUfunction fwd = nullptr, inv = nullptr;
 	int grid_cap = 0;        // staged: resident CTAs (persistent grid)
-	long long pf_dist = 0;   // plain batch kernel: L2 prefetch distance in CTAs (resident CTAs)
+	long long pf_dist = 0, pf_dist_inv = 0;  // batch kernel: L2 prefetch distance in CTAs
 	unsigned *err = nullptr; // staged: device error word
 };
 
@@ -109,9 +114,11 @@ void unit_root(unsigned long long k, unsigned long long L, double *re, double *i
 bool choose_radices(int n, std::vector<int> &radices);
 // allow_staged: 0 never, 1 when SSFFT_STAGED=1, 2 always (where the size allows it)
 bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, Schedule &s, int allow_staged = 1,
-                   const Knobs *knobs = nullptr);
+                   const Knobs *knobs = nullptr, int fuse = 0);
+// dir: -1 the direction-independent base schedule, 0 forward, 1 inverse (RealFFT plans may fuse
+// the split into a pass, with the radix list rotated per direction)
 bool single_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, Schedule &s,
-                     const Knobs *knobs = nullptr, int allow_staged = 1);
+                     const Knobs *knobs = nullptr, int allow_staged = 1, int dir = -1);
 void single_tables(const Schedule &s, size_t n_real, std::vector<double> &tw, std::vector<double> &roots,
                    std::vector<double> &rtw, std::vector<double> &rot);
 void radix_candidates(int n, std::vector<std::vector<int>> &out);

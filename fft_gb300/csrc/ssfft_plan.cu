@@ -220,7 +220,7 @@ std::string Knobs::str() const {
 }
 
 bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, Schedule &s, int allow_staged,
-                   const Knobs *knobs) {
+                   const Knobs *knobs, int fuse) {
 	s = Schedule();
 	s.dtype = dtype;
 	s.n = n;
@@ -248,11 +248,21 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	// threads per transform: every pass must fit its butterflies into `emax` values per thread;
 	// 16 normally, 32 when 16 would need more than one CTA's threads (long sizes whose composite
 	// radices hold a single butterfly per thread)
+	s.fuse = fuse;
 	auto threads_for = [&](int emax) {
 		int t = 1;
-		for (int r : s.radices) {
-			const int per = r == 1 ? 1 : std::max(1, emax / r);  // butterflies a thread holds
-			const int need = specialised(r) ? (n / r + per - 1) / per : (n + emax - 1) / emax;
+		for (size_t p = 0; p < s.radices.size(); ++p) {
+			const int r = s.radices[p];
+			const bool mirror = (fuse == 1 && p + 1 == s.radices.size()) || (fuse == 2 && p == 0);
+			int need;
+			if (mirror) {
+				// mirror-paired pass: units of two butterflies (2r values), n/r/2 + 1 of them
+				const int units = n / r / 2 + 1, per = std::max(1, emax / (2 * r));
+				need = (units + per - 1) / per;
+			} else {
+				const int per = r == 1 ? 1 : std::max(1, emax / r);  // butterflies a thread holds
+				need = specialised(r) ? (n / r + per - 1) / per : (n + emax - 1) / emax;
+			}
 			t = std::max(t, need);
 		}
 		return t;
@@ -346,6 +356,7 @@ std::string Schedule::name(bool inverse) const {
 	     std::to_string(smem_stride) + ", " + std::to_string(kind) + ", " + (inverse ? "true" : "false") + ", ";
 	if (!staged) r += std::string(odd ? "true" : "false") + ", ";
 	r += std::to_string(emax) + ", " + std::to_string(minb);
+	if (!staged) r += std::string(", ") + (fuse ? "true" : "false");
 	for (int x : radices) r += ", " + std::to_string(x);
 	r += ">";
 	return r;
@@ -398,12 +409,40 @@ static int kind_code(ssfft_kind kind) {
 
 // The single-CTA schedule of (n, dtype, kind, batch), or false if n needs the multi-pass path.
 bool single_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, Schedule &s, const Knobs *knobs,
-                     int allow_staged) {
+                     int allow_staged, int dir) {
 	const bool real = kind != SSFFT_COMPLEX;
 	const size_t cn = real ? n / 2 : n;
 	const int max_n = dtype == SSFFT_F32 ? kMaxSubTransform : kMaxSubTransform / 2;
 	if (cn == 0 || cn > (size_t)max_n) return false;
-	return make_schedule(dtype, (int)cn, kind_code(kind), real && (n & 1), batch, s, allow_staged, knobs);
+	if (!make_schedule(dtype, (int)cn, kind_code(kind), real && (n & 1), batch, s, allow_staged, knobs)) return false;
+	if (dir < 0) return true;
+	// RealFFT (not half-shift), even length, plain kernel, two passes or more, a register radix
+	// <= 8: fuse the split into the last pass (forward) / the pre-twiddle into the first pass
+	// (inverse), with that radix moved to the end / the front.  SSFFT_FUSE=0 turns it off for
+	// plans made while it is set; an explicit radix order keeps the base schedule.
+	const char *env = std::getenv("SSFFT_FUSE");
+	if ((env && env[0] == '0') || kind != SSFFT_REAL || (n & 1) || s.staged || s.tc || s.radices.size() < 2 ||
+	    (knobs && knobs->fuse == 0))
+		return true;
+	int best = -1;
+	for (size_t i = 0; i < s.radices.size(); ++i) {
+		const int r = s.radices[i];
+		if (specialised(r) && r >= 2 && r <= 8 && (best < 0 || r < s.radices[best])) best = (int)i;
+	}
+	if (best < 0) return true;
+	std::vector<int> rot = s.radices;
+	const int r = rot[best];
+	rot.erase(rot.begin() + best);
+	if (dir == 0) rot.push_back(r);
+	else rot.insert(rot.begin(), r);
+	Knobs k = knobs ? *knobs : Knobs();
+	k.radices = rot;
+	Schedule f;
+	if (!make_schedule(dtype, (int)cn, kind_code(kind), false, batch, f, allow_staged, &k, dir == 0 ? 1 : 2))
+		return true;
+	if (f.staged || f.tc) return true;
+	s = f;
+	return true;
 }
 
 // FP64 tables of a single-CTA schedule: pass twiddles, direct-pass roots, and for real kinds
@@ -481,15 +520,22 @@ static ssfft_status plan_build_single(Plan *p) {
 		if (st != SSFFT_SUCCESS) return st;
 		p->knobs = best;
 	}
-	if (!single_schedule(p->n, p->dtype, p->kind, p->batch, s, &p->knobs))
+	Schedule &si = p->main.sch_inv;
+	if (!single_schedule(p->n, p->dtype, p->kind, p->batch, s, &p->knobs, 1, 0) ||
+	    !single_schedule(p->n, p->dtype, p->kind, p->batch, si, &p->knobs, 1, 1))
 		return SSFFT_ERR_INVALID_VALUE;  // explicit knobs that do not fit this size
-	if (s.smem_bytes > device_smem_limit(p->device)) return SSFFT_ERR_UNSUPPORTED;
-	std::vector<double> tw, roots, rtw, rot;
+	const size_t smem_limit = device_smem_limit(p->device);
+	if (s.smem_bytes > smem_limit || si.smem_bytes > smem_limit) return SSFFT_ERR_UNSUPPORTED;
+	const bool split = si.radices != s.radices;  // inverse has its own pass tables
+	std::vector<double> tw, roots, rtw, rot, tw_i, roots_i, unused_rtw, unused_rot;
 	single_tables(s, p->n, tw, roots, rtw, rot);
+	if (split) single_tables(si, p->n, tw_i, roots_i, unused_rtw, unused_rot);
 	const size_t sb = p->dtype == SSFFT_F32 ? 4 : 8;
 	const size_t off_tw = 0;
 	const size_t off_roots = align_up(off_tw + tw.size() * sb, 256);
-	const size_t off_rtw = align_up(off_roots + roots.size() * sb, 256);
+	const size_t off_tw_i = align_up(off_roots + roots.size() * sb, 256);
+	const size_t off_roots_i = align_up(off_tw_i + tw_i.size() * sb, 256);
+	const size_t off_rtw = align_up(off_roots_i + roots_i.size() * sb, 256);
 	const size_t off_rot = align_up(off_rtw + rtw.size() * sb, 256);
 	std::vector<float> tcb;
 	if (s.tc) tc_matrix(s.radices[0], tcb);
@@ -497,16 +543,11 @@ static ssfft_status plan_build_single(Plan *p) {
 	const size_t off_err = align_up(off_tcb + tcb.size() * 4, 256);
 	const size_t total = align_up(off_err + 16, 256);
 	std::vector<unsigned char> blob(total, 0);
-	if (sb == 4) {
-		put_table<float>(blob, off_tw, tw);
-		put_table<float>(blob, off_roots, roots);
-		put_table<float>(blob, off_rtw, rtw);
-		put_table<float>(blob, off_rot, rot);
-	} else {
-		put_table<double>(blob, off_tw, tw);
-		put_table<double>(blob, off_roots, roots);
-		put_table<double>(blob, off_rtw, rtw);
-		put_table<double>(blob, off_rot, rot);
+	const std::pair<size_t, const std::vector<double> *> parts[] = {
+	    {off_tw, &tw}, {off_roots, &roots}, {off_tw_i, &tw_i}, {off_roots_i, &roots_i}, {off_rtw, &rtw}, {off_rot, &rot}};
+	for (const auto &pt : parts) {
+		if (sb == 4) put_table<float>(blob, pt.first, *pt.second);
+		else put_table<double>(blob, pt.first, *pt.second);
 	}
 	if (!tcb.empty()) std::memcpy(blob.data() + off_tcb, tcb.data(), tcb.size() * 4);
 	cudaError_t e = cudaMalloc(&p->d_tables, total);
@@ -520,17 +561,24 @@ static ssfft_status plan_build_single(Plan *p) {
 	p->main.tab.rtw = base + off_rtw;
 	p->main.tab.rot = base + off_rot;
 	p->main.tab.tcb = tcb.empty() ? nullptr : reinterpret_cast<const float *>(base + off_tcb);
+	p->main.tab_inv = p->main.tab;
+	if (split) {
+		p->main.tab_inv.tw = base + off_tw_i;
+		p->main.tab_inv.roots = base + off_roots_i;
+	}
 	p->main.err = reinterpret_cast<unsigned *>(static_cast<unsigned char *>(p->d_tables) + off_err);
 
 	std::vector<CUfunction> fns;
-	ssfft_status st = jit_kernels({s.name(false), s.name(true)}, s.smem_bytes, fns);
+	ssfft_status st = jit_kernels({s.name(false), si.name(true)}, std::max(s.smem_bytes, si.smem_bytes), fns);
 	if (st != SSFFT_SUCCESS) return st;
 	p->main.fwd = fns[0];
 	p->main.inv = fns[1];
 	{
-		const long long resident = resident_ctas(fns[0], fns[1], s, p->device);
-		if (s.staged) p->main.grid_cap = (int)resident;
+		const long long resident = resident_ctas(fns[0], fns[0], s, p->device);
+		const long long resident_i = resident_ctas(fns[1], fns[1], si, p->device);
+		if (s.staged) p->main.grid_cap = (int)std::min(resident, resident_i);
 		p->main.pf_dist = prefetch_distance(s, p->knobs, resident);
+		p->main.pf_dist_inv = prefetch_distance(si, p->knobs, resident_i);
 	}
 	p->launches_per_exec = 1;
 	return SSFFT_SUCCESS;
@@ -608,22 +656,23 @@ ssfft_status launch_batch_offs(const Plan *p, int inverse, const void *in, void 
 	if (batch == 0) return SSFFT_SUCCESS;
 	if (p->large) return SSFFT_ERR_UNSUPPORTED;
 	if (p->main.sch.staged) return launch_unstaged(p, inverse, in, out, batch, s, d_offs);
-	const Schedule &sch = p->main.sch;
+	const Schedule &sch = inverse ? p->main.sch_inv : p->main.sch;
+	const Tables &tab = inverse ? p->main.tab_inv : p->main.tab;
 	ssfft_cl::Args a;
 	std::memset(&a, 0, sizeof a);
 	a.in = in;
 	a.out = out;
 	a.batch = (long long)batch;
 	plan_dists(p, inverse, a.in_dist, a.out_dist);
-	a.tw = p->main.tab.tw;
-	a.rtw = p->main.tab.rtw;
-	a.rot = p->main.tab.rot;
-	a.roots = p->main.tab.roots;
-	a.tcb = p->main.tab.tcb;
+	a.tw = tab.tw;
+	a.rtw = tab.rtw;
+	a.rot = tab.rot;
+	a.roots = tab.roots;
+	a.tcb = tab.tcb;
 	a.err = p->main.err;
 	a.spin_limit = 1u << 22;
 	a.offs = d_offs;
-	a.pf_dist = p->main.pf_dist;
+	a.pf_dist = inverse ? p->main.pf_dist_inv : p->main.pf_dist;
 	const long long grid = ((long long)batch + sch.per_cta - 1) / sch.per_cta;
 	if (grid > 0x7fffffffLL) return SSFFT_ERR_INVALID_SIZE;
 	return jit_launch(inverse ? p->main.inv : p->main.fwd, (unsigned)grid, (unsigned)sch.cta_threads(),
@@ -632,22 +681,23 @@ ssfft_status launch_batch_offs(const Plan *p, int inverse, const void *in, void 
 
 ssfft_status launch_batch(const Plan *p, int inverse, const void *in, void *out, size_t batch, cudaStream_t s) {
 	if (batch == 0) return SSFFT_SUCCESS;
-	const Schedule &sch = p->main.sch;
+	const Schedule &sch = inverse ? p->main.sch_inv : p->main.sch;
+	const Tables &tab = inverse ? p->main.tab_inv : p->main.tab;
 	ssfft_cl::Args a;
 	std::memset(&a, 0, sizeof a);
 	a.in = in;
 	a.out = out;
 	a.batch = (long long)batch;
 	plan_dists(p, inverse, a.in_dist, a.out_dist);
-	a.tw = p->main.tab.tw;
-	a.rtw = p->main.tab.rtw;
-	a.rot = p->main.tab.rot;
-	a.roots = p->main.tab.roots;
+	a.tw = tab.tw;
+	a.rtw = tab.rtw;
+	a.rot = tab.rot;
+	a.roots = tab.roots;
 	a.err = p->main.err;
 	a.spin_limit = 1u << 22;
 	a.in_bytes = sch.in_bytes;
-	a.tcb = p->main.tab.tcb;
-	a.pf_dist = p->main.pf_dist;
+	a.tcb = tab.tcb;
+	a.pf_dist = inverse ? p->main.pf_dist_inv : p->main.pf_dist;
 	long long grid = ((long long)batch + sch.per_cta - 1) / sch.per_cta;
 	if (sch.staged) {
 		if ((uintptr_t)in % 16) return launch_unstaged(p, inverse, in, out, batch, s);
@@ -738,6 +788,7 @@ ssfft_status ssfft_plan_create_ex(ssfft_plan_t *out, size_t n, ssfft_dtype dtype
 		}
 		if (opt->prefetch_quarter_waves != 0) p->knobs.prefetch = std::max(0, opt->prefetch_quarter_waves);
 		for (int i = 0; i < 24 && opt->radices[i] > 0; ++i) p->knobs.radices.push_back(opt->radices[i]);
+		if (!p->knobs.radices.empty()) p->knobs.fuse = 0;  // the caller's order is kept as given
 	}
 	cudaError_t e = cudaGetDevice(&p->device);
 	ssfft_status st = e == cudaSuccess ? SSFFT_SUCCESS : cuda_fail(e, "cudaGetDevice");
@@ -904,6 +955,12 @@ ssfft_status ssfft_diag_staged_timeout(size_t n, unsigned spin_limit, unsigned *
 
 // Compile the kernels a plan of this shape would use (build-time check).
 static thread_local Knobs g_diag_knobs;  // options of the schedule diagnostics in this thread
+static thread_local int g_diag_dir = 0;   // direction whose schedule info / tables report
+
+ssfft_status ssfft_schedule_direction(int inverse) {
+	g_diag_dir = inverse ? 1 : 0;
+	return SSFFT_SUCCESS;
+}
 
 ssfft_status ssfft_schedule_options(const ssfft_plan_options *opt) {
 	g_diag_knobs = Knobs();
@@ -915,6 +972,7 @@ ssfft_status ssfft_schedule_options(const ssfft_plan_options *opt) {
 	g_diag_knobs.minb = opt->min_ctas_per_sm;
 	g_diag_knobs.precision = opt->precision;
 	for (int i = 0; i < 24 && opt->radices[i] > 0; ++i) g_diag_knobs.radices.push_back(opt->radices[i]);
+	if (!g_diag_knobs.radices.empty()) g_diag_knobs.fuse = 0;
 	return SSFFT_SUCCESS;
 }
 
@@ -960,15 +1018,17 @@ ssfft_status ssfft_diag_tc_tile(const float *h_a, const float *h_bt, float *h_d,
 
 ssfft_status ssfft_jit_check(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, const char *arch,
                              size_t *image_bytes) {
-	Schedule s;
-	if (!single_schedule(n, dtype, kind, batch, s, &g_diag_knobs)) return large_jit_check(n, dtype, kind, arch ? arch : "sm_103a", image_bytes);
-	return jit_compile_only({s.name(false), s.name(true)}, arch ? arch : "sm_103a", image_bytes);
+	Schedule s, si;
+	if (!single_schedule(n, dtype, kind, batch, s, &g_diag_knobs, 1, 0) ||
+	    !single_schedule(n, dtype, kind, batch, si, &g_diag_knobs, 1, 1))
+		return large_jit_check(n, dtype, kind, arch ? arch : "sm_103a", image_bytes);
+	return jit_compile_only({s.name(false), si.name(true)}, arch ? arch : "sm_103a", image_bytes);
 }
 
 ssfft_status ssfft_schedule_info(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, int *radices, int cap,
                                  int *npasses, int *threads, int *per_cta, size_t *smem_bytes) {
 	Schedule s;
-	if (!single_schedule(n, dtype, kind, batch, s, &g_diag_knobs)) return SSFFT_ERR_UNSUPPORTED;
+	if (!single_schedule(n, dtype, kind, batch, s, &g_diag_knobs, 1, g_diag_dir)) return SSFFT_ERR_UNSUPPORTED;
 	if (npasses) *npasses = (int)s.radices.size();
 	if (radices)
 		for (int i = 0; i < (int)s.radices.size() && i < cap; ++i) radices[i] = s.radices[i];
@@ -981,7 +1041,7 @@ ssfft_status ssfft_schedule_info(size_t n, ssfft_dtype dtype, ssfft_kind kind, s
 ssfft_status ssfft_schedule_name(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, int inverse, char *buf,
                                  size_t cap) {
 	Schedule s;
-	if (!single_schedule(n, dtype, kind, batch, s, &g_diag_knobs)) return SSFFT_ERR_UNSUPPORTED;
+	if (!single_schedule(n, dtype, kind, batch, s, &g_diag_knobs, 1, inverse ? 1 : 0)) return SSFFT_ERR_UNSUPPORTED;
 	const std::string name = s.name(inverse != 0);
 	if (!buf || cap < name.size() + 1) return SSFFT_ERR_INVALID_VALUE;
 	std::memcpy(buf, name.c_str(), name.size() + 1);
@@ -992,7 +1052,7 @@ ssfft_status ssfft_schedule_tables(size_t n, ssfft_dtype dtype, ssfft_kind kind,
                                    size_t *ntw, double *roots, size_t *nroots, double *rtw, size_t *nrtw, double *rot,
                                    size_t *nrot) {
 	Schedule s;
-	if (!single_schedule(n, dtype, kind, batch, s, &g_diag_knobs)) return SSFFT_ERR_UNSUPPORTED;
+	if (!single_schedule(n, dtype, kind, batch, s, &g_diag_knobs, 1, g_diag_dir)) return SSFFT_ERR_UNSUPPORTED;
 	std::vector<double> vtw, vroots, vrtw, vrot;
 	single_tables(s, n, vtw, vroots, vrtw, vrot);
 	const std::vector<double> *src[4] = {&vtw, &vroots, &vrtw, &vrot};

@@ -104,7 +104,7 @@ void store_locked(const std::string &key, const Knobs &k) {
 
 struct Candidate {
 	Knobs knobs;
-	Schedule sch;
+	Schedule sch, sch_inv;  // forward and inverse (RealFFT plans may differ per direction)
 	std::vector<CUfunction> fns;
 	ssfft_status st = SSFFT_ERR_UNSUPPORTED;
 	double fwd_us = 0, inv_us = 0;
@@ -137,21 +137,25 @@ void compile_all(const Plan *p, size_t tb, std::vector<Candidate> &cs) {
 			cudaSetDevice(p->device);
 			for (size_t i = next++; i < cs.size(); i = next++) {
 				Candidate &c = cs[i];
-				if (!single_schedule(p->n, p->dtype, p->kind, tb, c.sch, &c.knobs, 0) || c.sch.smem_bytes > limit) {
+				if (!single_schedule(p->n, p->dtype, p->kind, tb, c.sch, &c.knobs, 0, 0) ||
+				    !single_schedule(p->n, p->dtype, p->kind, tb, c.sch_inv, &c.knobs, 0, 1) ||
+				    c.sch.smem_bytes > limit || c.sch_inv.smem_bytes > limit) {
 					c.st = SSFFT_ERR_UNSUPPORTED;
 					continue;
 				}
-				c.st = jit_kernels({c.sch.name(false), c.sch.name(true)}, c.sch.smem_bytes, c.fns);
+				c.st = jit_kernels({c.sch.name(false), c.sch_inv.name(true)},
+				                   std::max(c.sch.smem_bytes, c.sch_inv.smem_bytes), c.fns);
 			}
 		});
 	for (auto &x : th) x.join();
 }
 
-ssfft_status time_one(const Plan *p, size_t tb, Scratch &sc, Candidate &c) {
+ssfft_status time_dir(const Plan *p, size_t tb, Scratch &sc, Candidate &c, int inv) {
+	const Schedule &sch = inv ? c.sch_inv : c.sch;
 	std::vector<double> tw, roots, rtw, rot;
-	single_tables(c.sch, p->n, tw, roots, rtw, rot);
+	single_tables(sch, p->n, tw, roots, rtw, rot);
 	std::vector<float> tcb;
-	if (c.sch.tc) tc_matrix(c.sch.radices[0], tcb);
+	if (sch.tc) tc_matrix(sch.radices[0], tcb);
 	const size_t sb = p->dtype == SSFFT_F32 ? 4 : 8;
 	const size_t o_roots = (tw.size() * sb + 255) & ~(size_t)255;
 	const size_t o_rtw = (o_roots + roots.size() * sb + 255) & ~(size_t)255;
@@ -186,8 +190,8 @@ ssfft_status time_one(const Plan *p, size_t tb, Scratch &sc, Candidate &c) {
 	cudaError_t e = cudaMemcpy(sc.tab, blob.data(), total, cudaMemcpyHostToDevice);
 	if (e != cudaSuccess) return cuda_fail(e, "tune tables copy");
 	const unsigned char *base = static_cast<const unsigned char *>(sc.tab);
-	const long long grid = ((long long)tb + c.sch.per_cta - 1) / c.sch.per_cta;
-	for (int inv = 0; inv < 2; ++inv) {
+	const long long grid = ((long long)tb + sch.per_cta - 1) / sch.per_cta;
+	{
 		ssfft_cl::Args a;
 		std::memset(&a, 0, sizeof a);
 		a.in = sc.in;
@@ -201,16 +205,16 @@ ssfft_status time_one(const Plan *p, size_t tb, Scratch &sc, Candidate &c) {
 		a.tcb = tcb.empty() ? nullptr : reinterpret_cast<const float *>(base + o_tcb);
 		a.err = reinterpret_cast<unsigned *>(static_cast<unsigned char *>(sc.tab) + o_err);
 		a.spin_limit = 1u << 22;
-		a.pf_dist = prefetch_distance(c.sch, c.knobs, resident_ctas(c.fns[0], c.fns[1], c.sch, p->device));
 		CUfunction f = c.fns[inv];
-		ssfft_status st = jit_launch(f, (unsigned)grid, (unsigned)c.sch.cta_threads(), c.sch.smem_bytes, sc.stream, &a);
+		a.pf_dist = prefetch_distance(sch, c.knobs, resident_ctas(f, f, sch, p->device));
+		ssfft_status st = jit_launch(f, (unsigned)grid, (unsigned)sch.cta_threads(), sch.smem_bytes, sc.stream, &a);
 		if (st != SSFFT_SUCCESS) return st;
 		// repeats scale with the work so that each measurement spans ~0.3 ms or more
 		const double work = (double)tb * (double)p->n;
 		const int reps = (int)std::min(20.0, std::max(3.0, std::ceil(3e7 / std::max(work, 1.0))));
 		cudaEventRecord(sc.ev[0], sc.stream);
 		for (int r = 0; r < reps && st == SSFFT_SUCCESS; ++r)
-			st = jit_launch(f, (unsigned)grid, (unsigned)c.sch.cta_threads(), c.sch.smem_bytes, sc.stream, &a);
+			st = jit_launch(f, (unsigned)grid, (unsigned)sch.cta_threads(), sch.smem_bytes, sc.stream, &a);
 		cudaEventRecord(sc.ev[1], sc.stream);
 		if (st != SSFFT_SUCCESS) return st;
 		e = cudaEventSynchronize(sc.ev[1]);
@@ -218,6 +222,14 @@ ssfft_status time_one(const Plan *p, size_t tb, Scratch &sc, Candidate &c) {
 		float ms = 0;
 		cudaEventElapsedTime(&ms, sc.ev[0], sc.ev[1]);
 		(inv ? c.inv_us : c.fwd_us) = 1e3 * ms / reps;
+	}
+	return SSFFT_SUCCESS;
+}
+
+ssfft_status time_one(const Plan *p, size_t tb, Scratch &sc, Candidate &c) {
+	for (int inv = 0; inv < 2; ++inv) {
+		ssfft_status st = time_dir(p, tb, sc, c, inv);
+		if (st != SSFFT_SUCCESS) return st;
 	}
 	return SSFFT_SUCCESS;
 }
@@ -268,7 +280,7 @@ ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log) 
 		std::lock_guard<std::mutex> lock(g_time_mu);
 		for (auto &c : cs) {
 			if (c.st != SSFFT_SUCCESS) continue;
-			const std::string nm = c.sch.name(false) + "|pf" + std::to_string(c.knobs.prefetch);
+			const std::string nm = c.sch.name(false) + "|" + c.sch_inv.name(true) + "|pf" + std::to_string(c.knobs.prefetch);
 			auto it = timed.find(nm);
 			if (it != timed.end()) {
 				c.fwd_us = it->second;

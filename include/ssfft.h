@@ -241,6 +241,9 @@ ssfft_status ssfft_fft_noalloc_f32(const void *d_in, void *d_out, size_t n, int 
  * get the counts). */
 /* Options the diagnostics below apply in the calling thread (NULL: planner defaults). */
 ssfft_status ssfft_schedule_options(const ssfft_plan_options *options);
+/* Direction (0 forward, 1 inverse) whose schedule ssfft_schedule_info / _tables report in the
+ * calling thread: a RealFFT plan may run its radix list in a different order per direction. */
+ssfft_status ssfft_schedule_direction(int inverse);
 /* Tensor-core tile check (GPU): D = A B for one 128 x 32 x 32 FP32 tile through the split-BF16
  * tcgen05 path (A row-major 128 x 32, bt = B transposed, 32 x 32 row-major, D row-major
  * 128 x 32, all host memory); *flags receives the kernel's error flag.  No reference

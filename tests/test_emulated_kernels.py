@@ -27,6 +27,9 @@ CASES = [
     (98, "f32", "real", 3, 3), (480, "f32", "real", 5, 5), (3840, "f32", "real", 2, 2),
     (64, "f32", "complex", 300, 300), (1024, "f64", "complex", 7, 7), (480, "f32", "real", 40, 40),
     (3840, "f32", "real", 5, 5), (960, "f32", "real_halfshift", 9, 9),
+    (1920, "f32", "real", 3, 3), (1000, "f64", "real", 2, 2), (64, "f32", "real", 50, 50), (30, "f64", "real", 3, 3),
+    (96, "f64", "real", 4, 4), (100, "f32", "real", 7, 7), (8192, "f32", "real", 1, 1), (36, "f32", "real", 9, 9),
+    (18, "f64", "real", 2, 2), (12, "f32", "real", 3, 3),
     (2, "f64", "real_halfshift", 1, 1), (4, "f64", "real_halfshift", 2, 2), (9, "f64", "real_halfshift", 1, 1),
     (12, "f32", "real_halfshift", 2, 2), (98, "f64", "real_halfshift", 1, 1), (960, "f32", "real_halfshift", 2, 2),
 ]
@@ -73,13 +76,16 @@ def emulator(staged_schedules, tmp_path_factory):
     for case, tc in [(c, False) for c in CASES] + [(c, True) for c in TC_CASES]:
         (n, dt, kind, pb, _) = case
         F.schedule_options(**({"precision": "split_bf16"} if tc else {}))
-        info = F.schedule_info(n, dt, kind, pb)
         for inv in (False, True):
+            # a RealFFT plan may run a different radix order per direction (fused split)
+            F.schedule_direction(inv)
+            info = F.schedule_info(n, dt, kind, pb)
             name = F.schedule_name(n, dt, kind, pb, inv)
             index[(n, dt, kind, pb, inv, tc)] = (len(lines), info)
             lines.append(f'{{"{n}-{dt}-{kind}-{int(inv)}", &{name}, {info["threads"] * info["per_cta"]}, '
                          f'{info["smem_bytes"]}}},')
         F.schedule_options()
+        F.schedule_direction(False)
     (d / "emu_cases.inc").write_text("\n".join(lines) + "\n")
     exe = d / "emu"
     cmd = ["g++", "-std=c++20", "-O1", "-pthread", "-w", "-I", str(d), "-I", os.path.join(ROOT, "tests", "emu"),
@@ -93,6 +99,7 @@ def _run(emulator, n, dt, kind, pb, eb, inv, x, tc=False):
     exe, index, d = emulator
     ci, info = index[(n, dt, kind, pb, inv, tc)]
     F.schedule_options(**({"precision": "split_bf16"} if tc else {}))
+    F.schedule_direction(inv)
     sdt = np.float32 if dt == "f32" else np.float64
     real = kind != "complex"
     h2 = 2 * (n // 2)
@@ -111,6 +118,7 @@ def _run(emulator, n, dt, kind, pb, eb, inv, x, tc=False):
     if "batch_tc" in name:
         blob += tc_matrix(info["radices"][0]).tobytes()
     F.schedule_options()
+    F.schedule_direction(False)
     fi, fo, ft = d / f"in{ci}", d / f"out{ci}", d / f"tab{ci}"
     fi.write_bytes(xin.tobytes())
     fo.write_bytes(out.tobytes())
