@@ -552,49 +552,87 @@ __device__ __forceinline__ void pretwiddle_pair(const typename Cx<T>::C *in, con
 	zci = sub(odd, even);
 }
 
+// Units: unit 0 holds the self-mirrored butterflies 0 and (for even M) M/2, unit u >= 1 holds u
+// and M - u, so every unit has two butterflies (but unit 0 of an odd M) and M/2 rounded up units
+// cover the pass.
+
+// Forward split of the outputs X[j + r NS] of a self-mirrored butterfly j (0 or NS/2).
+template <typename T, int H, int R, int NS>
+__device__ __forceinline__ void split_self(typename Cx<T>::C *out, const typename Cx<T>::C *rtw, int j,
+                                           const typename Cx<T>::C (&v)[R]) {
+	if (j == 0) {
+		__stcs(out, mkc(v[0].x + v[0].y, v[0].x - v[0].y));  // DC and Nyquist in bin 0
+#pragma unroll
+		for (int r = 1; r < R; ++r)
+			if (r <= R - r) split_pair<T, H>(out, rtw, r * NS, v[r], v[R - r]);
+	} else {
+#pragma unroll
+		for (int r = 0; r < R; ++r)
+			if (r <= R - 1 - r) split_pair<T, H>(out, rtw, j + r * NS, v[r], v[R - 1 - r]);
+	}
+}
+
 // Last pass of a RealFFT forward with the split fused: shared memory -> H bins in HBM.
 template <typename T, int H, int THREADS, int R, int NS, int TWO, int KIND, bool CIN, bool COUT>
 __device__ __forceinline__ void pass_last_r2c(const Ctx<T, KIND, CIN, COUT> &c, const typename Cx<T>::C *tw) {
 	using C = typename Cx<T>::C;
 	constexpr int PS = Cx<T>::kPadShift;
-	constexpr int U = NS / 2 + 1, UPT = (U + THREADS - 1) / THREADS;
+	constexpr int U = (NS + 1) / 2, UPT = (U + THREADS - 1) / THREADS;
 	static_assert(Specialised<R>::value && NS * R == H, "fused split needs a register butterfly as the last pass");
 	C *out = reinterpret_cast<C *>(c.gout);
 #pragma unroll
 	for (int q = 0; q < UPT; ++q) {
 		const int u = c.t + q * THREADS;
 		if (c.valid && u < U) {
-			const int j1 = u, j2 = NS - u;
-			const bool two = u != 0 && 2 * u != NS;
+			const int j1 = u, j2 = u == 0 ? NS / 2 : NS - u;
+			const bool has2 = u != 0 || NS % 2 == 0;
 			C v1[R], v2[R];
 #pragma unroll
 			for (int r = 0; r < R; ++r) {
 				v1[r] = c.sm[pidx<PS>(j1 + r * NS)];
-				v2[r] = two ? c.sm[pidx<PS>(j2 + r * NS)] : v1[r];
+				v2[r] = has2 ? c.sm[pidx<PS>(j2 + r * NS)] : v1[r];
 			}
 			if constexpr (NS > 1) {
 				apply_twiddles<T, R, NS, TWO>(v1, tw, j1);
-				if (two) apply_twiddles<T, R, NS, TWO>(v2, tw, j2);
+				if (has2) apply_twiddles<T, R, NS, TWO>(v2, tw, j2);
 			}
 			dft<R>(v1);
-			if (two) dft<R>(v2);
-			if (two) {
+			if (has2) dft<R>(v2);
+			if (u != 0) {
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
 					const int k = j1 + r * NS, mk = H - k;
 					if (k < mk) split_pair<T, H>(out, c.rtw, k, v1[r], v2[R - 1 - r]);
 					else split_pair<T, H>(out, c.rtw, mk, v2[R - 1 - r], v1[r]);
 				}
-			} else if (j1 == 0) {
-				__stcs(out, mkc(v1[0].x + v1[0].y, v1[0].x - v1[0].y));
-#pragma unroll
-				for (int r = 1; r < R; ++r)
-					if (r <= R - r) split_pair<T, H>(out, c.rtw, r * NS, v1[r], v1[R - r]);
 			} else {
-#pragma unroll
-				for (int r = 0; r < R; ++r)
-					if (r <= R - 1 - r) split_pair<T, H>(out, c.rtw, j1 + r * NS, v1[r], v1[R - 1 - r]);
+				split_self<T, H, R, NS>(out, c.rtw, 0, v1);
+				if (has2) split_self<T, H, R, NS>(out, c.rtw, NS / 2, v2);
 			}
+		}
+	}
+}
+
+// Inverse pre-twiddle of the inputs z[j + r NB] of a self-mirrored butterfly j (0 or NB/2).
+template <typename T, int H, int R, int NB>
+__device__ __forceinline__ void pretwiddle_self(const typename Cx<T>::C *in, const typename Cx<T>::C *rtw, int j,
+                                                typename Cx<T>::C (&v)[R]) {
+	using C = typename Cx<T>::C;
+	if (j == 0) {
+		const C x = __ldcs(in);
+		v[0] = conj(mkc(x.x + x.y, x.x - x.y));
+#pragma unroll
+		for (int r = 1; r < R; ++r) {
+			C unused;
+			if (r < R - r) pretwiddle_pair<T, H>(in, rtw, r * NB, v[r], v[R - r]);
+			else if (r == R - r) pretwiddle_pair<T, H>(in, rtw, r * NB, unused, v[r]);
+		}
+	} else {
+#pragma unroll
+		for (int r = 0; r < R; ++r) {
+			C unused;
+			if (r < R - 1 - r) pretwiddle_pair<T, H>(in, rtw, j + r * NB, v[r], v[R - 1 - r]);
+			else if (r == R - 1 - r) pretwiddle_pair<T, H>(in, rtw, j + r * NB, unused, v[r]);
 		}
 	}
 }
@@ -604,44 +642,31 @@ template <typename T, int H, int THREADS, int R, int KIND, bool CIN, bool COUT>
 __device__ __forceinline__ void pass_first_c2r(const Ctx<T, KIND, CIN, COUT> &c) {
 	using C = typename Cx<T>::C;
 	constexpr int PS = Cx<T>::kPadShift;
-	constexpr int NB = H / R, U = NB / 2 + 1, UPT = (U + THREADS - 1) / THREADS;
+	constexpr int NB = H / R, U = (NB + 1) / 2, UPT = (U + THREADS - 1) / THREADS;
 	static_assert(Specialised<R>::value && NB * R == H, "fused pre-twiddle needs a register butterfly first");
 	const C *in = reinterpret_cast<const C *>(c.gin);
 #pragma unroll
 	for (int q = 0; q < UPT; ++q) {
 		const int u = c.t + q * THREADS;
 		if (c.valid && u < U) {
-			const int j1 = u, j2 = NB - u;
-			const bool two = u != 0 && 2 * u != NB;
+			const int j1 = u, j2 = u == 0 ? NB / 2 : NB - u;
+			const bool has2 = u != 0 || NB % 2 == 0;
 			C v1[R], v2[R];
-			if (two) {
+			if (u != 0) {
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
 					const int k = j1 + r * NB, mk = H - k;
 					if (k < mk) pretwiddle_pair<T, H>(in, c.rtw, k, v1[r], v2[R - 1 - r]);
 					else pretwiddle_pair<T, H>(in, c.rtw, mk, v2[R - 1 - r], v1[r]);
 				}
-			} else if (j1 == 0) {
-				const C v = __ldcs(in);
-				v1[0] = conj(mkc(v.x + v.y, v.x - v.y));
-#pragma unroll
-				for (int r = 1; r < R; ++r) {
-					C unused;
-					if (r < R - r) pretwiddle_pair<T, H>(in, c.rtw, r * NB, v1[r], v1[R - r]);
-					else if (r == R - r) pretwiddle_pair<T, H>(in, c.rtw, r * NB, unused, v1[r]);
-				}
 			} else {
-#pragma unroll
-				for (int r = 0; r < R; ++r) {
-					C unused;
-					if (r < R - 1 - r) pretwiddle_pair<T, H>(in, c.rtw, j1 + r * NB, v1[r], v1[R - 1 - r]);
-					else if (r == R - 1 - r) pretwiddle_pair<T, H>(in, c.rtw, j1 + r * NB, unused, v1[r]);
-				}
+				pretwiddle_self<T, H, R, NB>(in, c.rtw, 0, v1);
+				if (has2) pretwiddle_self<T, H, R, NB>(in, c.rtw, NB / 2, v2);
 			}
 			dft<R>(v1);
 #pragma unroll
 			for (int r = 0; r < R; ++r) c.sm[pidx<PS>(j1 * R + r)] = v1[r];
-			if (two) {
+			if (has2) {
 				dft<R>(v2);
 #pragma unroll
 				for (int r = 0; r < R; ++r) c.sm[pidx<PS>(j2 * R + r)] = v2[r];

@@ -256,8 +256,8 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 			const bool mirror = (fuse == 1 && p + 1 == s.radices.size()) || (fuse == 2 && p == 0);
 			int need;
 			if (mirror) {
-				// mirror-paired pass: units of two butterflies (2r values), n/r/2 + 1 of them
-				const int units = n / r / 2 + 1, per = std::max(1, emax / (2 * r));
+				// mirror-paired pass: units of two butterflies (2r values), (n/r + 1)/2 of them
+				const int units = (n / r + 1) / 2, per = std::max(1, emax / (2 * r));
 				need = (units + per - 1) / per;
 			} else {
 				const int per = r == 1 ? 1 : std::max(1, emax / r);  // butterflies a thread holds
