@@ -421,8 +421,9 @@ bool single_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch,
 	// (inverse), with that radix moved to the end / the front.  SSFFT_FUSE=0 turns it off for
 	// plans made while it is set; an explicit radix order keeps the base schedule.
 	const char *env = std::getenv("SSFFT_FUSE");
-	if ((env && env[0] == '0') || kind != SSFFT_REAL || (n & 1) || s.staged || s.tc || s.radices.size() < 2 ||
-	    (knobs && knobs->fuse == 0))
+	// (below 256 reals the unfused kernel measured faster on GB300)
+	if ((env && env[0] == '0') || kind != SSFFT_REAL || (n & 1) || n < 256 || s.staged || s.tc ||
+	    s.radices.size() < 2 || (knobs && knobs->fuse == 0))
 		return true;
 	int best = -1;
 	for (size_t i = 0; i < s.radices.size(); ++i) {
