@@ -49,8 +49,8 @@ struct Knobs {
 	int minb = 0;              // launch-bound CTAs per SM
 	int precision = 0;         // SSFFT_PRECISION_*: 1 = first pass on the tensor cores (split BF16)
 	int prefetch = -1;         // L2 prefetch distance in quarter waves of resident CTAs (-1 default)
-	int fuse = -1;             // RealFFT split fused into a pass: -1 where possible, 0 never (an explicit
-	                           // radix order from the caller is kept as given)
+	int fuse = -1;             // RealFFT split fused into a pass: -1 planner default, 0 never (an
+	                           // explicit radix order from the caller is kept as given), 1 always
 	// no shape choice made (precision is not a shape choice)
 	bool empty() const { return radices.empty() && !cta_threads && !emax && !minb && prefetch < 0; }
 	std::string str() const;

@@ -422,8 +422,9 @@ bool single_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch,
 	// plans made while it is set; an explicit radix order keeps the base schedule.
 	const char *env = std::getenv("SSFFT_FUSE");
 	// (below 256 reals the unfused kernel measured faster on GB300)
-	if ((env && env[0] == '0') || kind != SSFFT_REAL || (n & 1) || n < 256 || s.staged || s.tc ||
-	    s.radices.size() < 2 || (knobs && knobs->fuse == 0))
+	const int fuse_knob = knobs ? knobs->fuse : -1;
+	if ((env && env[0] == '0') || kind != SSFFT_REAL || (n & 1) || (n < 256 && fuse_knob != 1) || s.staged ||
+	    s.tc || s.radices.size() < 2 || fuse_knob == 0)
 		return true;
 	int best = -1;
 	for (size_t i = 0; i < s.radices.size(); ++i) {
@@ -790,6 +791,11 @@ ssfft_status ssfft_plan_create_ex(ssfft_plan_t *out, size_t n, ssfft_dtype dtype
 		if (opt->prefetch_quarter_waves != 0) p->knobs.prefetch = std::max(0, opt->prefetch_quarter_waves);
 		for (int i = 0; i < 24 && opt->radices[i] > 0; ++i) p->knobs.radices.push_back(opt->radices[i]);
 		if (!p->knobs.radices.empty()) p->knobs.fuse = 0;  // the caller's order is kept as given
+		if (opt->fuse_split < -1 || opt->fuse_split > 1) {
+			delete p;
+			return SSFFT_ERR_INVALID_VALUE;
+		}
+		if (opt->fuse_split) p->knobs.fuse = opt->fuse_split > 0 ? 1 : 0;
 	}
 	cudaError_t e = cudaGetDevice(&p->device);
 	ssfft_status st = e == cudaSuccess ? SSFFT_SUCCESS : cuda_fail(e, "cudaGetDevice");
@@ -974,6 +980,7 @@ ssfft_status ssfft_schedule_options(const ssfft_plan_options *opt) {
 	g_diag_knobs.precision = opt->precision;
 	for (int i = 0; i < 24 && opt->radices[i] > 0; ++i) g_diag_knobs.radices.push_back(opt->radices[i]);
 	if (!g_diag_knobs.radices.empty()) g_diag_knobs.fuse = 0;
+	if (opt->fuse_split) g_diag_knobs.fuse = opt->fuse_split > 0 ? 1 : 0;
 	return SSFFT_SUCCESS;
 }
 

@@ -92,6 +92,8 @@ typedef struct ssfft_plan_options {
     int precision;         /* SSFFT_PRECISION_FP32 or SSFFT_PRECISION_SPLIT_BF16 */
     int prefetch_quarter_waves; /* L2 prefetch distance of the batch kernel in quarter waves of
                                  * resident CTAs: 0 = planner default (4: one wave), -1 = off */
+    int fuse_split;        /* RealFFT split fused into the last forward / first inverse pass:
+                            * 0 planner default (from 256 reals), 1 wherever possible, -1 never */
 } ssfft_plan_options;
 /* SSFFT_PRECISION_SPLIT_BF16 (complex FP32 plans that run in one CTA): the first radix pass
  * (radix <= 16) runs as tensor-core matrix products (tcgen05) on FP32 values split into three

@@ -75,7 +75,7 @@ def emulator(staged_schedules, tmp_path_factory):
     index = {}
     for case, tc in [(c, False) for c in CASES] + [(c, True) for c in TC_CASES]:
         (n, dt, kind, pb, _) = case
-        F.schedule_options(**({"precision": "split_bf16"} if tc else {}))
+        F.schedule_options(**({"precision": "split_bf16"} if tc else {"fuse_split": 1}))
         for inv in (False, True):
             # a RealFFT plan may run a different radix order per direction (fused split)
             F.schedule_direction(inv)
@@ -98,7 +98,7 @@ def emulator(staged_schedules, tmp_path_factory):
 def _run(emulator, n, dt, kind, pb, eb, inv, x, tc=False):
     exe, index, d = emulator
     ci, info = index[(n, dt, kind, pb, inv, tc)]
-    F.schedule_options(**({"precision": "split_bf16"} if tc else {}))
+    F.schedule_options(**({"precision": "split_bf16"} if tc else {"fuse_split": 1}))
     F.schedule_direction(inv)
     sdt = np.float32 if dt == "f32" else np.float64
     real = kind != "complex"

@@ -107,3 +107,11 @@ def test_multi_autotuned_equals_plain(F):
         ref = oracle.fft(x[off:off + n].astype(np.complex128))
         assert rel_l2(got[off:off + n], ref) <= F32_TOL, n
         off += n
+
+
+@pytest.mark.parametrize("n", [12, 36, 64, 96, 100, 1000, 1024, 3840, 8192])
+@pytest.mark.parametrize("fuse", [1, -1])
+def test_fused_split_on_and_off(F, n, fuse):
+    """The RealFFT split fused into the last forward / first inverse pass (mirror-paired
+    butterflies, odd and even unit counts) and the unfused kernels give the oracle's result."""
+    _real_case(F, n, 33, fuse_split=fuse)
