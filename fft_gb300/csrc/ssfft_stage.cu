@@ -7,6 +7,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
+#include <cstdlib>
 #include <cstring>
 
 #include "ssfft_host.h"
@@ -67,6 +69,24 @@ static ssfft_status stage_init(Plan *p) {
 
 using namespace ssfft;
 
+// The device address of `bytes` of pinned, device-mapped host memory at `p` (cudaHostAlloc,
+// cudaHostRegister), or null if any part of the range is not such memory.
+static void *mapped_host(const void *p, size_t bytes) {
+	if (!bytes) return nullptr;
+	cudaPointerAttributes a, b;
+	const unsigned char *last = static_cast<const unsigned char *>(p) + bytes - 1;
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess || cudaPointerGetAttributes(&b, last) != cudaSuccess) {
+		cudaGetLastError();  // clear the error of a pointer the runtime does not know
+		return nullptr;
+	}
+	if (a.type != cudaMemoryTypeHost || b.type != cudaMemoryTypeHost || !a.devicePointer || !b.devicePointer)
+		return nullptr;
+	if (static_cast<unsigned char *>(b.devicePointer) - static_cast<unsigned char *>(a.devicePointer) !=
+	    (std::ptrdiff_t)(bytes - 1))
+		return nullptr;
+	return a.devicePointer;
+}
+
 extern "C" ssfft_status ssfft_exec_host(ssfft_plan_t plan, int inverse, const void *h_in, void *h_out) {
 	Plan *p = reinterpret_cast<Plan *>(plan);
 	if (!p || !h_in || !h_out) return SSFFT_ERR_INVALID_VALUE;
@@ -74,6 +94,23 @@ extern "C" ssfft_status ssfft_exec_host(ssfft_plan_t plan, int inverse, const vo
 	int prev = -1;
 	cudaGetDevice(&prev);
 	if (prev != p->device) cudaSetDevice(p->device);
+	// zero copy (SSFFT_ZERO_COPY=1): when both buffers are pinned and mapped, the kernel reads and
+	// writes them over the host link directly; no staging copies
+	const char *zc = std::getenv("SSFFT_ZERO_COPY");
+	if (zc && zc[0] == '1' && !p->large) {
+		const void *d_in = mapped_host(h_in, plan_in_bytes(p, inverse, p->batch));
+		void *d_out = mapped_host(h_out, plan_out_bytes(p, inverse, p->batch));
+		if (d_in && d_out) {
+			ssfft_status st = stage_init(p);
+			if (st == SSFFT_SUCCESS) st = launch_batch(p, inverse, d_in, d_out, p->batch, p->stage->stream[0]);
+			if (st == SSFFT_SUCCESS) {
+				cudaError_t e = cudaStreamSynchronize(p->stage->stream[0]);
+				if (e != cudaSuccess) st = cuda_fail(e, "exec_host zero-copy sync");
+			}
+			if (prev >= 0 && prev != p->device) cudaSetDevice(prev);
+			return st;
+		}
+	}
 	ssfft_status st = stage_init(p);
 	if (st != SSFFT_SUCCESS) return st;
 	HostStage *sg = p->stage;
