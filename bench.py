@@ -48,7 +48,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the host-buffer leg (default: steps/10)")
-    ap.add_argument("--workload", default="realfft", choices=["realfft", "fp64", "large", "serve", "uneven"],
+    ap.add_argument("--workload", default="realfft",
+                    choices=["realfft", "fp64", "large", "serve", "uneven", "precision"],
                     help="realfft: the batched RealFFT<float> line (default); fp64: FFT<double> N=1024 x256; "
                          "large: single FP32 transforms of 2^24, 3^15, 2^12 3^4 5^2; serve: request serving sweep")
     ap.add_argument("--serve-duration", type=float, default=1.0)
@@ -561,6 +562,39 @@ def run_uneven(args):
           flush=True)
 
 
+def run_precision(args):
+    """Complex FP32 N=1024, 32768 transforms: the FP32-FMA kernel against the split-BF16
+    tensor-core first pass, forward + inverse, with relL2 against the FP64 oracle."""
+    import torch
+    import fft_gb300 as F
+    import oracle
+    n, b = 1024, 32768
+    rng = np.random.default_rng(11)
+    x = torch.empty(b, n, dtype=torch.complex64, device="cuda")
+    x.real.uniform_(-1, 1)
+    x.imag.uniform_(-1, 1)
+    y = torch.empty_like(x)
+    z = torch.empty_like(x)
+    sh = int(torch.cuda.current_stream().cuda_stream)
+    xs = x[:64].cpu().numpy()
+    ref = oracle.batch(xs.astype(np.complex128), n, real=False, inverse=False)
+    peak, kind = measured_peak_hbm()
+    out = {}
+    for prec in ("fp32", "split_bf16"):
+        p = F.Plan(n, "f32", "complex", b, precision=prec)
+        t = _time_device(lambda: (p.exec(False, x.data_ptr(), y.data_ptr(), sh),
+                                  p.exec(True, y.data_ptr(), z.data_ptr(), sh)), max(args.steps // 8, 20), 3)
+        torch.cuda.synchronize()
+        rel = float(np.linalg.norm(y[:64].cpu().numpy() - ref) / np.linalg.norm(ref))
+        alg = 2 * 16.0 * n * b
+        out[prec] = {"ms_fwd_inv": t * 1e3, "GFLOP_s": 2 * 5 * n * math.log2(n) * b / t / 1e9,
+                     "alg_GB_s": alg / t / 1e9, "frac_of_hbm": alg / t / 1e9 / peak, "relL2_vs_fp64_oracle": rel,
+                     "schedule": p.tuning()["choice"]}
+        del p
+    print(json.dumps({"workload": "complex FP32 N=1024 x 32768, forward + inverse, FP32-FMA vs split-BF16",
+                      "peak_GB_s": peak, "peak_source": kind, **out}), flush=True)
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -572,7 +606,8 @@ def main():
         from fft_gb300 import build as fb
         fb.build()
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        {"fp64": run_fp64, "large": run_large, "serve": run_serve, "uneven": run_uneven}[args.workload](args)
+        {"fp64": run_fp64, "large": run_large, "serve": run_serve, "uneven": run_uneven,
+         "precision": run_precision}[args.workload](args)
     else:
         run_gpu(args, rank, world if "WORLD_SIZE" in os.environ else 1)
 

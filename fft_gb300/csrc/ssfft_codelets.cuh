@@ -211,6 +211,49 @@ __device__ __forceinline__ void dft16(C *v) {
 	for (int k = 0; k < 16; ++k) v[k] = t[k];
 }
 
+// 25 = 5 x 5: DFT5 over n1 of x[5 n1 + n2], twiddle W25^{n2 k1}, DFT5 over n2, transpose.
+template <class C>
+__device__ __forceinline__ void dft25(C *v) {
+	using S = decltype(v[0].x);
+	// W25^e = cos(2 pi e/25) - i sin(2 pi e/25) for the exponents n2 k1 that occur
+	const C w1 = mkc(S(0.96858316112863108), S(-0.24868988716485479));
+	const C w2 = mkc(S(0.87630668004386358), S(-0.48175367410171527));
+	const C w3 = mkc(S(0.72896862742141155), S(-0.68454710592868873));
+	const C w4 = mkc(S(0.53582679497899666), S(-0.84432792550201508));
+	const C w6 = mkc(S(0.062790519529313527), S(-0.99802672842827156));
+	const C w8 = mkc(S(-0.42577929156507266), S(-0.90482705246601953));
+	const C w9 = mkc(S(-0.63742398974868971), S(-0.77051324277578925));
+	const C w12 = mkc(S(-0.99211470131447788), S(-0.12533323356430454));
+	const C w16 = mkc(S(-0.63742398974868949), S(0.77051324277578936));
+#pragma unroll
+	for (int n2 = 0; n2 < 5; ++n2) dft5(v[n2], v[n2 + 5], v[n2 + 10], v[n2 + 15], v[n2 + 20]);
+	v[6] = mul(v[6], w1);    // n2 1, k1 1
+	v[11] = mul(v[11], w2);  // n2 1, k1 2
+	v[16] = mul(v[16], w3);
+	v[21] = mul(v[21], w4);
+	v[7] = mul(v[7], w2);    // n2 2
+	v[12] = mul(v[12], w4);
+	v[17] = mul(v[17], w6);
+	v[22] = mul(v[22], w8);
+	v[8] = mul(v[8], w3);    // n2 3
+	v[13] = mul(v[13], w6);
+	v[18] = mul(v[18], w9);
+	v[23] = mul(v[23], w12);
+	v[9] = mul(v[9], w4);    // n2 4
+	v[14] = mul(v[14], w8);
+	v[19] = mul(v[19], w12);
+	v[24] = mul(v[24], w16);
+#pragma unroll
+	for (int k1 = 0; k1 < 5; ++k1) dft5(v[5 * k1], v[5 * k1 + 1], v[5 * k1 + 2], v[5 * k1 + 3], v[5 * k1 + 4]);
+	C t[25];
+#pragma unroll
+	for (int k1 = 0; k1 < 5; ++k1)
+#pragma unroll
+		for (int k2 = 0; k2 < 5; ++k2) t[k1 + 5 * k2] = v[5 * k1 + k2];
+#pragma unroll
+	for (int k = 0; k < 25; ++k) v[k] = t[k];
+}
+
 // Prime-factor (Good-Thomas) composites R = A * B with gcd(A, B) = 1: input n = (B a + A b) mod R,
 // output k = (B (B^-1 mod A) ka + A (A^-1 mod B) kb) mod R; an A-point DFT over a for each b,
 // then a B-point DFT over b for each ka, with no twiddles in between.  The index maps are
@@ -237,6 +280,16 @@ struct SmallDft<5> {
 	template <class C>
 	__device__ __forceinline__ static void run(C *v) { dft5(v[0], v[1], v[2], v[3], v[4]); }
 };
+template <>
+struct SmallDft<8> {
+	template <class C>
+	__device__ __forceinline__ static void run(C *v) { dft8(v); }
+};
+template <>
+struct SmallDft<9> {
+	template <class C>
+	__device__ __forceinline__ static void run(C *v) { dft9(v); }
+};
 
 template <int A, int B, int KA, int KB, class C>
 __device__ __forceinline__ void dft_pfa(C *v) {
@@ -262,7 +315,8 @@ __device__ __forceinline__ void dft_pfa(C *v) {
 template <int R>
 struct Specialised {
 	static constexpr bool value = R == 1 || R == 2 || R == 3 || R == 4 || R == 5 || R == 6 || R == 8 || R == 9 ||
-	                              R == 10 || R == 12 || R == 15 || R == 16;
+	                              R == 10 || R == 12 || R == 15 || R == 16 || R == 18 || R == 20 || R == 24 ||
+	                              R == 25;
 };
 
 template <int R, class C>
@@ -278,6 +332,10 @@ __device__ __forceinline__ void dft(C *v) {
 	else if constexpr (R == 12) dft_pfa<4, 3, 9, 4>(v);    // 3 (3^-1 mod 4), 4 (4^-1 mod 3)
 	else if constexpr (R == 15) dft_pfa<3, 5, 10, 6>(v);   // 5 (5^-1 mod 3), 3 (3^-1 mod 5)
 	else if constexpr (R == 16) dft16(v);
+	else if constexpr (R == 18) dft_pfa<2, 9, 9, 10>(v);    // 9 (9^-1 mod 2), 2 (2^-1 mod 9 = 5)
+	else if constexpr (R == 20) dft_pfa<4, 5, 5, 16>(v);    // 5 (5^-1 mod 4 = 1), 4 (4^-1 mod 5 = 4)
+	else if constexpr (R == 24) dft_pfa<8, 3, 9, 16>(v);    // 3 (3^-1 mod 8 = 3), 8 (8^-1 mod 3 = 2)
+	else if constexpr (R == 25) dft25(v);
 }
 
 // ------------------------------------------------------------------ per-thread context
@@ -382,16 +440,17 @@ __device__ __forceinline__ void gstore(const Ctx<T, KIND, CIN, COUT> &c, int e, 
 
 // ------------------------------------------------------------------ one pass
 
-// Twiddle rows stored for a pass of radix R: exponents 1, 2, 4, 8 (< R) for the register
+// Twiddle rows stored for a pass of radix R: exponents 1, 2, 4, 8, 16 (< R) for the register
 // butterflies, 1..R-1 for the direct passes.
 template <int R>
 struct TwRows {
-	static constexpr int value = Specialised<R>::value ? (R > 8 ? 4 : R > 4 ? 3 : R > 2 ? 2 : 1) : R - 1;
+	static constexpr int value =
+	    Specialised<R>::value ? (R > 16 ? 5 : R > 8 ? 4 : R > 4 ? 3 : R > 2 ? 2 : 1) : R - 1;
 };
 
-// v[r] *= W_{NS R}^{m r}: rows W^{m}, W^{2m}, W^{4m}, W^{8m} are loaded, the other powers are
-// products w_r = w_{r - lowbit(r)} * w_{lowbit(r)} (at most 3 products deep); a quarter to a half
-// of the twiddle loads, which were most of the L1 traffic.
+// v[r] *= W_{NS R}^{m r}: rows W^{m}, W^{2m}, W^{4m}, W^{8m}, W^{16m} are loaded, the other powers
+// are products w_r = w_{r - lowbit(r)} * w_{lowbit(r)} (at most 4 products deep); a quarter to a
+// half of the twiddle loads, which were most of the L1 traffic.
 template <typename T, int R, int NS, int TWO>
 __device__ __forceinline__ void apply_twiddles(typename Cx<T>::C (&v)[R], const typename Cx<T>::C *tw, int m) {
 	using C = typename Cx<T>::C;
@@ -402,7 +461,7 @@ __device__ __forceinline__ void apply_twiddles(typename Cx<T>::C (&v)[R], const 
 #pragma unroll
 	for (int r = 1; r < R; ++r) {
 		const int lb = r & -r;
-		const int b = lb == 1 ? 0 : lb == 2 ? 1 : lb == 4 ? 2 : 3;
+		const int b = lb == 1 ? 0 : lb == 2 ? 1 : lb == 4 ? 2 : lb == 8 ? 3 : 4;
 		w[r] = r == lb ? pw[b] : mul(w[r - lb], pw[b]);
 		v[r] = mul(v[r], w[r]);
 	}

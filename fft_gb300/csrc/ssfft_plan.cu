@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <functional>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -106,7 +107,45 @@ void unit_root(unsigned long long k, unsigned long long L, double *re, double *i
 
 static bool specialised(int r) {
 	return r == 1 || r == 2 || r == 3 || r == 4 || r == 5 || r == 6 || r == 8 || r == 9 || r == 10 || r == 12 ||
-	       r == 15 || r == 16;
+	       r == 15 || r == 16 || r == 18 || r == 20 || r == 24 || r == 25;
+}
+
+// Fewest passes for 2^a 3^b 5^c over the register radices including the large composites
+// 18, 20, 24, 25 (which hold up to 25 values a thread); ties prefer fewer large composites.
+// Order: powers of two first (largest first), then the others (largest first).
+static bool fewest_passes(int a, int b, int c, std::vector<int> &out) {
+	struct Rd { int r, x, y, z; };
+	static const Rd kR[] = {{2, 1, 0, 0},  {3, 0, 1, 0},  {4, 2, 0, 0},  {5, 0, 0, 1},  {6, 1, 1, 0},
+	                        {8, 3, 0, 0},  {9, 0, 2, 0},  {10, 1, 0, 1}, {12, 2, 1, 0}, {15, 0, 1, 1},
+	                        {16, 4, 0, 0}, {18, 1, 2, 0}, {20, 2, 0, 1}, {24, 3, 1, 0}, {25, 0, 0, 2}};
+	if (a > 40 || b > 25 || c > 20) return false;
+	const int A = a + 1, B = b + 1, Cc = c + 1;
+	std::vector<int> cost((size_t)A * B * Cc, 1 << 29), pick((size_t)A * B * Cc, -1);
+	auto at = [&](int x, int y, int z) { return ((size_t)x * B + y) * Cc + z; };
+	cost[at(0, 0, 0)] = 0;
+	for (int x = 0; x <= a; ++x)
+		for (int y = 0; y <= b; ++y)
+			for (int z = 0; z <= c; ++z) {
+				if (!x && !y && !z) continue;
+				for (int i = 0; i < (int)(sizeof kR / sizeof kR[0]); ++i) {
+					const Rd &d = kR[i];
+					if (d.x > x || d.y > y || d.z > z) continue;
+					const int cst = cost[at(x - d.x, y - d.y, z - d.z)] + 1000 + (d.r > 16 ? 1 : 0);
+					if (cst < cost[at(x, y, z)]) cost[at(x, y, z)] = cst, pick[at(x, y, z)] = i;
+				}
+			}
+	if (pick[at(a, b, c)] < 0 && (a || b || c)) return false;
+	std::vector<int> p2, rest;
+	for (int x = a, y = b, z = c; x || y || z;) {
+		const Rd &d = kR[pick[at(x, y, z)]];
+		((d.y == 0 && d.z == 0) ? p2 : rest).push_back(d.r);
+		x -= d.x, y -= d.y, z -= d.z;
+	}
+	std::sort(p2.begin(), p2.end(), std::greater<int>());
+	std::sort(rest.begin(), rest.end(), std::greater<int>());
+	out = p2;
+	out.insert(out.end(), rest.begin(), rest.end());
+	return true;
 }
 
 // Radices for n = 2^a 3^b 5^c * rest: 3 x 5 pairs become radix-15 prime-factor butterflies;
@@ -138,7 +177,7 @@ static void radices_for(int a, int b, int c, const std::vector<int> &rest, bool 
 	out.insert(out.end(), rest.begin(), rest.end());
 }
 
-bool choose_radices(int n, std::vector<int> &radices) {
+bool choose_radices(int n, std::vector<int> &radices, bool large_composites) {
 	radices.clear();
 	if (n < 1) return false;
 	if (n == 1) {
@@ -162,10 +201,13 @@ bool choose_radices(int n, std::vector<int> &radices) {
 			p += 2;
 		}
 	}
-	std::vector<int> plain, borrowed;
+	std::vector<int> plain, borrowed, fewest;
 	radices_for(a, b, c, rest, false, plain);
 	radices_for(a, b, c, rest, true, borrowed);
 	radices = borrowed.size() < plain.size() ? borrowed : plain;
+	// the large composites only where they save a pass (more values a thread otherwise)
+	if (large_composites && rest.empty() && fewest_passes(a, b, c, fewest) && fewest.size() < radices.size())
+		radices = fewest;
 	return radices.size() <= 24;
 }
 
@@ -235,7 +277,8 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 		}
 		if (prod != n || knobs->radices.size() > 24) return false;
 		s.radices = knobs->radices;
-	} else if (!choose_radices(n, s.radices)) {
+	} else if (!choose_radices(n, s.radices, !(knobs && knobs->precision == 1))) {
+		// (the tensor-core pass needs a first radix <= 16: no large composites there)
 		return false;
 	}
 	// split-BF16 tensor-core first pass: complex FP32, first radix <= 16 (moved to the front)

@@ -30,6 +30,9 @@ CASES = [
     (1920, "f32", "real", 3, 3), (1000, "f64", "real", 2, 2), (64, "f32", "real", 50, 50), (30, "f64", "real", 3, 3),
     (96, "f64", "real", 4, 4), (100, "f32", "real", 7, 7), (8192, "f32", "real", 1, 1), (36, "f32", "real", 9, 9),
     (18, "f64", "real", 2, 2), (12, "f32", "real", 3, 3),
+    # large composite radices 18, 20, 24, 25 (where they save a pass)
+    (480, "f32", "complex", 3, 3), (15625, "f32", "complex", 1, 1), (11250, "f32", "complex", 1, 1), (7500, "f64", "complex", 1, 1),
+    (13824, "f32", "complex", 1, 1), (960, "f64", "real", 2, 2),
     (2, "f64", "real_halfshift", 1, 1), (4, "f64", "real_halfshift", 2, 2), (9, "f64", "real_halfshift", 1, 1),
     (12, "f32", "real_halfshift", 2, 2), (98, "f64", "real_halfshift", 1, 1), (960, "f32", "real_halfshift", 2, 2),
 ]
