@@ -149,7 +149,10 @@ static ssfft_status large_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind,
 		if (!make_schedule(dtype, (int)Fi, 0, false, 1, s, false)) return SSFFT_ERR_UNSUPPORTED;
 		// G sub-transforms per CTA: 128-256 B segments, <= 1024 threads, <= ~100 KiB smem
 		const long long U0 = last ? F[0] : R;
-		int G = (int)std::min<long long>(kGroup, U0);
+		// SSFFT_LARGE_GROUP overrides the group size (experiments; read when the plan is made)
+		const char *ge = std::getenv("SSFFT_LARGE_GROUP");
+		const int group = ge && std::atoi(ge) > 0 ? std::min(64, std::atoi(ge)) : kGroup;
+		int G = (int)std::min<long long>(group, U0);
 		while (G > 1 && (G * s.threads > kMaxCtaThreads || (size_t)G * s.smem_stride * eb > 100 * 1024)) --G;
 		s.per_cta = G;
 		s.smem_bytes = (size_t)G * s.smem_stride * eb;
