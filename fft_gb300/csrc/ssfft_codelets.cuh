@@ -1433,6 +1433,26 @@ __global__ void __launch_bounds__(THREADS *G) strided(const StridedArgs a) {
 	c.gin = reinterpret_cast<const T *>(in + (c.valid ? ib + (u00 + g) * a.is0 : 0));
 	c.gout = reinterpret_cast<T *>(out + (c.valid ? ob + (u00 + g) * a.os0 : 0));
 	c.rot = reinterpret_cast<const C *>(a.rot);
+	// Inter-pass twiddles W^{u0 k} for this CTA's G sub-transforms, k = kh KL + kl:
+	// W^{u0 KL kh} and W^{u0 kl} (KH + KL values per sub-transform, from the two-level table)
+	// in shared memory after the transforms' slots; the store then needs two shared loads and one
+	// product per element instead of two scattered global loads.
+	constexpr int KL = 16, KH = (N + KL - 1) / KL;
+	C *twk = sm_all + G * STRIDE;
+	if constexpr (SSTORE && TWN > 1) {
+		const C *twlo = reinterpret_cast<const C *>(a.twlo);
+		const C *twhi = reinterpret_cast<const C *>(a.twhi);
+		for (int idx = threadIdx.x; idx < G * (KH + KL); idx += CTA) {
+			const int gg = idx / (KH + KL), q = idx - gg * (KH + KL);
+			const long long u0 = u00 + gg;
+			if (u0 < a.U0) {
+				const unsigned long long e = q < KH ? (unsigned long long)q * KL : (unsigned long long)(q - KH);
+				const unsigned long long t = ((unsigned long long)u0 * e) % (unsigned long long)TWN;
+				twk[idx] = mul(__ldg(twhi + (t >> LB)), __ldg(twlo + (t & ((1ull << LB) - 1))));
+			}
+		}
+		// (read after the passes' barriers)
+	}
 	if (a.pf_dist > 0 && (long long)blockIdx.x + a.pf_dist < (long long)gridDim.x) {
 		// the input the CTA pf_dist blocks ahead will read, one 128-byte line per prefetch
 		long long pc = (long long)blockIdx.x + a.pf_dist;
@@ -1474,8 +1494,6 @@ __global__ void __launch_bounds__(THREADS *G) strided(const StridedArgs a) {
 	passes<T, N, THREADS, 1, 0, 0, SLOAD ? kSmem : kGlobal, SSTORE ? kSmem : kGlobal, kComplex, CIN, COUT, false, EMAX,
 	       Rs...>(c, reinterpret_cast<const C *>(a.tw), reinterpret_cast<const C *>(a.roots));
 	if constexpr (SSTORE) {
-		const C *twlo = reinterpret_cast<const C *>(a.twlo);
-		const C *twhi = reinterpret_cast<const C *>(a.twhi);
 #pragma unroll 4
 		for (int idx = threadIdx.x; idx < G * N; idx += CTA) {
 			const int gg = idx % G, k = idx / G;
@@ -1483,8 +1501,8 @@ __global__ void __launch_bounds__(THREADS *G) strided(const StridedArgs a) {
 			if (u0 < a.U0) {
 				C v = sm_all[gg * STRIDE + pidx<PS>(k)];
 				if constexpr (TWN > 1) {
-					const unsigned long long t = ((unsigned long long)u0 * (unsigned long long)k) % (unsigned long long)TWN;
-					v = mul(v, mul(__ldg(twhi + (t >> LB)), __ldg(twlo + (t & ((1ull << LB) - 1)))));
+					const int kh = k / KL, kl = k - kh * KL;
+					v = mul(v, mul(twk[gg * (KH + KL) + kh], twk[gg * (KH + KL) + KH + kl]));
 				}
 				const long long off = ob + u0 * a.os0 + (long long)k * a.out_es;
 				if constexpr (ROT == 2) {
