@@ -1437,7 +1437,9 @@ __global__ void __launch_bounds__(THREADS *G) strided(const StridedArgs a) {
 	// W^{u0 KL kh} and W^{u0 kl} (KH + KL values per sub-transform, from the two-level table)
 	// in shared memory after the transforms' slots; the store then needs two shared loads and one
 	// product per element instead of two scattered global loads.
-	constexpr int KL = 16, KH = (N + KL - 1) / KL;
+	// rows of TWS = (KH + KL) | 1 slots: an odd stride, so the G sub-transforms of one k (adjacent
+	// threads in the store loop) read different banks
+	constexpr int KL = 16, KH = (N + KL - 1) / KL, TWS = (KH + KL) | 1;
 	C *twk = sm_all + G * STRIDE;
 	if constexpr (SSTORE && TWN > 1) {
 		const C *twlo = reinterpret_cast<const C *>(a.twlo);
@@ -1448,7 +1450,7 @@ __global__ void __launch_bounds__(THREADS *G) strided(const StridedArgs a) {
 			if (u0 < a.U0) {
 				const unsigned long long e = q < KH ? (unsigned long long)q * KL : (unsigned long long)(q - KH);
 				const unsigned long long t = ((unsigned long long)u0 * e) % (unsigned long long)TWN;
-				twk[idx] = mul(__ldg(twhi + (t >> LB)), __ldg(twlo + (t & ((1ull << LB) - 1))));
+				twk[gg * TWS + q] = mul(__ldg(twhi + (t >> LB)), __ldg(twlo + (t & ((1ull << LB) - 1))));
 			}
 		}
 		// (read after the passes' barriers)
@@ -1502,7 +1504,7 @@ __global__ void __launch_bounds__(THREADS *G) strided(const StridedArgs a) {
 				C v = sm_all[gg * STRIDE + pidx<PS>(k)];
 				if constexpr (TWN > 1) {
 					const int kh = k / KL, kl = k - kh * KL;
-					v = mul(v, mul(twk[gg * (KH + KL) + kh], twk[gg * (KH + KL) + KH + kl]));
+					v = mul(v, mul(twk[gg * TWS + kh], twk[gg * TWS + KH + kl]));
 				}
 				const long long off = ob + u0 * a.os0 + (long long)k * a.out_es;
 				if constexpr (ROT == 2) {

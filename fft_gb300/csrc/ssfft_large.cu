@@ -156,7 +156,7 @@ static ssfft_status large_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind,
 		while (G > 1 && (G * s.threads > kMaxCtaThreads || (size_t)G * s.smem_stride * eb > 100 * 1024)) --G;
 		s.per_cta = G;
 		// + the CTA's inter-pass twiddles (G x (KH + KL) values, KL = 16) for passes that have them
-		const size_t twk = (i < P - 1) ? (size_t)G * ((Fi + 15) / 16 + 16) * eb : 0;
+		const size_t twk = (i < P - 1) ? (size_t)G * (((Fi + 15) / 16 + 16) | 1) * eb : 0;
 		s.smem_bytes = (size_t)G * s.smem_stride * eb + twk;
 		if (s.smem_bytes > smem_limit) return SSFFT_ERR_UNSUPPORTED;
 		ps.sub = s;
