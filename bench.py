@@ -442,8 +442,17 @@ def run_fp64(args):
         yy = oracle.batch(x, n, real=False, inverse=False, threads=threads)
         oracle.batch(yy, n, real=False, inverse=True, threads=threads)
     tc = (time.perf_counter() - t0) / reps
+    # FP64 roofline: this batch (4 MiB each way) sits in L2 and is bound by FP64 arithmetic, so
+    # the reference rate is a measured FP64 GEMM (cuBLAS DGEMM 4096^3, best of 3)
+    a64 = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    b64 = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    dg = min(_time_device(lambda: torch.matmul(a64, b64), 1, 1) for _ in range(3))
+    fp64_peak = 2 * 4096 ** 3 / dg / 1e12
     print(json.dumps({"workload": "FFT<double> N=1024 x256, fwd+inv", "value": flops / t / 1e9, "unit": "GFLOP/s",
                       "ms_per_step": t * 1e3, "GB_s": 2 * 2 * b * n * 16 / t / 1e9, "relL2_vs_oracle": rel,
+                      "fp64_roofline": {"measured_dgemm_TFLOP_s": fp64_peak,
+                                        "frac": flops / t / 1e12 / fp64_peak,
+                                        "note": "5N log2 N flops per transform against cuBLAS DGEMM throughput"},
                       "cpu_baseline": {"value": flops / tc / 1e9, "unit": "GFLOP/s", "cores": threads, "kind": "port"},
                       "plan": p.describe()}), flush=True)
 
