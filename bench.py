@@ -52,7 +52,7 @@ def parse():
                     choices=["realfft", "fp64", "large", "serve", "uneven", "precision"],
                     help="realfft: the batched RealFFT<float> line (default); fp64: FFT<double> N=1024 x256; "
                          "large: single FP32 transforms of 2^24, 3^15, 2^12 3^4 5^2; serve: request serving sweep")
-    ap.add_argument("--serve-duration", type=float, default=1.0)
+    ap.add_argument("--serve-duration", type=float, default=3.0)
     ap.add_argument("--tune", type=int, default=2, choices=[0, 1, 2],
                     help="autotune level of the plans (0 planner defaults, 1 CTA shape, 2 also radix order)")
     ap.add_argument("--streams", type=int, default=4,
