@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <thread>
@@ -30,7 +31,7 @@ ssfft_status plan_prepare_launch(const Plan *p);
 
 namespace {
 
-constexpr int kBranches = 8;
+constexpr int kMaxBranches = 32;
 
 struct Group {
 	size_t n = 0, count = 0;
@@ -55,8 +56,9 @@ struct MultiPlan {
 	size_t total = 0;
 	std::vector<Group> groups;
 	cudaStream_t cap = nullptr;
-	cudaStream_t branch[kBranches] = {};
-	cudaEvent_t fork = nullptr, join[kBranches] = {};
+	int branches = 8;  // parallel graph branches (SSFFT_MULTI_BRANCHES overrides, up to 32)
+	cudaStream_t branch[kMaxBranches] = {};
+	cudaEvent_t fork = nullptr, join[kMaxBranches] = {};
 	std::mutex mu;
 	std::map<GraphKey, cudaGraphExec_t> graphs;
 
@@ -66,7 +68,7 @@ struct MultiPlan {
 			if (g.d_offs) cudaFree(g.d_offs);
 			if (g.plan) ssfft_plan_destroy(g.plan);
 		}
-		for (int b = 0; b < kBranches; ++b) {
+		for (int b = 0; b < kMaxBranches; ++b) {
 			if (join[b]) cudaEventDestroy(join[b]);
 			if (branch[b]) cudaStreamDestroy(branch[b]);
 		}
@@ -88,9 +90,9 @@ struct MultiPlan {
 		if (e != cudaSuccess) return cuda_fail(e, "cudaStreamBeginCapture");
 		ssfft_status st = SSFFT_SUCCESS;
 		e = cudaEventRecord(fork, cap);
-		for (int b = 0; b < kBranches && e == cudaSuccess; ++b) e = cudaStreamWaitEvent(branch[b], fork, 0);
+		for (int b = 0; b < branches && e == cudaSuccess; ++b) e = cudaStreamWaitEvent(branch[b], fork, 0);
 		if (e == cudaSuccess) st = launch_all(k.inverse, k.in, k.out, branch);
-		for (int b = 0; b < kBranches && e == cudaSuccess; ++b) {
+		for (int b = 0; b < branches && e == cudaSuccess; ++b) {
 			e = cudaEventRecord(join[b], branch[b]);
 			if (e == cudaSuccess) e = cudaStreamWaitEvent(cap, join[b], 0);
 		}
@@ -181,10 +183,15 @@ ssfft_status ssfft_multi_create_ex(ssfft_multi_t *out, const size_t *sizes, size
 	std::vector<size_t> order(m->groups.size());
 	for (size_t i = 0; i < order.size(); ++i) order[i] = i;
 	std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return m->groups[a].work > m->groups[b].work; });
-	double load[kBranches] = {};
+	{
+		const char *env = std::getenv("SSFFT_MULTI_BRANCHES");
+		if (env && std::atoi(env) > 0) m->branches = std::min(kMaxBranches, std::atoi(env));
+	}
+	const int nb = m->branches;
+	double load[kMaxBranches] = {};
 	for (size_t i : order) {
 		int best = 0;
-		for (int b = 1; b < kBranches; ++b)
+		for (int b = 1; b < nb; ++b)
 			if (load[b] < load[best]) best = b;
 		m->groups[i].branch = best;
 		load[best] += m->groups[i].work;
@@ -194,7 +201,7 @@ ssfft_status ssfft_multi_create_ex(ssfft_multi_t *out, const size_t *sizes, size
 	m->groups.swap(sorted);
 	e = cudaStreamCreateWithFlags(&m->cap, cudaStreamNonBlocking);
 	if (e == cudaSuccess) e = cudaEventCreateWithFlags(&m->fork, cudaEventDisableTiming);
-	for (int b = 0; b < kBranches && e == cudaSuccess; ++b) {
+	for (int b = 0; b < nb && e == cudaSuccess; ++b) {
 		e = cudaStreamCreateWithFlags(&m->branch[b], cudaStreamNonBlocking);
 		if (e == cudaSuccess) e = cudaEventCreateWithFlags(&m->join[b], cudaEventDisableTiming);
 	}
@@ -229,8 +236,8 @@ ssfft_status ssfft_multi_exec(ssfft_multi_t multi, int inverse, const void *d_in
 ssfft_status ssfft_multi_exec_plain(ssfft_multi_t multi, int inverse, const void *d_in, void *d_out, void *stream) {
 	if (!multi || !d_in || !d_out) return SSFFT_ERR_INVALID_VALUE;
 	MultiPlan *m = reinterpret_cast<MultiPlan *>(multi);
-	cudaStream_t s[kBranches];
-	for (int b = 0; b < kBranches; ++b) s[b] = static_cast<cudaStream_t>(stream);
+	cudaStream_t s[kMaxBranches];
+	for (int b = 0; b < kMaxBranches; ++b) s[b] = static_cast<cudaStream_t>(stream);
 	return m->launch_all(inverse ? 1 : 0, d_in, d_out, s);
 }
 
