@@ -368,11 +368,16 @@ __device__ __forceinline__ typename Cx<T>::C sload(const Ctx<T, KIND, CIN, COUT>
 	}
 }
 
-// L2 prefetch of one line (a hint: no data returns, nothing waits on it).
+// L2 prefetch of one line, or (bulk) of a 16-byte aligned range whose size is a multiple of 16
+// bytes by the copy engine of the SM (hints: no data returns, nothing waits on them).
 #if defined(__CUDA_ARCH__)
 __device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+__device__ __forceinline__ void prefetch_l2_bulk(const void *p, unsigned bytes) {
+	asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
 #else
 inline void prefetch_l2(const void *) {}
+inline void prefetch_l2_bulk(const void *, unsigned) {}
 #endif
 
 // The input of the CTA pf_dist blocks ahead (transforms stored back to back), one 128-byte
@@ -389,8 +394,13 @@ __device__ __forceinline__ void prefetch_ahead(const Args &a) {
 	if (!a.offs) {
 		const unsigned char *base = in + first * per;
 		const long long bytes = cnt * per;
-		for (long long off = (long long)threadIdx.x * 128; off < bytes; off += (long long)CTA_THREADS * 128)
-			prefetch_l2(base + off);
+		if ((((unsigned long long)base | (unsigned long long)bytes) & 15) == 0 && bytes < (1ll << 31)) {
+			// one bulk prefetch for the whole range (TMA), issued by one thread
+			if (threadIdx.x == 0) prefetch_l2_bulk(base, (unsigned)bytes);
+		} else {
+			for (long long off = (long long)threadIdx.x * 128; off < bytes; off += (long long)CTA_THREADS * 128)
+				prefetch_l2(base + off);
+		}
 	} else {
 		// scattered transforms (offset table): line k of transform g = k / lines
 		const long long lines = (per + 127) / 128;
