@@ -290,6 +290,11 @@ struct SmallDft<9> {
 	template <class C>
 	__device__ __forceinline__ static void run(C *v) { dft9(v); }
 };
+template <>
+struct SmallDft<16> {
+	template <class C>
+	__device__ __forceinline__ static void run(C *v) { dft16(v); }
+};
 
 template <int A, int B, int KA, int KB, class C>
 __device__ __forceinline__ void dft_pfa(C *v) {
@@ -312,11 +317,72 @@ __device__ __forceinline__ void dft_pfa(C *v) {
 	}
 }
 
+// Cooley-Tukey composites R = A * B (A-point DFTs over n1 of x[B n1 + n2], twiddles
+// W_R^{n2 k1} from the table w, B-point DFTs over n2, transpose to k = k1 + A k2).
+template <int A, int B, int E, class C>
+__device__ __forceinline__ void dft_ct(C *v, const C (&w)[E]) {
+	constexpr int R = A * B;
+#pragma unroll
+	for (int n2 = 0; n2 < B; ++n2) {
+		C u[A];
+#pragma unroll
+		for (int n1 = 0; n1 < A; ++n1) u[n1] = v[B * n1 + n2];
+		SmallDft<A>::run(u);
+#pragma unroll
+		for (int k1 = 0; k1 < A; ++k1) v[B * k1 + n2] = (n2 && k1) ? mul(u[k1], w[n2 * k1]) : u[k1];
+	}
+#pragma unroll
+	for (int k1 = 0; k1 < A; ++k1) SmallDft<B>::run(v + B * k1);
+	C t[R];
+#pragma unroll
+	for (int k1 = 0; k1 < A; ++k1)
+#pragma unroll
+		for (int k2 = 0; k2 < B; ++k2) t[k1 + A * k2] = v[B * k1 + k2];
+#pragma unroll
+	for (int k = 0; k < R; ++k) v[k] = t[k];
+}
+
+// 27 = 3 x 9 and 32 = 4 x 8; w[e] = W_R^e = cos(2 pi e/R) - i sin(2 pi e/R)
+template <class C>
+__device__ __forceinline__ void dft27(C *v) {
+	using S = decltype(v[0].x);
+	const C w[17] = {
+	    mkc(S(1.0), S(-0.0)), mkc(S(0.9730448705798238), S(-0.23061587074244017)),
+	    mkc(S(0.8936326403234123), S(-0.44879918020046217)), mkc(S(0.766044443118978), S(-0.6427876096865393)),
+	    mkc(S(0.5971585917027862), S(-0.8021231927550437)), mkc(S(0.3960797660391569), S(-0.918216106880274)),
+	    mkc(S(0.17364817766693041), S(-0.984807753012208)), mkc(S(-0.058144828910475774), S(-0.9983081582712682)),
+	    mkc(S(-0.2868032327110902), S(-0.9579895123154889)), mkc(S(-0.4999999999999998), S(-0.8660254037844387)),
+	    mkc(S(-0.6862416378687335), S(-0.7273736415730488)), mkc(S(-0.8354878114129363), S(-0.5495089780708062)),
+	    mkc(S(-0.9396926207859083), S(-0.3420201433256689)), mkc(S(-0.993238357741943), S(-0.11609291412522993)),
+	    mkc(S(-0.993238357741943), S(0.11609291412523012)), mkc(S(-0.9396926207859085), S(0.3420201433256682)),
+	    mkc(S(-0.8354878114129365), S(0.549508978070806)),
+	};
+	dft_ct<3, 9>(v, w);
+}
+template <class C>
+__device__ __forceinline__ void dft32(C *v) {
+	using S = decltype(v[0].x);
+	const C w[22] = {
+	    mkc(S(1.0), S(-0.0)), mkc(S(0.9807852804032304), S(-0.19509032201612825)),
+	    mkc(S(0.9238795325112867), S(-0.3826834323650898)), mkc(S(0.8314696123025452), S(-0.5555702330196022)),
+	    mkc(S(0.7071067811865476), S(-0.7071067811865475)), mkc(S(0.5555702330196023), S(-0.8314696123025452)),
+	    mkc(S(0.38268343236508984), S(-0.9238795325112867)), mkc(S(0.19509032201612833), S(-0.9807852804032304)),
+	    mkc(S(0.0), S(-1.0)), mkc(S(-0.1950903220161282), S(-0.9807852804032304)),
+	    mkc(S(-0.3826834323650897), S(-0.9238795325112867)), mkc(S(-0.555570233019602), S(-0.8314696123025455)),
+	    mkc(S(-0.7071067811865475), S(-0.7071067811865476)), mkc(S(-0.8314696123025453), S(-0.5555702330196022)),
+	    mkc(S(-0.9238795325112867), S(-0.3826834323650899)), mkc(S(-0.9807852804032304), S(-0.1950903220161286)),
+	    mkc(S(-1.0), S(-0.0)), mkc(S(-0.9807852804032304), S(0.19509032201612836)),
+	    mkc(S(-0.9238795325112868), S(0.38268343236508967)), mkc(S(-0.8314696123025455), S(0.555570233019602)),
+	    mkc(S(-0.7071067811865477), S(0.7071067811865475)), mkc(S(-0.5555702330196022), S(0.8314696123025452)),
+	};
+	dft_ct<4, 8>(v, w);
+}
+
 template <int R>
 struct Specialised {
 	static constexpr bool value = R == 1 || R == 2 || R == 3 || R == 4 || R == 5 || R == 6 || R == 8 || R == 9 ||
 	                              R == 10 || R == 12 || R == 15 || R == 16 || R == 18 || R == 20 || R == 24 ||
-	                              R == 25;
+	                              R == 25 || R == 27 || R == 32 || R == 36 || R == 40 || R == 45;
 };
 
 template <int R, class C>
@@ -336,6 +402,11 @@ __device__ __forceinline__ void dft(C *v) {
 	else if constexpr (R == 20) dft_pfa<4, 5, 5, 16>(v);    // 5 (5^-1 mod 4 = 1), 4 (4^-1 mod 5 = 4)
 	else if constexpr (R == 24) dft_pfa<8, 3, 9, 16>(v);    // 3 (3^-1 mod 8 = 3), 8 (8^-1 mod 3 = 2)
 	else if constexpr (R == 25) dft25(v);
+	else if constexpr (R == 27) dft27(v);
+	else if constexpr (R == 32) dft32(v);
+	else if constexpr (R == 36) dft_pfa<4, 9, 9, 28>(v);    // 9 (9^-1 mod 4 = 1), 4 (4^-1 mod 9 = 7)
+	else if constexpr (R == 40) dft_pfa<8, 5, 25, 16>(v);   // 5 (5^-1 mod 8 = 5), 8 (8^-1 mod 5 = 2)
+	else if constexpr (R == 45) dft_pfa<9, 5, 10, 36>(v);   // 5 (5^-1 mod 9 = 2), 9 (9^-1 mod 5 = 4)
 }
 
 // ------------------------------------------------------------------ per-thread context
@@ -455,7 +526,7 @@ __device__ __forceinline__ void gstore(const Ctx<T, KIND, CIN, COUT> &c, int e, 
 template <int R>
 struct TwRows {
 	static constexpr int value =
-	    Specialised<R>::value ? (R > 16 ? 5 : R > 8 ? 4 : R > 4 ? 3 : R > 2 ? 2 : 1) : R - 1;
+	    Specialised<R>::value ? (R > 32 ? 6 : R > 16 ? 5 : R > 8 ? 4 : R > 4 ? 3 : R > 2 ? 2 : 1) : R - 1;
 };
 
 // v[r] *= W_{NS R}^{m r}: rows W^{m}, W^{2m}, W^{4m}, W^{8m}, W^{16m} are loaded, the other powers
@@ -471,7 +542,7 @@ __device__ __forceinline__ void apply_twiddles(typename Cx<T>::C (&v)[R], const 
 #pragma unroll
 	for (int r = 1; r < R; ++r) {
 		const int lb = r & -r;
-		const int b = lb == 1 ? 0 : lb == 2 ? 1 : lb == 4 ? 2 : lb == 8 ? 3 : 4;
+		const int b = lb == 1 ? 0 : lb == 2 ? 1 : lb == 4 ? 2 : lb == 8 ? 3 : lb == 16 ? 4 : 5;
 		w[r] = r == lb ? pw[b] : mul(w[r - lb], pw[b]);
 		v[r] = mul(v[r], w[r]);
 	}

@@ -107,17 +107,20 @@ void unit_root(unsigned long long k, unsigned long long L, double *re, double *i
 
 static bool specialised(int r) {
 	return r == 1 || r == 2 || r == 3 || r == 4 || r == 5 || r == 6 || r == 8 || r == 9 || r == 10 || r == 12 ||
-	       r == 15 || r == 16 || r == 18 || r == 20 || r == 24 || r == 25;
+	       r == 15 || r == 16 || r == 18 || r == 20 || r == 24 || r == 25 || r == 27 || r == 32 || r == 36 ||
+	       r == 40 || r == 45;
 }
 
 // Fewest passes for 2^a 3^b 5^c over the register radices including the large composites
-// 18, 20, 24, 25 (which hold up to 25 values a thread); ties prefer fewer large composites.
+// 18, 20, 24, 25, 27, 32, 36, 40, 45 (which hold up to 45 values a thread); ties prefer
+// fewer and smaller large composites.
 // Order: powers of two first (largest first), then the others (largest first).
-static bool fewest_passes(int a, int b, int c, std::vector<int> &out) {
+static bool fewest_passes(int a, int b, int c, int max_radix, std::vector<int> &out) {
 	struct Rd { int r, x, y, z; };
 	static const Rd kR[] = {{2, 1, 0, 0},  {3, 0, 1, 0},  {4, 2, 0, 0},  {5, 0, 0, 1},  {6, 1, 1, 0},
 	                        {8, 3, 0, 0},  {9, 0, 2, 0},  {10, 1, 0, 1}, {12, 2, 1, 0}, {15, 0, 1, 1},
-	                        {16, 4, 0, 0}, {18, 1, 2, 0}, {20, 2, 0, 1}, {24, 3, 1, 0}, {25, 0, 0, 2}};
+	                        {16, 4, 0, 0}, {18, 1, 2, 0}, {20, 2, 0, 1}, {24, 3, 1, 0}, {25, 0, 0, 2},
+	                        {27, 0, 3, 0}, {32, 5, 0, 0}, {36, 2, 2, 0}, {40, 3, 0, 1}, {45, 0, 2, 1}};
 	if (a > 40 || b > 25 || c > 20) return false;
 	const int A = a + 1, B = b + 1, Cc = c + 1;
 	std::vector<int> cost((size_t)A * B * Cc, 1 << 29), pick((size_t)A * B * Cc, -1);
@@ -129,8 +132,9 @@ static bool fewest_passes(int a, int b, int c, std::vector<int> &out) {
 				if (!x && !y && !z) continue;
 				for (int i = 0; i < (int)(sizeof kR / sizeof kR[0]); ++i) {
 					const Rd &d = kR[i];
-					if (d.x > x || d.y > y || d.z > z) continue;
-					const int cst = cost[at(x - d.x, y - d.y, z - d.z)] + 1000 + (d.r > 16 ? 1 : 0);
+					if (d.x > x || d.y > y || d.z > z || d.r > max_radix) continue;
+					// a pass costs 1000; larger butterflies a little more (registers)
+					const int cst = cost[at(x - d.x, y - d.y, z - d.z)] + 1000 + (d.r > 16 ? 1 : 0) + (d.r > 25 ? 2 : 0);
 					if (cst < cost[at(x, y, z)]) cost[at(x, y, z)] = cst, pick[at(x, y, z)] = i;
 				}
 			}
@@ -205,9 +209,15 @@ bool choose_radices(int n, std::vector<int> &radices, bool large_composites) {
 	radices_for(a, b, c, rest, false, plain);
 	radices_for(a, b, c, rest, true, borrowed);
 	radices = borrowed.size() < plain.size() ? borrowed : plain;
-	// the large composites only where they save a pass (more values a thread otherwise)
-	if (large_composites && rest.empty() && fewest_passes(a, b, c, fewest) && fewest.size() < radices.size())
-		radices = fewest;
+	// The large composites only where they save a pass: for transforms of 4 passes or more (up
+	// to radix 25), and for the long transforms that run one or two CTAs per SM anyway (from 8192
+	// points, up to radix 45).  Measured on GB300: at a few thousand points and below, the
+	// register cost of radix 24+ butterflies outweighs the saved pass.
+	if (large_composites && rest.empty()) {
+		const int max_radix = n >= 8192 ? 45 : radices.size() >= 4 ? 25 : 0;
+		if (max_radix && fewest_passes(a, b, c, max_radix, fewest) && fewest.size() < radices.size())
+			radices = fewest;
+	}
 	return radices.size() <= 24;
 }
 
@@ -316,9 +326,13 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 		s.emax = knobs->emax;
 		t = threads_for(s.emax);
 	} else {
-		s.emax = kElemsPerThread;
+		// 16 values a thread, or 32 when a butterfly holds more than 16 (the smaller radices then
+		// take two butterflies a thread, so the thread count follows the large one) or when 16
+		// would need more than one CTA's threads
+		const int rmax = *std::max_element(s.radices.begin(), s.radices.end());
+		s.emax = rmax > kElemsPerThread ? 2 * kElemsPerThread : kElemsPerThread;
 		t = threads_for(s.emax);
-		if (t > kMaxCtaThreads) {
+		if (t > kMaxCtaThreads && s.emax == kElemsPerThread) {
 			s.emax = 2 * kElemsPerThread;
 			t = threads_for(s.emax);
 		}

@@ -33,6 +33,11 @@ CASES = [
     # large composite radices 18, 20, 24, 25 (where they save a pass)
     (480, "f32", "complex", 3, 3), (15625, "f32", "complex", 1, 1), (11250, "f32", "complex", 1, 1), (7500, "f64", "complex", 1, 1),
     (13824, "f32", "complex", 1, 1), (960, "f64", "real", 2, 2),
+    # radix 27, 32, 36, 40, 45 for long transforms
+    (16384, "f32", "complex", 1, 1), (13500, "f32", "complex", 1, 1), (15552, "f32", "complex", 1, 1),
+    (13122, "f32", "complex", 1, 1), (12800, "f32", "complex", 1, 1), (15000, "f32", "complex", 1, 1),
+    (8100, "f64", "complex", 1, 1), (8748, "f32", "complex", 1, 1), (9720, "f32", "complex", 1, 1),
+    (10240, "f32", "complex", 1, 1), (11664, "f32", "complex", 1, 1),
     (2, "f64", "real_halfshift", 1, 1), (4, "f64", "real_halfshift", 2, 2), (9, "f64", "real_halfshift", 1, 1),
     (12, "f32", "real_halfshift", 2, 2), (98, "f64", "real_halfshift", 1, 1), (960, "f32", "real_halfshift", 2, 2),
 ]
