@@ -181,7 +181,7 @@ static void radices_for(int a, int b, int c, const std::vector<int> &rest, bool 
 	out.insert(out.end(), rest.begin(), rest.end());
 }
 
-bool choose_radices(int n, std::vector<int> &radices, bool large_composites) {
+bool choose_radices(int n, std::vector<int> &radices, bool large_composites, bool real_split) {
 	radices.clear();
 	if (n < 1) return false;
 	if (n == 1) {
@@ -213,9 +213,16 @@ bool choose_radices(int n, std::vector<int> &radices, bool large_composites) {
 	// to radix 25), and for the long transforms that run one or two CTAs per SM anyway (from 8192
 	// points, up to radix 45).  Measured on GB300: at a few thousand points and below, the
 	// register cost of radix 24+ butterflies outweighs the saved pass.
+	// For a RealFFT the split costs one more shared-memory round trip unless the list has a
+	// radix <= 8 to fuse it into (see the fused split passes), so count that too.
+	auto cost = [&](const std::vector<int> &l) {
+		bool fusable = false;
+		for (int r : l) fusable = fusable || (r >= 2 && r <= 8);
+		return (int)l.size() + (real_split && !fusable ? 1 : 0);
+	};
 	if (large_composites && rest.empty()) {
 		const int max_radix = n >= 8192 ? 45 : radices.size() >= 4 ? 25 : 0;
-		if (max_radix && fewest_passes(a, b, c, max_radix, fewest) && fewest.size() < radices.size())
+		if (max_radix && fewest_passes(a, b, c, max_radix, fewest) && cost(fewest) < cost(radices))
 			radices = fewest;
 	}
 	return radices.size() <= 24;
@@ -287,7 +294,7 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 		}
 		if (prod != n || knobs->radices.size() > 24) return false;
 		s.radices = knobs->radices;
-	} else if (!choose_radices(n, s.radices, !(knobs && knobs->precision == 1))) {
+	} else if (!choose_radices(n, s.radices, !(knobs && knobs->precision == 1), kind == 1 && !odd)) {
 		// (the tensor-core pass needs a first radix <= 16: no large composites there)
 		return false;
 	}
