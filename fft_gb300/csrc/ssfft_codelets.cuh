@@ -1125,8 +1125,14 @@ constexpr unsigned kTcAPart = 8192, kTcBPart = 2048;
 __host__ __device__ constexpr unsigned tc_off_a(int per_cta, int stride) {
 	return ((unsigned)per_cta * (unsigned)stride * 8u + 1023u) & ~1023u;
 }
-__host__ __device__ constexpr unsigned tc_smem_bytes(int per_cta, int stride) {
-	return tc_off_a(per_cta, stride) + 3 * kTcAPart + 3 * kTcBPart + 16;
+// With a single 128-row tile per CTA the A parts share the work buffer's space (they are dead
+// once the MMAs complete, before the read-back writes the work buffer); B follows both.
+__host__ __device__ constexpr unsigned tc_off_b(int per_cta, int stride, int tiles) {
+	return tiles == 1 ? (tc_off_a(per_cta, stride) > 3 * kTcAPart ? tc_off_a(per_cta, stride) : 3 * kTcAPart)
+	                  : tc_off_a(per_cta, stride) + 3 * kTcAPart;
+}
+__host__ __device__ constexpr unsigned tc_smem_bytes(int per_cta, int stride, int tiles) {
+	return tc_off_b(per_cta, stride, tiles) + 3 * kTcBPart + 16;
 }
 __host__ __device__ constexpr unsigned tc_core_off(int row, int k) {
 	return (unsigned)(row >> 3) * kTcSbo + (unsigned)(k >> 3) * kTcLbo + (unsigned)(row & 7) * 16u + (unsigned)(k & 7) * 2u;
@@ -1267,8 +1273,8 @@ __global__ void __launch_bounds__(THREADS *PER_CTA, MINB) batch_tc(const Args a)
 	constexpr int PS = Cx<T>::kPadShift;
 	constexpr bool LAST = sizeof...(Rest) == 0;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	constexpr unsigned OFF_A = tc_off_a(PER_CTA, SMEM_STRIDE);
-	constexpr unsigned OFF_B = OFF_A + 3 * kTcAPart;
+	constexpr unsigned OFF_A = TILES == 1 ? 0 : tc_off_a(PER_CTA, SMEM_STRIDE);
+	constexpr unsigned OFF_B = tc_off_b(PER_CTA, SMEM_STRIDE, TILES);
 	constexpr unsigned OFF_BAR = OFF_B + 3 * kTcBPart;
 	unsigned char *tile_a = smem_raw + OFF_A;
 	unsigned char *tile_b = smem_raw + OFF_B;
@@ -1305,37 +1311,44 @@ __global__ void __launch_bounds__(THREADS *PER_CTA, MINB) batch_tc(const Args a)
 		const bool live = tid < 128 && row < ROWS && gi < a.batch;
 		if (tid < 128) {
 			// this row of the three A parts, packed two BF16 per word: columns 0-15 real parts,
-			// 16-31 imaginary parts (zero beyond R0)
-			unsigned w[3][16];
+			// 16-31 imaginary parts (zero beyond R0, so no stale shared memory meets the zero
+			// rows of B), built in two halves of 8 columns to keep few values live
+			const float2 *src = in + (live ? (a.offs ? a.offs[gi] : gi * a.in_dist) / 2 : 0);
 #pragma unroll
-			for (int q = 0; q < 16; ++q) w[0][q] = w[1][q] = w[2][q] = 0;
-			if (live) {
-				const float2 *src = in + (a.offs ? a.offs[gi] : gi * a.in_dist) / 2;
+			for (int hf = 0; hf < 2; ++hf) {
+				unsigned w[3][2][4];
 #pragma unroll
-				for (int r = 0; r < R0; ++r) {
-					float2 v = __ldcs(src + j + r * NB);
-					if (INV) v.y = -v.y;
-					unsigned short h[2][3];
-					split3(v.x, h[0][0], h[0][1], h[0][2]);
-					split3(v.y, h[1][0], h[1][1], h[1][2]);
+				for (int q = 0; q < 4; ++q) w[0][0][q] = w[0][1][q] = w[1][0][q] = w[1][1][q] = w[2][0][q] = w[2][1][q] = 0;
+				if (live) {
 #pragma unroll
-					for (int part = 0; part < 2; ++part) {
-						const int k = part * 16 + r;
+					for (int rr = 0; rr < 8; ++rr) {
+						const int r = 8 * hf + rr;
+						if (r < R0) {
+							float2 v = __ldcs(src + j + r * NB);
+							if (INV) v.y = -v.y;
+							unsigned short h[2][3];
+							split3(v.x, h[0][0], h[0][1], h[0][2]);
+							split3(v.y, h[1][0], h[1][1], h[1][2]);
 #pragma unroll
-						for (int sp = 0; sp < 3; ++sp) w[sp][k >> 1] |= (unsigned)h[part][sp] << ((k & 1) * 16);
+							for (int part = 0; part < 2; ++part)
+#pragma unroll
+								for (int sp = 0; sp < 3; ++sp) w[sp][part][rr >> 1] |= (unsigned)h[part][sp] << ((rr & 1) * 16);
+						}
 					}
 				}
+#pragma unroll
+				for (int sp = 0; sp < 3; ++sp)
+#pragma unroll
+					for (int part = 0; part < 2; ++part) {
+						// column block (part * 16 + 8 hf) / 8
+						unsigned *dst = reinterpret_cast<unsigned *>(tile_a + sp * kTcAPart +
+						                                             tc_core_off(tid, (2 * part + hf) * 8));
+						dst[0] = w[sp][part][0];
+						dst[1] = w[sp][part][1];
+						dst[2] = w[sp][part][2];
+						dst[3] = w[sp][part][3];
+					}
 			}
-#pragma unroll
-			for (int sp = 0; sp < 3; ++sp)
-#pragma unroll
-				for (int kb = 0; kb < 4; ++kb) {
-					unsigned *dst = reinterpret_cast<unsigned *>(tile_a + sp * kTcAPart + tc_core_off(tid, kb * 8));
-					dst[0] = w[sp][kb * 4];
-					dst[1] = w[sp][kb * 4 + 1];
-					dst[2] = w[sp][kb * 4 + 2];
-					dst[3] = w[sp][kb * 4 + 3];
-				}
 		}
 		fence_async_smem();
 		tc_fence_before();

@@ -372,7 +372,10 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	s.smem_bytes = (size_t)s.per_cta * per;
 	// a single-pass complex transform never touches shared memory
 	if (kind == 0 && s.radices.size() == 1) s.smem_bytes = 0;
-	if (s.tc) s.smem_bytes = ssfft_cl::tc_smem_bytes(s.per_cta, s.smem_stride);
+	if (s.tc) {
+		const int rows = s.per_cta * (n / s.radices[0]);
+		s.smem_bytes = ssfft_cl::tc_smem_bytes(s.per_cta, s.smem_stride, (rows + 127) / 128);
+	}
 	// Staged input (bulk copies into shared memory, persistent CTAs) when one transform's input is
 	// a whole number of 16-byte units and a group of them fits the copy and shared-memory limits.
 	const size_t sb = eb / 2;
