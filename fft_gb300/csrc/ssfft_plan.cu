@@ -111,6 +111,17 @@ static bool specialised(int r) {
 	       r == 40 || r == 45;
 }
 
+// Largest radix whose mirror-paired pass (2R values a thread) carries the fused RealFFT split:
+// 8 (SSFFT_FUSE_RADIX overrides for experiments, read once).
+static int fuse_radix_limit() {
+	static const int v = [] {
+		const char *e = std::getenv("SSFFT_FUSE_RADIX");
+		const int x = e ? std::atoi(e) : 0;
+		return x >= 2 && x <= 16 ? x : 8;
+	}();
+	return v;
+}
+
 // Fewest passes for 2^a 3^b 5^c over the register radices including the large composites
 // 18, 20, 24, 25, 27, 32, 36, 40, 45 (which hold up to 45 values a thread); ties prefer
 // fewer and smaller large composites.
@@ -217,7 +228,7 @@ bool choose_radices(int n, std::vector<int> &radices, bool large_composites, boo
 	// radix <= 8 to fuse it into (see the fused split passes), so count that too.
 	auto cost = [&](const std::vector<int> &l) {
 		bool fusable = false;
-		for (int r : l) fusable = fusable || (r >= 2 && r <= 8);
+		for (int r : l) fusable = fusable || (r >= 2 && r <= fuse_radix_limit());
 		return (int)l.size() + (real_split && !fusable ? 1 : 0);
 	};
 	if (large_composites && rest.empty()) {
@@ -496,7 +507,7 @@ bool single_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch,
 	int best = -1;
 	for (size_t i = 0; i < s.radices.size(); ++i) {
 		const int r = s.radices[i];
-		if (specialised(r) && r >= 2 && r <= 8 && (best < 0 || r < s.radices[best])) best = (int)i;
+		if (specialised(r) && r >= 2 && r <= fuse_radix_limit() && (best < 0 || r < s.radices[best])) best = (int)i;
 	}
 	if (best < 0) return true;
 	std::vector<int> rot = s.radices;
