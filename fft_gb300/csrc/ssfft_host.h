@@ -121,7 +121,7 @@ bool single_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch,
                      const Knobs *knobs = nullptr, int allow_staged = 1, int dir = -1);
 void single_tables(const Schedule &s, size_t n_real, std::vector<double> &tw, std::vector<double> &roots,
                    std::vector<double> &rtw, std::vector<double> &rot);
-void radix_candidates(int n, std::vector<std::vector<int>> &out);
+void radix_candidates(int n, std::vector<std::vector<int>> &out, bool real_split = false);
 void tc_matrix(int r0, std::vector<float> &bt);
 // autotuner (ssfft_tune.cu): picks knobs for a single-CTA plan, cached per device and shape
 ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log);

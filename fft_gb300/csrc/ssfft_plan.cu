@@ -249,10 +249,10 @@ size_t device_smem_limit(int dev) {
 // Threads per transform, transforms per CTA and shared memory for n points.
 // Distinct radix lists worth timing for n complex points: the planner's choice and its pass
 // orders, and the list without borrowed composite radices and its orders (at most 8 in all).
-void radix_candidates(int n, std::vector<std::vector<int>> &out) {
+void radix_candidates(int n, std::vector<std::vector<int>> &out, bool real_split) {
 	out.clear();
 	std::vector<int> def;
-	if (!choose_radices(n, def)) return;
+	if (!choose_radices(n, def, true, real_split)) return;
 	auto add_orders = [&](std::vector<int> r) {
 		std::vector<int> sorted = r;
 		std::sort(sorted.begin(), sorted.end());
@@ -276,6 +276,22 @@ void radix_candidates(int n, std::vector<std::vector<int>> &out) {
 		radices_for(a, b, c, {}, true, borrowed);
 		if (plain != def && plain.size() <= def.size() + 1) add_orders(plain);
 		if (borrowed != def && borrowed.size() <= def.size() + 1) add_orders(borrowed);
+	}
+	// a RealFFT whose list has no radix <= 8 cannot fuse its split: also try one radix split in
+	// two so that it can (one more pass, one shared-memory round trip less)
+	bool fusable = false;
+	for (int r : def) fusable = fusable || (r >= 2 && r <= fuse_radix_limit());
+	if (real_split && !fusable) {
+		static const int kSplit[][3] = {{16, 4, 4}, {16, 8, 2}, {15, 3, 5}, {12, 4, 3}, {10, 2, 5}, {9, 3, 3}};
+		for (const auto &sp : kSplit) {
+			auto it = std::find(def.begin(), def.end(), sp[0]);
+			if (it == def.end()) continue;
+			std::vector<int> l(def.begin(), it);
+			l.push_back(sp[1]);
+			l.push_back(sp[2]);
+			l.insert(l.end(), it + 1, def.end());
+			if (std::find(out.begin(), out.end(), l) == out.end() && out.size() < 12) out.push_back(l);
+		}
 	}
 }
 

@@ -304,7 +304,7 @@ ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log) 
 
 	if (level >= 2) {
 		std::vector<std::vector<int>> lists;
-		radix_candidates(cn, lists);
+		radix_candidates(cn, lists, p->kind == SSFFT_REAL && !(p->n & 1));
 		std::vector<Candidate> cs;
 		for (auto &l : lists) {
 			Candidate c;
