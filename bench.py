@@ -298,19 +298,21 @@ def run_gpu(args, rank: int, world: int):
     elapsed = max_over_ranks(t0.elapsed_time(t1) / 1e3, dist, "cuda")
     value = flops_per_step(frames) * args.steps * world / elapsed / 1e9
 
-    # per-kernel durations: a sequential pass (one stream, CUDA events around every launch), so
-    # that each kernel is timed alone for the roofline
-    rsteps = max(20, args.steps // 4)
-    evsets = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nl)]
-              for _ in range(rsteps)]
-    for k in range(rsteps):
-        step(evsets[k], ns=1)
-    torch.cuda.synchronize()
+    # per-kernel durations for the roofline: each kernel timed alone on the launching stream,
+    # CUDA events around `reps` back-to-back launches of it (idempotent: same input and output),
+    # mean per launch; each launch streams >= 63 MB, so no launch is served from L2
+    reps = max(10, args.steps // 20)
     kt = np.zeros(nl)
-    for evs in evsets:
-        for j, (a, b) in enumerate(evs):
-            kt[j] += a.elapsed_time(b) / 1e3
-    kt /= rsteps
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for i, (p, x, s, b) in enumerate(zip(plans, xs, specs, backs)):
+        for d, (src, dst) in enumerate(((x, s), (s, b))):
+            p.exec(bool(d), src.data_ptr(), dst.data_ptr(), sh)
+            ev0.record(stream)
+            for _ in range(reps):
+                p.exec(bool(d), src.data_ptr(), dst.data_ptr(), sh)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            kt[2 * i + d] = ev0.elapsed_time(ev1) / 1e3 / reps
     names, alg = [], []
     for n in SIZES:
         for d in ("r2c", "c2r"):
@@ -386,7 +388,7 @@ def run_gpu(args, rank: int, world: int):
             "roofline": {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": peak,
                          "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic_for(names[top]), "alg_bytes_per_launch": alg[top],
-                         "timing": "kernel alone: sequential pass, CUDA events per launch",
+                         "timing": "kernel alone: CUDA events around back-to-back launches of it, mean",
                          "aggregate_GB_s": agg_gbs, "aggregate_frac": agg_gbs / peak},
             "kernels": kernels,
             "e2e": e2e,
