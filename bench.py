@@ -250,26 +250,16 @@ def run_gpu(args, rank: int, world: int):
             print(f"tune N={n}: {line}", file=sys.stderr)
     nl = len(SIZES) * 2
 
-    def step(evs=None, ns=None):
-        ns = nstreams if ns is None else ns
-        k = 0
+    def step():
+        ns = nstreams
         if ns > 1:
             fork_ev.record(stream)
             for st in side[1:ns]:
                 st.wait_event(fork_ev)
         for i, (p, x, s, b) in enumerate(zip(plans, xs, specs, backs)):
-            st = side[i % ns]
-            h = int(st.cuda_stream)
-            if evs is not None:
-                evs[k][0].record(st)
+            h = int(side[i % ns].cuda_stream)
             p.exec(False, x.data_ptr(), s.data_ptr(), h)
-            if evs is not None:
-                evs[k][1].record(st)
-                evs[k + 1][0].record(st)
             p.exec(True, s.data_ptr(), b.data_ptr(), h)
-            if evs is not None:
-                evs[k + 1][1].record(st)
-            k += 2
         if ns > 1:
             for st, ev in zip(side[1:ns], join_ev[1:ns]):
                 ev.record(st)
