@@ -5,7 +5,7 @@
 // plan asks for it, the tuner times candidate schedules on the plan's own batch (zero-filled
 // scratch buffers, CUDA events on a private stream) by coordinate descent:
 //   level 2: radix order (the planner's list, its permutations, the alternative grouping);
-//   level 1 and 2: values per thread {8, 16, 32}, then CTA size {64, 128, 256, 512};
+//   level 1 and 2: values per thread {8, 16, 32}, then CTA size {32, 64, 128, 256, 512};
 //   level 2: L2 prefetch distance (1/2, 1, 2 waves of resident CTAs), then register caps
 //   (launch bounds for at most 48 or 40 registers a thread).
 // Candidates of one stage compile concurrently (NVRTC), and are timed one at a time under a
@@ -330,7 +330,7 @@ ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log) 
 	}
 	{
 		std::vector<Candidate> cs;
-		for (int ct : {64, 128, 256, 512}) {
+		for (int ct : {32, 64, 128, 256, 512}) {
 			Candidate c;
 			c.knobs = best;
 			c.knobs.cta_threads = ct;
