@@ -316,10 +316,18 @@ def run_gpu(args, rank: int, world: int):
     agg_bytes = sum(alg)
     agg_gbs = agg_bytes / (elapsed / args.steps) / 1e9 / world
 
-    # numerics spot check of what was timed
+    # numerics of what was timed: 64 frames of every size, forward spectrum and inverse output,
+    # against the FP64 oracle (relL2, the FP32 bar is 1e-6)
     import oracle
-    sref = np.stack([oracle.rfft(r.astype(np.float64)) for r in xs[-1][:64].cpu().numpy()])
-    rel = float(np.linalg.norm(specs[-1][:64].cpu().numpy() - sref) / np.linalg.norm(sref))
+    rel_sizes = {}
+    for n, x, s, b in zip(SIZES, xs, specs, backs):
+        xh = x[:64].cpu().numpy().astype(np.float64)
+        sref = np.stack([oracle.rfft(r) for r in xh])
+        rf = float(np.linalg.norm(s[:64].cpu().numpy() - sref) / np.linalg.norm(sref))
+        bref = np.stack([oracle.irfft(r.astype(np.complex128), n) for r in s[:64].cpu().numpy()])
+        ri = float(np.linalg.norm(b[:64].cpu().numpy() - bref) / np.linalg.norm(bref))
+        rel_sizes[f"N{n}"] = {"fwd": rf, "inv": ri}
+    rel = max(max(v.values()) for v in rel_sizes.values())
 
     # end to end through the C ABI with pinned host buffers
     e2e_steps = args.e2e_steps or max(3, args.steps // 10)
@@ -374,7 +382,7 @@ def run_gpu(args, rank: int, world: int):
                        "l2": "each step streams ~1.9 GB (> 129 MB L2), no flush",
                        "autotune": args.tune, "schedules": schedules},
             "gpu_launches": nl * args.steps,
-            "relL2_vs_fp64_oracle": rel,
+            "relL2_vs_fp64_oracle": rel, "relL2_per_size": rel_sizes,
             "roofline": {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": peak,
                          "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic_for(names[top]), "alg_bytes_per_launch": alg[top],
