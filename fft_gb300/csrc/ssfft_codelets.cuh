@@ -1614,6 +1614,54 @@ __global__ void __launch_bounds__(THREADS *G) strided(const StridedArgs a) {
 	}
 }
 
+// Bluestein's algorithm for lengths whose prime factors the pass kernels cannot take (beyond
+// one CTA): with w_k = e^{-i pi k^2 / N}, X_k = w_k sum_j (x_j w_j) conj(w_{k-j}), a circular
+// convolution of length M >= 2N - 1 done by two M-point transforms: the chirp product and zero
+// padding (blue_pre), the product with the precomputed spectrum of conj(w) (blue_mul) and the
+// final chirp product scaled by 1/M (blue_post).  CONJ conjugates the input (pre) or the output
+// (post) for the inverse.  One thread per element, blockIdx.y = transform.
+struct BlueArgs {
+	const void *in;     // N complex per transform, `dist` apart
+	void *out;
+	void *work;         // M complex per transform
+	const void *chirp;  // w_k, k < N
+	const void *bhat;   // M-point spectrum of b (b_m = conj(w_|m|), |m| < N, zero elsewhere)
+	long long n, m, batch, dist;
+};
+
+template <typename T, bool CONJ>
+__global__ void __launch_bounds__(256) blue_pre(const BlueArgs a) {
+	using C = typename Cx<T>::C;
+	const long long k = (long long)blockIdx.x * 256 + threadIdx.x, b = blockIdx.y;
+	if (k >= a.m || b >= a.batch) return;
+	C v = mkc(T(0), T(0));
+	if (k < a.n) {
+		C x = __ldcs(reinterpret_cast<const C *>(a.in) + b * a.dist + k);
+		if (CONJ) x = conj(x);
+		v = mul(x, __ldg(reinterpret_cast<const C *>(a.chirp) + k));
+	}
+	reinterpret_cast<C *>(a.work)[b * a.m + k] = v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) blue_mul(const BlueArgs a) {
+	using C = typename Cx<T>::C;
+	const long long k = (long long)blockIdx.x * 256 + threadIdx.x, b = blockIdx.y;
+	if (k >= a.m || b >= a.batch) return;
+	C *w = reinterpret_cast<C *>(a.work) + b * a.m + k;
+	*w = mul(*w, __ldg(reinterpret_cast<const C *>(a.bhat) + k));
+}
+
+template <typename T, bool CONJ>
+__global__ void __launch_bounds__(256) blue_post(const BlueArgs a) {
+	using C = typename Cx<T>::C;
+	const long long k = (long long)blockIdx.x * 256 + threadIdx.x, b = blockIdx.y;
+	if (k >= a.n || b >= a.batch) return;
+	C y = mul(reinterpret_cast<const C *>(a.work)[b * a.m + k], __ldg(reinterpret_cast<const C *>(a.chirp) + k));
+	y = scale(y, T(1) / T(a.m));
+	__stcs(reinterpret_cast<C *>(a.out) + b * a.dist + k, CONJ ? conj(y) : y);
+}
+
 // Real split / merge over global memory for real transforms longer than one CTA holds
 // (signalsmith-fft.h:459-472 forward, :477-492 inverse).  One thread per pair (i, conj(i)),
 // in place on `buf` (H complex per transform, batch transforms `dist` complex apart).

@@ -14,6 +14,12 @@
 // memory, and the inter-pass twiddle is applied in the pass's store.  Real transforms of
 // h = n/2 > 16384 points add the even/odd split (forward) or pre-twiddle (inverse) as one
 // element-wise kernel (ssfft_cl::real_split).
+//
+// Lengths with a prime factor above 1024 (which no pass can take) run Bluestein's algorithm
+// instead: a chirp product, an M-point forward transform (M >= 2N - 1, 2^a 3^b 5^c), a product
+// with the precomputed spectrum of the conjugate chirp, an M-point inverse transform and a final
+// chirp product (ssfft_cl::blue_*); the M-point transforms are ordinary plans of this library.
+// The reference handles such primes with its O(p^2) generic step (signalsmith-fft.h:187-215).
 #include <algorithm>
 #include <cstdlib>
 #include <cmath>
@@ -51,7 +57,30 @@ struct LargePlan {
 	void *d_tables = nullptr;
 	void *d_scratch = nullptr;
 	size_t scratch_batch = 0;
+	// Bluestein (M > 0): inner M-point plan, chirp w_k and spectrum of conj(w) in d_tables
+	long long M = 0;
+	ssfft_plan_t inner = nullptr;
+	size_t off_chirp = 0, off_bhat = 0;
+	CUfunction blue_pre[2] = {}, blue_mul = nullptr, blue_post[2] = {};
 };
+
+// Smallest 2^a 3^b 5^c >= v.
+static long long smooth_at_least(long long v) {
+	long long best = -1;
+	for (long long p5 = 1; p5 < 2 * v + 1; p5 *= 5)
+		for (long long p3 = p5; p3 < 2 * v + 1; p3 *= 3) {
+			long long x = p3;
+			while (x < v) x *= 2;
+			if (best < 0 || x < best) best = x;
+		}
+	return best;
+}
+
+static std::string blue_name(const char *k, ssfft_dtype dt, int conj) {
+	std::string r = std::string("ssfft_cl::") + k + "<" + (dt == SSFFT_F32 ? "float" : "double");
+	if (conj >= 0) r += conj ? ", true" : ", false";
+	return r + ">";
+}
 
 std::string LargePass::name(bool inverse, bool first, bool last, int rot) const {
 	const bool cin = inverse && first, cout = inverse && last;
@@ -110,6 +139,7 @@ static void put(std::vector<unsigned char> &blob, size_t off, const std::vector<
 
 void large_release(LargePlan *lp) {
 	if (!lp) return;
+	if (lp->inner) ssfft_plan_destroy(lp->inner);
 	if (lp->d_scratch) cudaFree(lp->d_scratch);
 	if (lp->d_tables) cudaFree(lp->d_tables);
 	delete lp;
@@ -126,7 +156,17 @@ static ssfft_status large_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind,
 	if (real && (n & 1)) return SSFFT_ERR_UNSUPPORTED;  // long odd real lengths
 	const long long N = (long long)(real ? n / 2 : n);
 	std::vector<long long> F;
-	if (!large_factors(N, F)) return SSFFT_ERR_UNSUPPORTED;
+	if (!large_factors(N, F)) {
+		// Bluestein: complex and RealFFT kinds (the half-shift rotation lives in the passes)
+		if (kind == SSFFT_REAL_HALFSHIFT || N > (1ll << 29)) return SSFFT_ERR_UNSUPPORTED;
+		lp->N = N;
+		lp->F.clear();
+		lp->real = real;
+		lp->modified = false;
+		lp->pass.clear();
+		lp->M = smooth_at_least(2 * N - 1);
+		return SSFFT_SUCCESS;
+	}
 	lp->N = N;
 	lp->F = F;
 	lp->real = real;
@@ -209,6 +249,15 @@ static ssfft_status large_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind,
 // Kernel names of a multi-pass plan: per pass forward then inverse, then the real split/merge.
 static std::vector<std::string> large_kernel_names(const LargePlan *lp, ssfft_dtype dtype) {
 	std::vector<std::string> names;
+	if (lp->M) {
+		names = {blue_name("blue_pre", dtype, 0), blue_name("blue_pre", dtype, 1), blue_name("blue_mul", dtype, -1),
+		         blue_name("blue_post", dtype, 0), blue_name("blue_post", dtype, 1)};
+		if (lp->real) {
+			names.push_back(split_name(dtype, lp->N, false, false));
+			names.push_back(split_name(dtype, lp->N, false, true));
+		}
+		return names;
+	}
 	const int P = (int)lp->pass.size();
 	for (int i = 0; i < P; ++i) {
 		const LargePass &ps = lp->pass[i];
@@ -230,7 +279,119 @@ ssfft_status large_jit_check(size_t n, ssfft_dtype dtype, ssfft_kind kind, const
 	LargeTables t;
 	ssfft_status st = large_schedule(n, dtype, kind, 227 * 1024, &lp, t);
 	if (st != SSFFT_SUCCESS) return st;
-	return jit_compile_only(large_kernel_names(&lp, dtype), arch, image_bytes);
+	st = jit_compile_only(large_kernel_names(&lp, dtype), arch, image_bytes);
+	if (st == SSFFT_SUCCESS && lp.M) {
+		size_t inner = 0;  // the M-point transforms
+		st = ssfft_jit_check((size_t)lp.M, dtype, SSFFT_COMPLEX, 1, arch, &inner);
+		if (image_bytes) *image_bytes += inner;
+	}
+	return st;
+}
+
+// Bluestein plan: chirp w_k = e^{-i pi k^2 / N} (k^2 reduced mod 2N exactly), the M-point
+// spectrum of b (b_m = conj(w_|m|) for |m| < N, m taken mod M) computed once with the inner
+// plan, and scratch for a chunk of transforms.
+static ssfft_status plan_build_bluestein(Plan *p, LargePlan *lp) {
+	const long long N = lp->N, M = lp->M;
+	const size_t eb = p->dtype == SSFFT_F32 ? 8 : 16, sb = eb / 2;
+	std::vector<double> chirp, rtw, b((size_t)M * 2, 0.0);
+	chirp.reserve((size_t)N * 2);
+	for (long long k = 0; k < N; ++k) {
+		const unsigned long long k2 =
+		    (unsigned long long)(((unsigned __int128)k * (unsigned __int128)k) % (unsigned __int128)(2 * N));
+		double re, im;
+		unit_root(k2, 2 * (unsigned long long)N, &re, &im);
+		chirp.push_back(re);
+		chirp.push_back(im);
+		b[2 * k] = re;  // conj(w_k)
+		b[2 * k + 1] = -im;
+		if (k) {
+			b[2 * (M - k)] = re;
+			b[2 * (M - k) + 1] = -im;
+		}
+	}
+	if (lp->real)
+		for (long long i = 0; i <= N / 2; ++i) {
+			double re, im;
+			unit_root(i, p->n, &re, &im);
+			rtw.push_back(im);
+			rtw.push_back(-re);
+		}
+	lp->off_rtw = 0;
+	lp->off_chirp = align_up(rtw.size() * sb, 256);
+	lp->off_bhat = align_up(lp->off_chirp + chirp.size() * sb, 256);
+	const size_t total = align_up(lp->off_bhat + (size_t)M * eb, 256);
+	std::vector<unsigned char> blob(lp->off_bhat, 0);
+	if (sb == 4) {
+		put<float>(blob, lp->off_rtw, rtw);
+		put<float>(blob, lp->off_chirp, chirp);
+	} else {
+		put<double>(blob, lp->off_rtw, rtw);
+		put<double>(blob, lp->off_chirp, chirp);
+	}
+	std::vector<unsigned char> bb((size_t)M * eb);
+	if (sb == 4) put<float>(bb, 0, b);
+	else put<double>(bb, 0, b);
+	cudaError_t e = cudaMalloc(&lp->d_tables, total);
+	if (e == cudaSuccess) e = cudaMemcpy(lp->d_tables, blob.data(), blob.size(), cudaMemcpyHostToDevice);
+	unsigned char *bhat = static_cast<unsigned char *>(lp->d_tables) + lp->off_bhat;
+	if (e == cudaSuccess) e = cudaMemcpy(bhat, bb.data(), bb.size(), cudaMemcpyHostToDevice);
+	if (e != cudaSuccess) return cuda_fail(e, "bluestein tables");
+	p->table_bytes = total;
+	// scratch: M complex per transform in flight, up to ~256 MiB
+	const size_t per = (size_t)M * eb;
+	lp->scratch_batch = std::max<size_t>(1, std::min<size_t>(std::min<size_t>(p->batch, 65535), (256u << 20) / per));
+	e = cudaMalloc(&lp->d_scratch, per * lp->scratch_batch);
+	if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(bluestein scratch)");
+	p->scratch_bytes = per * lp->scratch_batch;
+	ssfft_status st = ssfft_plan_create(&lp->inner, (size_t)M, p->dtype, SSFFT_COMPLEX, lp->scratch_batch);
+	if (st != SSFFT_SUCCESS) return st;
+	// spectrum of b, in place, once
+	st = ssfft_exec_batch(lp->inner, 0, bhat, bhat, 1, nullptr);
+	if (st == SSFFT_SUCCESS) {
+		e = cudaDeviceSynchronize();
+		if (e != cudaSuccess) st = cuda_fail(e, "bluestein spectrum");
+	}
+	if (st != SSFFT_SUCCESS) return st;
+	std::vector<CUfunction> fns;
+	st = jit_kernels(large_kernel_names(lp, p->dtype), 0, fns);
+	if (st != SSFFT_SUCCESS) return st;
+	lp->blue_pre[0] = fns[0];
+	lp->blue_pre[1] = fns[1];
+	lp->blue_mul = fns[2];
+	lp->blue_post[0] = fns[3];
+	lp->blue_post[1] = fns[4];
+	if (lp->real) {
+		lp->split_fwd = fns[5];
+		lp->split_inv = fns[6];
+	}
+	p->launches_per_exec = 3 + 2 * reinterpret_cast<const Plan *>(lp->inner)->launches_per_exec + (lp->real ? 1 : 0);
+	return SSFFT_SUCCESS;
+}
+
+// The complex N-point transform of nb transforms (dist N) through Bluestein, src -> dst; cin /
+// cout conjugate the input / output.
+static ssfft_status launch_bluestein(LargePlan *lp, ssfft_dtype dtype, const void *src, void *dst, long long nb,
+                                     bool cin, bool cout, cudaStream_t s) {
+	const unsigned char *tab = static_cast<const unsigned char *>(lp->d_tables);
+	ssfft_cl::BlueArgs a;
+	a.in = src;
+	a.out = dst;
+	a.work = lp->d_scratch;
+	a.chirp = tab + lp->off_chirp;
+	a.bhat = tab + lp->off_bhat;
+	a.n = lp->N;
+	a.m = lp->M;
+	a.batch = nb;
+	a.dist = lp->N;
+	const unsigned gm = (unsigned)((lp->M + 255) / 256), gn = (unsigned)((lp->N + 255) / 256);
+	ssfft_status st = jit_launch_grid(lp->blue_pre[cin ? 1 : 0], gm, (unsigned)nb, 256, 0, s, &a);
+	if (st == SSFFT_SUCCESS) st = ssfft_exec_batch(lp->inner, 0, lp->d_scratch, lp->d_scratch, (size_t)nb, s);
+	if (st == SSFFT_SUCCESS) st = jit_launch_grid(lp->blue_mul, gm, (unsigned)nb, 256, 0, s, &a);
+	if (st == SSFFT_SUCCESS) st = ssfft_exec_batch(lp->inner, 1, lp->d_scratch, lp->d_scratch, (size_t)nb, s);
+	if (st == SSFFT_SUCCESS) st = jit_launch_grid(lp->blue_post[cout ? 1 : 0], gn, (unsigned)nb, 256, 0, s, &a);
+	(void)dtype;
+	return st;
 }
 
 ssfft_status plan_build_large(Plan *p) {
@@ -239,6 +400,7 @@ ssfft_status plan_build_large(Plan *p) {
 	LargeTables tabs;
 	ssfft_status st0 = large_schedule(p->n, p->dtype, p->kind, device_smem_limit(p->device), lp, tabs);
 	if (st0 != SSFFT_SUCCESS) return st0;
+	if (lp->M) return plan_build_bluestein(p, lp);
 	const bool real = lp->real;
 	const long long N = lp->N;
 	const int P = (int)lp->pass.size();
@@ -360,6 +522,12 @@ ssfft_status launch_large(Plan *p, int inverse, const void *in, void *out, size_
 			ssfft_status st = jit_launch_grid(lp->split_inv, (unsigned)((pairs + 255) / 256), (unsigned)nb, 256, 0, s, &a);
 			if (st != SSFFT_SUCCESS) return st;
 			first_in = dst;
+		}
+		if (lp->M) {
+			// complex engine: Bluestein (a RealFFT inverse arrives pre-twiddled and conjugated)
+			const bool cin = inverse && !lp->real, cout = inverse;
+			ssfft_status st = launch_bluestein(lp, p->dtype, first_in, dst, nb, cin, cout, s);
+			if (st != SSFFT_SUCCESS) return st;
 		}
 		for (int i = 0; i < P; ++i) {
 			const LargePass &ps = lp->pass[i];

@@ -2,7 +2,8 @@
 the C ABI, against the FP64 oracle (oracle/ssfft_oracle.c) and size-independent properties.
 
 Tolerances: relL2 <= 1e-6 (FP32) up to 2^16 points, <= 5e-6 at 2^24 and the other large single
-transforms, <= 1e-14 for FP64."""
+transforms, <= 1e-14 for FP64; Bluestein lengths (a prime factor above 1024): <= 2e-6 (FP32),
+<= 1e-13 (FP64), two M-point transforms and two chirp products deep."""
 import numpy as np
 import pytest
 
@@ -120,3 +121,38 @@ def test_linearity_large(F):
     fc = c2c(F, c)[0].cpu().numpy().astype(np.complex128)
     fac = c2c(F, (a + c).astype(np.complex64))[0].cpu().numpy().astype(np.complex128)
     assert rel_l2(fac, fa + fc) <= 2e-6
+
+
+# Bluestein lengths: a prime factor above 1024 (which no pass takes) beyond one CTA
+@pytest.mark.parametrize("n,dt,tol", [(17 * 1031, "f32", 2e-6), (2 * 20011, "f32", 2e-6), (10007, "f64", 1e-13),
+                                      (3 * 4099, "f64", 1e-13)])
+def test_bluestein_c2c_vs_oracle(F, n, dt, tol):
+    rng = np.random.default_rng(n)
+    cdt = np.complex64 if dt == "f32" else np.complex128
+    x = (rng.uniform(-1, 1, (2, n)) + 1j * rng.uniform(-1, 1, (2, n))).astype(cdt)
+    y, xi, d = c2c(F, x)
+    assert d["radices"] == []  # no pass schedule: Bluestein
+    ref = oracle.fft(x[0].astype(np.complex128))
+    got = y.cpu().numpy()
+    assert rel_l2(got[0], ref) <= tol, rel_l2(got[0], ref)
+    ref1 = oracle.fft(x[1].astype(np.complex128))
+    assert rel_l2(got[1], ref1) <= tol
+    # inverse (unnormalised) brings it back
+    z, _, _ = c2c(F, got, inverse=True)
+    assert rel_l2(z.cpu().numpy() / n, x) <= 2 * tol
+
+
+def test_bluestein_real_vs_oracle(F):
+    n = 2 * 20011 * 2  # h = 40022 = 2 x 20011
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((1, n)).astype(np.float32)
+    p = F.Plan(n, "f32", "real", 1)
+    xi = torch.from_numpy(x).cuda()
+    s = torch.empty((1, n // 2), dtype=torch.complex64, device="cuda")
+    b = torch.empty_like(xi)
+    p.exec(False, xi.data_ptr(), s.data_ptr(), 0)
+    p.exec(True, s.data_ptr(), b.data_ptr(), 0)
+    torch.cuda.synchronize()
+    ref = oracle.rfft(x[0].astype(np.float64))
+    assert rel_l2(s.cpu().numpy()[0], ref) <= 2e-6, rel_l2(s.cpu().numpy()[0], ref)
+    assert rel_l2(b.cpu().numpy() / n, x) <= 4e-6
