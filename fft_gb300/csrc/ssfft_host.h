@@ -152,6 +152,7 @@ size_t plan_out_bytes(const Plan *p, int inverse, size_t batch);
 size_t size_minimum(size_t n);
 size_t size_maximum(size_t n);
 ssfft_status plan_build_large(Plan *p);
+bool plan_single_cta(size_t n, ssfft_dtype dtype, ssfft_kind kind);
 void plan_release(Plan *p);
 ssfft_status launch_batch(const Plan *p, int inverse, const void *in, void *out, size_t batch, cudaStream_t s);
 ssfft_status launch_large(Plan *p, int inverse, const void *in, void *out, size_t batch, cudaStream_t s);

@@ -603,13 +603,22 @@ long long prefetch_distance(const Schedule &s, const Knobs &k, long long residen
 	return resident * quarters / 4;
 }
 
+// Whether (n, dtype, kind) runs in one CTA per transform (otherwise: multi-pass or Bluestein,
+// which hold per-plan scratch).  A direct pass of a prime above 1024 is O(p^2) per point; such
+// lengths go to Bluestein instead (even real lengths and complex ones).
+bool plan_single_cta(size_t n, ssfft_dtype dtype, ssfft_kind kind) {
+	Schedule d;
+	if (!single_schedule(n, dtype, kind, 1, d)) return false;
+	const bool odd_real = kind != SSFFT_COMPLEX && (n & 1);
+	for (int r : d.radices)
+		if (!specialised(r) && r > 1024 && !odd_real) return false;
+	return true;
+}
+
 static ssfft_status plan_build_single(Plan *p) {
 	Schedule &s = p->main.sch;
-	{
-		// the default schedule decides whether n runs in one CTA; explicit or tuned knobs refine it
-		Schedule d;
-		if (!single_schedule(p->n, p->dtype, p->kind, p->batch, d)) return SSFFT_ERR_UNSUPPORTED;
-	}
+	// the default schedule decides whether n runs in one CTA; explicit or tuned knobs refine it
+	if (!plan_single_cta(p->n, p->dtype, p->kind)) return SSFFT_ERR_UNSUPPORTED;
 	if (p->autotune > 0 && p->knobs.empty()) {
 		Knobs best;
 		ssfft_status st = autotune_single(p, p->autotune, best, p->tune_log);

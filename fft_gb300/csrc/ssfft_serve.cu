@@ -96,9 +96,18 @@ struct ShapeKey {
 };
 
 // Shapes longer than one CTA holds run multi-pass plans with plan-owned scratch.
+// Shapes whose plans hold scratch (multi-pass or Bluestein): one plan per wave slot.  The
+// planner's answer is cached per shape (the serving loop asks for every wave).
 bool multi_pass(const ssfft_request &r) {
-	const size_t cn = r.kind == SSFFT_COMPLEX ? r.n : r.n / 2;
-	return cn > (r.dtype == SSFFT_F32 ? (size_t)kMaxSubTransform : (size_t)kMaxSubTransform / 2);
+	static std::mutex mu;
+	static std::map<std::tuple<size_t, int, int>, bool> memo;
+	const auto key = std::make_tuple(r.n, (int)r.dtype, (int)r.kind);
+	std::lock_guard<std::mutex> lock(mu);
+	auto it = memo.find(key);
+	if (it != memo.end()) return it->second;
+	const bool mp = !plan_single_cta(r.n, r.dtype, r.kind);
+	memo.emplace(key, mp);
+	return mp;
 }
 
 size_t scalar_bytes(ssfft_dtype dt) { return dt == SSFFT_F32 ? 4 : 8; }

@@ -123,9 +123,10 @@ def test_linearity_large(F):
     assert rel_l2(fac, fa + fc) <= 2e-6
 
 
-# Bluestein lengths: a prime factor above 1024 (which no pass takes) beyond one CTA
+# Bluestein lengths: a prime factor above 1024 (which no pass takes, and which a direct pass would
+# run in O(p^2)), in and beyond one CTA
 @pytest.mark.parametrize("n,dt,tol", [(17 * 1031, "f32", 2e-6), (2 * 20011, "f32", 2e-6), (10007, "f64", 1e-13),
-                                      (3 * 4099, "f64", 1e-13)])
+                                      (3 * 4099, "f64", 1e-13), (12289, "f32", 2e-6), (1031, "f64", 1e-13)])
 def test_bluestein_c2c_vs_oracle(F, n, dt, tol):
     rng = np.random.default_rng(n)
     cdt = np.complex64 if dt == "f32" else np.complex128
@@ -142,8 +143,8 @@ def test_bluestein_c2c_vs_oracle(F, n, dt, tol):
     assert rel_l2(z.cpu().numpy() / n, x) <= 2 * tol
 
 
-def test_bluestein_real_vs_oracle(F):
-    n = 2 * 20011 * 2  # h = 40022 = 2 x 20011
+@pytest.mark.parametrize("n", [2 * 20011 * 2, 2 * 1031])
+def test_bluestein_real_vs_oracle(F, n):
     rng = np.random.default_rng(5)
     x = rng.standard_normal((1, n)).astype(np.float32)
     p = F.Plan(n, "f32", "real", 1)
