@@ -133,11 +133,21 @@ def test_bluestein_c2c_vs_oracle(F, n, dt, tol):
     x = (rng.uniform(-1, 1, (2, n)) + 1j * rng.uniform(-1, 1, (2, n))).astype(cdt)
     y, xi, d = c2c(F, x)
     assert d["radices"] == []  # no pass schedule: Bluestein
-    ref = oracle.fft(x[0].astype(np.complex128))
     got = y.cpu().numpy()
-    assert rel_l2(got[0], ref) <= tol, rel_l2(got[0], ref)
-    ref1 = oracle.fft(x[1].astype(np.complex128))
-    assert rel_l2(got[1], ref1) <= tol
+    if dt == "f32":
+        ref = oracle.fft(x[0].astype(np.complex128))
+        assert rel_l2(got[0], ref) <= tol, rel_l2(got[0], ref)
+        ref1 = oracle.fft(x[1].astype(np.complex128))
+        assert rel_l2(got[1], ref1) <= tol
+    else:
+        # At these prime lengths the reference's own FFT<double> (its generic step evaluates
+        # cos/sin of phases up to 2 pi p) carries ~1e-12 error, so the FP64 result is held to
+        # 1e-13 against an exact DFT (numpy's FFT in FP64) and to the reference's accuracy
+        # against the oracle.
+        exact = np.fft.fft(x.astype(np.complex128), axis=1)
+        assert rel_l2(got, exact) <= tol, rel_l2(got, exact)
+        ref = oracle.fft(x[0].astype(np.complex128))
+        assert rel_l2(got[0], ref) <= 5e-11, rel_l2(got[0], ref)
     # inverse (unnormalised) brings it back
     z, _, _ = c2c(F, got, inverse=True)
     assert rel_l2(z.cpu().numpy() / n, x) <= 2 * tol
