@@ -112,7 +112,6 @@ ssfft_status cuda_fail(cudaError_t e, const char *what);
 // roots of unity, schedules and tables
 void unit_root(unsigned long long k, unsigned long long L, double *re, double *im);
 bool choose_radices(int n, std::vector<int> &radices, bool large_composites = true, bool real_split = false);
-bool fewest_radices(int n, int max_radix, std::vector<int> &out);
 // allow_staged: 0 never, 1 when SSFFT_STAGED=1, 2 always (where the size allows it)
 bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, Schedule &s, int allow_staged = 1,
                    const Knobs *knobs = nullptr, int fuse = 0);

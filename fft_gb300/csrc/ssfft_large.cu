@@ -186,15 +186,8 @@ static ssfft_status large_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind,
 		const long long Fi = F[i], R = L / Fi, Q = N / L;
 		const bool last = i == P - 1;
 		Schedule s;
-		// SSFFT_LARGE_FEWEST=1 (experiment): sub-transforms in the fewest register-radix passes
-		const char *fe = std::getenv("SSFFT_LARGE_FEWEST");
-		Knobs kn;
-		if (fe && fe[0] == '1') {
-			std::vector<int> r;
-			if (fewest_radices((int)Fi, 32, r)) kn.radices = r;
-		}
-		if (!make_schedule(dtype, (int)Fi, 0, false, 1, s, false, kn.radices.empty() ? nullptr : &kn))
-			return SSFFT_ERR_UNSUPPORTED;
+		// (fewest-pass sub-transform lists, e.g. 243 = 27 * 9, measured no faster on GB300)
+		if (!make_schedule(dtype, (int)Fi, 0, false, 1, s, false)) return SSFFT_ERR_UNSUPPORTED;
 		// G sub-transforms per CTA: 128-256 B segments, <= 1024 threads, <= ~100 KiB smem
 		const long long U0 = last ? F[0] : R;
 		// SSFFT_LARGE_GROUP overrides the group size (experiments; read when the plan is made)

@@ -192,16 +192,6 @@ static void radices_for(int a, int b, int c, const std::vector<int> &rest, bool 
 	out.insert(out.end(), rest.begin(), rest.end());
 }
 
-// The fewest-pass list (radices up to max_radix) for a 2^a 3^b 5^c length, ordered as the
-// planner orders lists; false for other lengths.
-bool fewest_radices(int n, int max_radix, std::vector<int> &out) {
-	int m = n, a = 0, b = 0, c = 0;
-	while (m % 2 == 0) m /= 2, ++a;
-	while (m % 3 == 0) m /= 3, ++b;
-	while (m % 5 == 0) m /= 5, ++c;
-	return m == 1 && n > 1 && fewest_passes(a, b, c, max_radix, out);
-}
-
 bool choose_radices(int n, std::vector<int> &radices, bool large_composites, bool real_split) {
 	radices.clear();
 	if (n < 1) return false;
