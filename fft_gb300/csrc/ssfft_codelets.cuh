@@ -1614,6 +1614,298 @@ __global__ void __launch_bounds__(THREADS *G) strided(const StridedArgs a) {
 	}
 }
 
+// ------------------------------------------------------------------ two-CTA (cluster) transforms
+//
+// Complex FP32 transforms of N = N1 N2 points too long for two CTAs of the batch kernel to share
+// an SM (from ~8192 points one transform fills 64-140 KB of shared memory and 128+ registers a
+// thread; with one CTA per SM its HBM and arithmetic phases cannot overlap).  A cluster of two
+// CTAs (on two SMs) runs one transform as a four-step inside the cluster, each CTA holding half:
+//   n = n1 N2 + n2, k = k1 + N1 k2,
+//   phase A (CTA c, columns n2 = c N2/2 + v): Y[k1][n2] = W_N^{n2 k1} sum_n1 x[n1 N2 + n2] W_N1^{n1 k1}
+//   phase B (CTA c, rows k1 = c N1/2 + u):    X[k1 + N1 k2] = sum_n2 Y[k1][n2] W_N2^{n2 k2}.
+// Phase A reads N1 segments of N2/2 contiguous points from HBM; its last pass writes Y transposed
+// (column-major, odd row length P) into its own shared memory; after a cluster barrier, phase B's
+// first pass reads each row from both CTAs' shared memory (distributed shared memory), and a
+// second barrier guards the buffers before they are overwritten.  Phase B's last pass writes N2
+// segments of N1/2 contiguous points.  Inside a phase the passes are the batch kernel's Stockham
+// passes over V interleaved columns (element (v, e) at s[e V + v]: consecutive threads take
+// consecutive columns, so shared-memory and HBM accesses are unit-stride).  With half a transform
+// per CTA, two CTAs of different transforms share each SM and overlap each other's phases.
+template <int... Rs>
+struct Radices {};
+
+template <int NS, int... Rs>
+struct TwTotal {
+	static constexpr int value = 0;
+};
+template <int NS, int R, int... Rs>
+struct TwTotal<NS, R, Rs...> {
+	static constexpr int value = TwCount<R, NS>::value + TwTotal<NS * R, Rs...>::value;
+};
+template <class L>
+struct RadixList;
+template <int... Rs>
+struct RadixList<Radices<Rs...>> {
+	static constexpr int n = (1 * ... * Rs);
+	static constexpr int tw = TwTotal<1, Rs...>::value;  // pass-twiddle slots
+};
+
+// inter-phase twiddle W_N^t = hi[t >> b] lo[t & (2^b - 1)], 4^b >= N
+__host__ __device__ constexpr int pair_lo_bits(int n) {
+	int b = 0;
+	while ((1 << (2 * b)) < n) ++b;
+	return b;
+}
+
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ unsigned pair_rank() {
+	unsigned r;
+	asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+	return r;
+}
+// all threads of both CTAs; release / acquire orders the shared-memory writes and reads around it
+__device__ __forceinline__ void pair_sync() {
+	asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ unsigned char *pair_smem() {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	return smem_raw;
+}
+// shared memory of cluster CTA `rank` at the offset of `p` in this CTA's, as a cluster address
+struct ClusterSmem {
+	unsigned base;
+};
+__device__ __forceinline__ ClusterSmem cluster_smem(const void *p, unsigned rank) {
+	unsigned a;
+	asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(a) : "r"(smem_u32(p)), "r"(rank));
+	return ClusterSmem{a};
+}
+__device__ __forceinline__ float2 cluster_load(ClusterSmem s, int i) {
+	float2 v;
+	asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(s.base + 8u * (unsigned)i));
+	return v;
+}
+#elif defined(SSFFT_EMULATION)
+// Host emulation: the two CTAs of a cluster run at once, each with its own shared-memory array.
+extern thread_local unsigned char *emu_cta_smem, *emu_peer_smem;
+extern thread_local std::barrier<> *emu_cluster_barrier;
+inline unsigned pair_rank() { return blockIdx.x & 1u; }
+inline void pair_sync() { emu_cluster_barrier->arrive_and_wait(); }
+inline unsigned char *pair_smem() { return emu_cta_smem; }
+struct ClusterSmem {
+	const float2 *base;
+};
+inline ClusterSmem cluster_smem(const void *p, unsigned rank) {
+	const long off = static_cast<const unsigned char *>(p) - emu_cta_smem;
+	unsigned char *b = rank == pair_rank() ? emu_cta_smem : emu_peer_smem;
+	return ClusterSmem{reinterpret_cast<const float2 *>(b + off)};
+}
+float2 emu_cluster_load(ClusterSmem s, int i);  // bounds-checked (emu_main.cpp)
+inline float2 cluster_load(ClusterSmem s, int i) { return emu_cluster_load(s, i); }
+#else
+// host pass of the library build: declarations only
+unsigned pair_rank();
+void pair_sync();
+unsigned char *pair_smem();
+struct ClusterSmem {
+	unsigned base;
+};
+ClusterSmem cluster_smem(const void *p, unsigned rank);
+float2 cluster_load(ClusterSmem s, int i);
+#endif
+
+template <typename T>
+struct PairCtx {
+	using C = typename Cx<T>::C;
+	C *s;              // this CTA's shared-memory slots
+	const C *lo, *hi;  // inter-phase twiddle table (shared memory)
+	const C *gin;      // this CTA's first input column of the transform
+	C *gout;           // this CTA's first output row
+	ClusterSmem cl[2]; // both CTAs' slots, as cluster addresses
+	unsigned rank;
+	int t;
+	bool valid;
+};
+
+// One pass of phase A: radix R over the N1-point columns, V = N2/2 of them interleaved.
+template <typename T, int N1, int N2, int THREADS, bool INV, int EMAX, int R, int NS, int TWO, bool FIRST, bool LAST>
+__device__ __forceinline__ void pair_a_pass(const PairCtx<T> &c, const typename Cx<T>::C *tw) {
+	using C = typename Cx<T>::C;
+	constexpr int V = N2 / 2, P = N1 | 1, NB = N1 / R, NBF = V * NB;
+	constexpr int NBPT = (NBF + THREADS - 1) / THREADS;
+	constexpr bool GUARD = NBF % THREADS != 0;
+	constexpr int LB = pair_lo_bits(N1 * N2);
+	static_assert(Specialised<R>::value, "pair passes use register butterflies");
+	static_assert(NBPT * R <= EMAX, "a pass holds at most EMAX values a thread");
+	C v[NBPT][R];
+#pragma unroll
+	for (int i = 0; i < NBPT; ++i) {
+		const int b = c.t + i * THREADS;
+		if (c.valid && (!GUARD || b < NBF)) {
+			const int col = b % V, j = b / V;
+#pragma unroll
+			for (int r = 0; r < R; ++r) {
+				const int e = j + r * NB;
+				if constexpr (FIRST) {
+					const C x = __ldcs(c.gin + (long long)e * N2 + col);
+					v[i][r] = INV ? conj(x) : x;
+				} else {
+					v[i][r] = c.s[e * V + col];
+				}
+			}
+			if constexpr (NS > 1) apply_twiddles<T, R, NS, TWO>(v[i], tw, j % NS);
+			dft<R>(v[i]);
+		}
+	}
+	if constexpr (!FIRST) __syncthreads();
+#pragma unroll
+	for (int i = 0; i < NBPT; ++i) {
+		const int b = c.t + i * THREADS;
+		if (c.valid && (!GUARD || b < NBF)) {
+			const int col = b % V, j = b / V;
+			const int base = (j / NS) * NS * (R - 1) + j;
+#pragma unroll
+			for (int r = 0; r < R; ++r) {
+				const int k = base + r * NS;
+				if constexpr (LAST) {
+					const int t = ((int)c.rank * V + col) * k;  // n2 k1 < N
+					c.s[col * P + k] = mul(v[i][r], mul(c.hi[t >> LB], c.lo[t & ((1 << LB) - 1)]));
+				} else {
+					c.s[k * V + col] = v[i][r];
+				}
+			}
+		}
+	}
+	if constexpr (LAST) pair_sync();
+	else __syncthreads();
+}
+
+// One pass of phase B: radix R over the N2-point rows, V = N1/2 of them interleaved.  The first
+// pass reads the rows from both CTAs (column n2 lives in CTA n2 / (N2/2)).
+template <typename T, int N1, int N2, int THREADS, bool INV, int EMAX, int R, int NS, int TWO, bool FIRST, bool LAST>
+__device__ __forceinline__ void pair_b_pass(const PairCtx<T> &c, const typename Cx<T>::C *tw) {
+	using C = typename Cx<T>::C;
+	constexpr int VA = N2 / 2, V = N1 / 2, P = N1 | 1, NB = N2 / R, NBF = V * NB;
+	constexpr int NBPT = (NBF + THREADS - 1) / THREADS;
+	constexpr bool GUARD = NBF % THREADS != 0;
+	static_assert(Specialised<R>::value, "pair passes use register butterflies");
+	static_assert(NBPT * R <= EMAX, "a pass holds at most EMAX values a thread");
+	static_assert(!FIRST || R % 2 == 0, "the first phase-B radix is even (half its inputs in each CTA)");
+	C v[NBPT][R];
+#pragma unroll
+	for (int i = 0; i < NBPT; ++i) {
+		const int b = c.t + i * THREADS;
+		if (c.valid && (!GUARD || b < NBF)) {
+			const int row = b % V, j = b / V;
+#pragma unroll
+			for (int r = 0; r < R; ++r) {
+				if constexpr (FIRST) {
+					// n2 = j + r NB: CTA q = r / (R/2), column n2 - q VA
+					constexpr int H = R / 2;
+					const int q = r / H;
+					v[i][r] = cluster_load(c.cl[q], (j + (r - q * H) * NB) * P + (int)c.rank * V + row);
+				} else {
+					v[i][r] = c.s[(j + r * NB) * V + row];
+				}
+			}
+			if constexpr (NS > 1) apply_twiddles<T, R, NS, TWO>(v[i], tw, j % NS);
+			dft<R>(v[i]);
+		}
+	}
+	if constexpr (FIRST) pair_sync();  // both CTAs have read their rows: the buffers may be reused
+	else __syncthreads();
+#pragma unroll
+	for (int i = 0; i < NBPT; ++i) {
+		const int b = c.t + i * THREADS;
+		if (c.valid && (!GUARD || b < NBF)) {
+			const int row = b % V, j = b / V;
+			const int base = (j / NS) * NS * (R - 1) + j;
+#pragma unroll
+			for (int r = 0; r < R; ++r) {
+				const int k = base + r * NS;
+				if constexpr (LAST) __stcs(c.gout + (long long)k * N1 + row, INV ? conj(v[i][r]) : v[i][r]);
+				else c.s[k * V + row] = v[i][r];
+			}
+		}
+	}
+	if constexpr (!LAST) __syncthreads();
+}
+
+template <typename T, int N1, int N2, int THREADS, bool INV, int EMAX, bool B, int NS, int TWO, int R, int... Rest>
+__device__ __forceinline__ void pair_passes(const PairCtx<T> &c, const typename Cx<T>::C *tw) {
+	constexpr bool FIRST = NS == 1, LAST = sizeof...(Rest) == 0;
+	if constexpr (B) pair_b_pass<T, N1, N2, THREADS, INV, EMAX, R, NS, TWO, FIRST, LAST>(c, tw);
+	else pair_a_pass<T, N1, N2, THREADS, INV, EMAX, R, NS, TWO, FIRST, LAST>(c, tw);
+	if constexpr (!LAST)
+		pair_passes<T, N1, N2, THREADS, INV, EMAX, B, NS * R, TWO + TwCount<R, NS>::value, Rest...>(c, tw);
+}
+template <class L>
+struct PairPhase;
+template <int... Rs>
+struct PairPhase<Radices<Rs...>> {
+	template <typename T, int N1, int N2, int THREADS, bool INV, int EMAX, bool B, int TWO>
+	__device__ __forceinline__ static void run(const PairCtx<T> &c, const typename Cx<T>::C *tw) {
+		pair_passes<T, N1, N2, THREADS, INV, EMAX, B, 1, TWO, Rs...>(c, tw);
+	}
+};
+
+// shared-memory slots of a pair CTA: the larger of the interleaved halves (N/2) and the
+// transposed phase-A output (N2/2 rows of P), then the inter-phase table
+__host__ __device__ constexpr int pair_slots(int n1, int n2) {
+	const int data = (n2 / 2) * (n1 | 1) > (n1 * n2) / 2 ? (n2 / 2) * (n1 | 1) : (n1 * n2) / 2;
+	const int lb = pair_lo_bits(n1 * n2);
+	return data + (1 << lb) + (n1 * n2 + (1 << lb) - 1) / (1 << lb);
+}
+
+// Args: in / out / batch / in_dist / out_dist / offs as for the batch kernel; tw = phase A's pass
+// twiddles, phase B's, then the inter-phase table (lo, hi); pf_dist in transforms.  Grid: two CTAs
+// per transform.
+template <typename T, int N1, int N2, int THREADS, bool INV, int EMAX, int MINB, class LA, class LB>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, MINB) pair(const Args a) {
+	using C = typename Cx<T>::C;
+	static_assert(RadixList<LA>::n == N1 && RadixList<LB>::n == N2, "radix lists multiply to N1 and N2");
+	static_assert(N1 % 2 == 0 && N2 % 2 == 0, "both factors even");
+	constexpr int N = N1 * N2, LOB = pair_lo_bits(N), LO = 1 << LOB, HI = (N + LO - 1) / LO;
+	constexpr int DATA = pair_slots(N1, N2) - LO - HI;
+	PairCtx<T> c;
+	c.s = reinterpret_cast<C *>(pair_smem());
+	c.lo = c.s + DATA;
+	c.hi = c.s + DATA + LO;
+	c.rank = pair_rank();
+	c.t = threadIdx.x;
+	const long long g = (long long)(blockIdx.x >> 1);
+	c.valid = g < a.batch;
+	long long oin = 0, oout = 0;
+	if (c.valid) {
+		if (a.offs) oin = oout = a.offs[g];
+		else oin = g * a.in_dist, oout = g * a.out_dist;
+	}
+	c.gin = reinterpret_cast<const C *>(reinterpret_cast<const T *>(a.in) + oin) + c.rank * (N2 / 2);
+	c.gout = reinterpret_cast<C *>(reinterpret_cast<T *>(a.out) + oout) + c.rank * (N1 / 2);
+	c.cl[0] = cluster_smem(c.s, 0);
+	c.cl[1] = cluster_smem(c.s, 1);
+	const C *tw = reinterpret_cast<const C *>(a.tw);
+	C *tab = c.s + DATA;
+	for (int i = threadIdx.x; i < LO + HI; i += THREADS)
+		tab[i] = __ldg(tw + RadixList<LA>::tw + RadixList<LB>::tw + i);
+	// L2 prefetch of the transform pf_dist ahead: each CTA one contiguous half of it
+	if (a.pf_dist > 0 && g + a.pf_dist < a.batch) {
+		const long long pg = g + a.pf_dist;
+		const long long po = a.offs ? a.offs[pg] : pg * a.in_dist;
+		const unsigned half = (unsigned)(N / 2 * sizeof(C));
+		const unsigned char *base =
+		    reinterpret_cast<const unsigned char *>(reinterpret_cast<const T *>(a.in) + po) + c.rank * half;
+		if (((unsigned long long)base & 15) == 0 && half % 16 == 0) {
+			if (threadIdx.x == 0) prefetch_l2_bulk(base, half);
+		} else {
+			for (unsigned off = threadIdx.x * 128u; off < half; off += THREADS * 128u) prefetch_l2(base + off);
+		}
+	}
+	__syncthreads();
+	PairPhase<LA>::template run<T, N1, N2, THREADS, INV, EMAX, false, 0>(c, tw);
+	PairPhase<LB>::template run<T, N1, N2, THREADS, INV, EMAX, true, RadixList<LA>::tw>(c, tw);
+}
+
 // Bluestein's algorithm for lengths whose prime factors the pass kernels cannot take (beyond
 // one CTA): with w_k = e^{-i pi k^2 / N}, X_k = w_k sum_j (x_j w_j) conj(w_{k-j}), a circular
 // convolution of length M >= 2N - 1 done by two M-point transforms: the chirp product and zero

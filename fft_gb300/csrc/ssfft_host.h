@@ -36,7 +36,10 @@ struct Schedule {
 	int emax = 16;            // complex values a thread holds in one pass
 	unsigned in_bytes = 0;    // staged: input bytes of one transform
 	size_t smem_bytes = 0;
+	int pair = 0;             // ssfft_cl::pair (two-CTA cluster): the first `pair` radices are phase A
+	int n1 = 0;               // pair: phase A length (product of its radices)
 	int cta_threads() const { return threads * per_cta; }
+	long long grid(long long batch) const { return pair ? 2 * batch : (batch + per_cta - 1) / per_cta; }
 	std::string name(bool inverse) const;
 };
 
@@ -51,8 +54,10 @@ struct Knobs {
 	int prefetch = -1;         // L2 prefetch distance in quarter waves of resident CTAs (-1 default)
 	int fuse = -1;             // RealFFT split fused into a pass: -1 planner default, 0 never (an
 	                           // explicit radix order from the caller is kept as given), 1 always
+	int pair = -1;             // two-CTA cluster schedule: -1 planner default, 0 never, k > 0 with the
+	                           // first k of `radices` as phase A
 	// no shape choice made (precision is not a shape choice)
-	bool empty() const { return radices.empty() && !cta_threads && !emax && !minb && prefetch < 0; }
+	bool empty() const { return radices.empty() && !cta_threads && !emax && !minb && prefetch < 0 && pair < 0; }
 	std::string str() const;
 };
 
@@ -122,6 +127,8 @@ bool single_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch,
 void single_tables(const Schedule &s, size_t n_real, std::vector<double> &tw, std::vector<double> &roots,
                    std::vector<double> &rtw, std::vector<double> &rot);
 void radix_candidates(int n, std::vector<std::vector<int>> &out, bool real_split = false);
+// two-CTA cluster schedule of an n-point complex FP32 transform (ssfft_cl::pair)
+bool pair_schedule(int n, Schedule &s, const Knobs *knobs);
 void tc_matrix(int r0, std::vector<float> &bt);
 // autotuner (ssfft_tune.cu): picks knobs for a single-CTA plan, cached per device and shape
 ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log);

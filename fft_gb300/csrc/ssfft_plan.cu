@@ -235,6 +235,19 @@ bool choose_radices(int n, std::vector<int> &radices, bool large_composites, boo
 		const int max_radix = n >= 8192 ? 45 : radices.size() >= 4 ? 25 : 0;
 		if (max_radix && fewest_passes(a, b, c, max_radix, fewest) && cost(fewest) < cost(radices))
 			radices = fewest;
+		// a RealFFT list whose fewest passes have no radix <= 8: the same number of passes with
+		// one fusable radix (8192 = 32 32 8 instead of 32 16 16) saves the split's round trip
+		if (max_radix && real_split) {
+			struct Fz { int r, x, y, z; };
+			for (const Fz f : {Fz{8, 3, 0, 0}, Fz{4, 2, 0, 0}, Fz{6, 1, 1, 0}, Fz{5, 0, 0, 1}, Fz{3, 0, 1, 0},
+			                   Fz{2, 1, 0, 0}}) {
+				std::vector<int> sub;
+				if (f.r > fuse_radix_limit() || f.x > a || f.y > b || f.z > c) continue;
+				if (!fewest_passes(a - f.x, b - f.y, c - f.z, max_radix, sub)) continue;
+				sub.push_back(f.r);
+				if (cost(sub) < cost(radices)) radices = sub;
+			}
+		}
 	}
 	return radices.size() <= 24;
 }
@@ -302,6 +315,7 @@ std::string Knobs::str() const {
 	r += " cta=" + std::to_string(cta_threads) + " emax=" + std::to_string(emax) + " minb=" + std::to_string(minb);
 	if (prefetch >= 0) r += " prefetch=" + std::to_string(prefetch) + "/4";
 	if (precision == 1) r += " precision=split_bf16";
+	if (pair >= 0) r += " pair=" + std::to_string(pair);
 	return r;
 }
 
@@ -427,9 +441,16 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 		return e ? std::atoi(e) : 0;
 	}();
 	// Measured on GB300: forcing more resident CTAs (register caps with small spills) did not
-	// beat the compiler's own allocation for the plain kernel; the staged kernel's loop needs a
-	// cap of two CTAs.  SSFFT_MINB overrides for experiments.
+	// beat the compiler's own allocation for the plain kernel of small transforms; the staged
+	// kernel's loop needs a cap of two CTAs.  A FP32 transform holding 32 values a thread in a CTA
+	// of at most 256 threads (8192 points and up) compiles to 128-170 registers, one CTA per SM:
+	// capped at two CTAs (128 registers, no spills) it overlaps one CTA's HBM phase with the
+	// other's arithmetic (complex 8192: 51% -> 74% of the copy bandwidth).  SSFFT_MINB overrides
+	// for experiments.
 	int mb = s.staged ? 2 : 1;
+	if (!s.staged && dtype == SSFFT_F32 && s.emax == 2 * kElemsPerThread && s.per_cta * s.threads <= 256 &&
+	    2 * s.smem_bytes <= 227 * 1024)
+		mb = 2;
 	if (minb_env > 0) mb = minb_env;
 	if (knobs && knobs->minb > 0) mb = knobs->minb;
 	s.minb = std::max(1, mb);
@@ -437,6 +458,16 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 }
 
 std::string Schedule::name(bool inverse) const {
+	if (pair) {
+		auto list = [&](size_t b, size_t e) {
+			std::string l = "ssfft_cl::Radices<";
+			for (size_t i = b; i < e; ++i) l += (i > b ? ", " : "") + std::to_string(radices[i]);
+			return l + ">";
+		};
+		return "ssfft_cl::pair<float, " + std::to_string(n1) + ", " + std::to_string(n / n1) + ", " +
+		       std::to_string(threads) + ", " + (inverse ? "true" : "false") + ", " + std::to_string(emax) + ", " +
+		       std::to_string(minb) + ", " + list(0, (size_t)pair) + ", " + list((size_t)pair, radices.size()) + ">";
+	}
 	if (tc) {
 		std::string r = "ssfft_cl::batch_tc<" + std::to_string(n) + ", " + std::to_string(threads) + ", " +
 		                std::to_string(per_cta) + ", " + std::to_string(smem_stride) + ", " +
@@ -459,6 +490,25 @@ std::string Schedule::name(bool inverse) const {
 // Per-pass twiddles [pass][r-1][m] = W_{ns R}^{m r} (passes after the first) and the roots
 // W_R^k of direct passes, in the order the kernel's compile-time offsets expect.
 void schedule_twiddles(const Schedule &s, std::vector<double> &tw, std::vector<double> &roots) {
+	if (s.pair) {
+		// phase A's pass twiddles (an n1-point list), phase B's (n2 points), then the inter-phase
+		// table W_n^t = hi[t >> b] lo[t & (2^b - 1)]: lo[k] = W_n^k (k < 2^b), hi[k] = W_n^{k 2^b}
+		Schedule a = s, b = s;
+		a.pair = b.pair = 0;
+		a.radices.assign(s.radices.begin(), s.radices.begin() + s.pair);
+		b.radices.assign(s.radices.begin() + s.pair, s.radices.end());
+		schedule_twiddles(a, tw, roots);
+		schedule_twiddles(b, tw, roots);
+		const int lb = ssfft_cl::pair_lo_bits(s.n);
+		const unsigned long long lo = 1ull << lb, hi = ((unsigned long long)s.n + lo - 1) / lo;
+		for (unsigned long long k = 0; k < lo + hi; ++k) {
+			double re, im;
+			unit_root(k < lo ? k : (k - lo) * lo, (unsigned long long)s.n, &re, &im);
+			tw.push_back(re);
+			tw.push_back(im);
+		}
+		return;
+	}
 	long long ns = 1;
 	for (int R : s.radices) {
 		// register butterflies store the rows of exponents 1, 2, 4, 8 (< R) and form the other
@@ -501,6 +551,111 @@ static int kind_code(ssfft_kind kind) {
 	return kind == SSFFT_COMPLEX ? ssfft_cl::kComplex : kind == SSFFT_REAL ? ssfft_cl::kReal : ssfft_cl::kRealHalfShift;
 }
 
+// Fewest register-radix passes (radix <= max_radix) for m = 2^a 3^b 5^c.
+static bool fewest_list(int m, int max_radix, std::vector<int> &out) {
+	int a = 0, b = 0, c = 0;
+	while (m % 2 == 0) m /= 2, ++a;
+	while (m % 3 == 0) m /= 3, ++b;
+	while (m % 5 == 0) m /= 5, ++c;
+	return m == 1 && fewest_passes(a, b, c, max_radix, out);
+}
+
+// Threads of a pair CTA for phase lists (la, lb) of an n-point transform when a pass holds at
+// most emax values a thread (0 if a radix does not fit).
+static int pair_threads(int n, const std::vector<int> &la, const std::vector<int> &lb, int emax) {
+	long long t = 32;
+	for (const auto *l : {&la, &lb})
+		for (int r : *l) {
+			const int per = emax / r;
+			if (per < 1) return 0;
+			t = std::max<long long>(t, ((long long)n / 2 / r + per - 1) / per);
+		}
+	return (int)((t + 31) / 32 * 32);
+}
+
+// Values a thread holds (32, or 16 where 32 would need more than 384 threads) and threads of a
+// pair CTA; false if the lists do not fit one CTA.
+static bool pair_shape(int n, const std::vector<int> &la, const std::vector<int> &lb, const Knobs *knobs, int &emax,
+                       int &t) {
+	emax = knobs && knobs->emax > 0 ? knobs->emax : 2 * kElemsPerThread;
+	t = pair_threads(n, la, lb, emax);
+	if (!(knobs && knobs->emax > 0) && (!t || t > 384)) {
+		emax = kElemsPerThread;
+		t = pair_threads(n, la, lb, emax);
+	}
+	return t > 0 && t <= kMaxCtaThreads;
+}
+
+// The two-CTA cluster schedule of an n-point complex FP32 transform: n = n1 n2, both even, phase
+// A's radices (n1) then phase B's (n2, an even radix first).  Default split: fewest passes, then
+// few threads (at most 256, else 320), then the longer HBM segments (n1/2 and n2/2 points).  Two
+// CTAs per SM (the register cap of two CTAs: 128 registers at 256 threads).
+bool pair_schedule(int n, Schedule &s, const Knobs *knobs) {
+	std::vector<int> la, lb;
+	if (knobs && knobs->pair > 0) {
+		if ((int)knobs->radices.size() <= knobs->pair) return false;
+		la.assign(knobs->radices.begin(), knobs->radices.begin() + knobs->pair);
+		lb.assign(knobs->radices.begin() + knobs->pair, knobs->radices.end());
+	} else {
+		long long best = 1ll << 40;
+		static const int kMax[] = {32, 27, 25, 16};
+		for (int n1 = 2; n1 <= n / 2; n1 += 2) {
+			if (n % n1 || (n / n1) % 2) continue;
+			const int n2 = n / n1;
+			for (int ma : kMax)
+				for (int mb : kMax) {
+					std::vector<int> a, b;
+					if (!fewest_list(n1, ma, a) || !fewest_list(n2, mb, b)) continue;
+					auto it = std::find_if(b.begin(), b.end(), [](int r) { return r % 2 == 0; });
+					if (it == b.end()) continue;
+					std::rotate(b.begin(), it, it + 1);
+					int em, t;
+					if (!pair_shape(n, a, b, knobs, em, t)) continue;
+					const long long cost = 100000ll * (long long)(a.size() + b.size()) + (t > 256 ? 20000 : 0) +
+					                       (t > 320 ? 20000 : 0) + (em < 2 * kElemsPerThread ? 30000 : 0) -
+					                       2 * std::min(n1, n2) + (n1 > n2);
+					if (cost < best) best = cost, la = a, lb = b;
+				}
+		}
+		if (la.empty()) return false;
+	}
+	long long n1 = 1, n2 = 1;
+	for (int r : la) n1 *= r;
+	for (int r : lb) n2 *= r;
+	if (n1 * n2 != n || n1 % 2 || n2 % 2 || lb[0] % 2) return false;
+	for (int r : la)
+		if (!specialised(r) || r < 2 || r > 32) return false;
+	for (int r : lb)
+		if (!specialised(r) || r < 2 || r > 32) return false;
+	int emax, t;
+	if (!pair_shape(n, la, lb, knobs, emax, t)) return false;
+	s = Schedule();
+	s.dtype = SSFFT_F32;
+	s.n = n;
+	s.kind = ssfft_cl::kComplex;
+	s.radices = la;
+	s.radices.insert(s.radices.end(), lb.begin(), lb.end());
+	s.pair = (int)la.size();
+	s.n1 = (int)n1;
+	s.threads = t;
+	s.per_cta = 1;
+	s.emax = emax;
+	s.minb = knobs && knobs->minb > 0 ? knobs->minb : (t <= 512 ? 2 : 1);
+	s.smem_bytes = (size_t)ssfft_cl::pair_slots((int)n1, (int)n2) * 8;
+	return s.smem_bytes <= 227 * 1024;
+}
+
+// Whether the planner's default for a complex FP32 transform of n points is the two-CTA cluster
+// schedule: off (measured on GB300 slower than the one-CTA schedules at 8192-16384 points:
+// complex 16384 46-53% of the copy bandwidth against 55%, the cluster barriers and
+// distributed-shared-memory reads cost more than the second CTA per SM gains).  SSFFT_PAIR_MIN
+// sets the smallest such n for plans made while it is set.
+static bool pair_default(int n) {
+	const char *e = std::getenv("SSFFT_PAIR_MIN");
+	const long long lo = e ? std::atoll(e) : 0;
+	return lo > 0 && n >= lo;
+}
+
 // The single-CTA schedule of (n, dtype, kind, batch), or false if n needs the multi-pass path.
 bool single_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, Schedule &s, const Knobs *knobs,
                      int allow_staged, int dir) {
@@ -508,6 +663,18 @@ bool single_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch,
 	const size_t cn = real ? n / 2 : n;
 	const int max_n = dtype == SSFFT_F32 ? kMaxSubTransform : kMaxSubTransform / 2;
 	if (cn == 0 || cn > (size_t)max_n) return false;
+	if (!real && dtype == SSFFT_F32 && allow_staged != 2) {
+		// two-CTA cluster schedule: asked for, or the default for long transforms when no other
+		// shape was asked for
+		const bool asked = knobs && knobs->pair > 0;
+		const bool other = knobs && (!knobs->radices.empty() || knobs->emax || knobs->cta_threads ||
+		                             knobs->precision == 1 || knobs->pair == 0);
+		if (asked || (!other && pair_default((int)cn))) {
+			if (pair_schedule((int)cn, s, knobs)) return true;
+			if (asked) return false;
+		}
+	}
+	if (knobs && knobs->pair > 0) return false;
 	if (!make_schedule(dtype, (int)cn, kind_code(kind), real && (n & 1), batch, s, allow_staged, knobs)) return false;
 	if (dir < 0) return true;
 	// RealFFT (not half-shift), even length, plain kernel, two passes or more, a register radix
@@ -600,7 +767,8 @@ long long prefetch_distance(const Schedule &s, const Knobs &k, long long residen
 	const char *env = std::getenv("SSFFT_PREFETCH");
 	if (env && env[0] == '0') return 0;
 	const int quarters = k.prefetch >= 0 ? k.prefetch : 4;
-	return resident * quarters / 4;
+	// (cluster-pair schedules count in transforms, two CTAs each)
+	return resident * quarters / 4 / (s.pair ? 2 : 1);
 }
 
 // Whether (n, dtype, kind) runs in one CTA per transform (otherwise: multi-pass or Bluestein,
@@ -778,7 +946,7 @@ ssfft_status launch_batch_offs(const Plan *p, int inverse, const void *in, void 
 	a.spin_limit = 1u << 22;
 	a.offs = d_offs;
 	a.pf_dist = inverse ? p->main.pf_dist_inv : p->main.pf_dist;
-	const long long grid = ((long long)batch + sch.per_cta - 1) / sch.per_cta;
+	const long long grid = sch.grid((long long)batch);
 	if (grid > 0x7fffffffLL) return SSFFT_ERR_INVALID_SIZE;
 	return jit_launch(inverse ? p->main.inv : p->main.fwd, (unsigned)grid, (unsigned)sch.cta_threads(),
 	                  sch.smem_bytes, s, &a);
@@ -803,7 +971,7 @@ ssfft_status launch_batch(const Plan *p, int inverse, const void *in, void *out,
 	a.in_bytes = sch.in_bytes;
 	a.tcb = tab.tcb;
 	a.pf_dist = inverse ? p->main.pf_dist_inv : p->main.pf_dist;
-	long long grid = ((long long)batch + sch.per_cta - 1) / sch.per_cta;
+	long long grid = sch.grid((long long)batch);
 	if (sch.staged) {
 		if ((uintptr_t)in % 16) return launch_unstaged(p, inverse, in, out, batch, s);
 		grid = std::min<long long>(grid, p->main.grid_cap);
@@ -899,6 +1067,12 @@ ssfft_status ssfft_plan_create_ex(ssfft_plan_t *out, size_t n, ssfft_dtype dtype
 			return SSFFT_ERR_INVALID_VALUE;
 		}
 		if (opt->fuse_split) p->knobs.fuse = opt->fuse_split > 0 ? 1 : 0;
+		if (opt->cluster_split < -1 || opt->cluster_split > 24 ||
+		    (opt->cluster_split > 0 && (int)p->knobs.radices.size() <= opt->cluster_split)) {
+			delete p;
+			return SSFFT_ERR_INVALID_VALUE;
+		}
+		if (opt->cluster_split) p->knobs.pair = opt->cluster_split > 0 ? opt->cluster_split : 0;
 	}
 	cudaError_t e = cudaGetDevice(&p->device);
 	ssfft_status st = e == cudaSuccess ? SSFFT_SUCCESS : cuda_fail(e, "cudaGetDevice");
@@ -1084,6 +1258,7 @@ ssfft_status ssfft_schedule_options(const ssfft_plan_options *opt) {
 	for (int i = 0; i < 24 && opt->radices[i] > 0; ++i) g_diag_knobs.radices.push_back(opt->radices[i]);
 	if (!g_diag_knobs.radices.empty()) g_diag_knobs.fuse = 0;
 	if (opt->fuse_split) g_diag_knobs.fuse = opt->fuse_split > 0 ? 1 : 0;
+	if (opt->cluster_split) g_diag_knobs.pair = opt->cluster_split > 0 ? opt->cluster_split : 0;
 	return SSFFT_SUCCESS;
 }
 

@@ -49,7 +49,7 @@ std::string encode(const Knobs &k) {
 	std::string r = "r=";
 	for (size_t i = 0; i < k.radices.size(); ++i) r += (i ? "." : "") + std::to_string(k.radices[i]);
 	r += " c=" + std::to_string(k.cta_threads) + " e=" + std::to_string(k.emax) + " m=" + std::to_string(k.minb) +
-	     " p=" + std::to_string(k.precision) + " f=" + std::to_string(k.prefetch);
+	     " p=" + std::to_string(k.precision) + " f=" + std::to_string(k.prefetch) + " s=" + std::to_string(k.pair);
 	return r;
 }
 
@@ -75,6 +75,8 @@ bool decode(const std::string &txt, Knobs &k) {
 			k.precision = std::atoi(v.c_str());
 		} else if (tok[0] == 'f') {
 			k.prefetch = std::atoi(v.c_str());
+		} else if (tok[0] == 's') {
+			k.pair = std::atoi(v.c_str());
 		}
 	}
 	return true;
@@ -190,7 +192,7 @@ ssfft_status time_dir(const Plan *p, size_t tb, Scratch &sc, Candidate &c, int i
 	cudaError_t e = cudaMemcpy(sc.tab, blob.data(), total, cudaMemcpyHostToDevice);
 	if (e != cudaSuccess) return cuda_fail(e, "tune tables copy");
 	const unsigned char *base = static_cast<const unsigned char *>(sc.tab);
-	const long long grid = ((long long)tb + sch.per_cta - 1) / sch.per_cta;
+	const long long grid = sch.grid((long long)tb);
 	{
 		ssfft_cl::Args a;
 		std::memset(&a, 0, sizeof a);
@@ -302,6 +304,30 @@ ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log) 
 		return SSFFT_SUCCESS;
 	};
 
+	{
+		// a two-CTA cluster default against the single-CTA schedules; if the cluster schedule
+		// wins, only its register cap (two or three CTAs per SM) is tuned further
+		Schedule d0;
+		if (single_schedule(p->n, p->dtype, p->kind, tb, d0, &best, 0) && d0.pair) {
+			std::vector<Candidate> cs(2);
+			cs[0].knobs = best;
+			cs[1].knobs = best;
+			cs[1].knobs.pair = 0;
+			ssfft_status st = run_stage(cs);
+			if (st != SSFFT_SUCCESS) return st;
+			if (best.pair != 0) {
+				std::vector<Candidate> cm(2);
+				cm[0].knobs = best;
+				cm[1].knobs = best;
+				cm[1].knobs.minb = d0.minb + 1;
+				st = run_stage(cm);
+				if (st != SSFFT_SUCCESS) return st;
+				std::lock_guard<std::mutex> lock(g_cache_mu);
+				store_locked(key, best);
+				return SSFFT_SUCCESS;
+			}
+		}
+	}
 	if (level >= 2) {
 		std::vector<std::vector<int>> lists;
 		radix_candidates(cn, lists, p->kind == SSFFT_REAL && !(p->n & 1));
@@ -352,14 +378,20 @@ ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log) 
 		if (st != SSFFT_SUCCESS) return st;
 	}
 	if (level >= 2) {
-		// register caps: enough CTAs per SM for at most 48 or 40 registers a thread (more warps
-		// in flight hide the first pass's HBM latency, if the caps do not force spills)
+		// register caps: enough CTAs per SM for at most 128 ... 40 registers a thread (more CTAs
+		// in flight overlap one CTA's HBM phase with another's arithmetic, if the caps do not
+		// force spills), as far as shared memory and the SM's 2048 threads allow
 		Schedule cur;
 		if (single_schedule(p->n, p->dtype, p->kind, tb, cur, &best, 0)) {
 			std::vector<Candidate> cs;
-			for (int regs : {48, 40}) {
+			const int by_smem = cur.smem_bytes ? (int)((227 * 1024) / cur.smem_bytes) : 32;
+			const int by_threads = 2048 / cur.cta_threads();
+			std::vector<int> seen{cur.minb};
+			for (int regs : {128, 96, 64, 48, 40}) {
 				const int m = 65536 / (cur.cta_threads() * regs);
-				if (m < 2 || m > 32) continue;
+				if (m < 2 || m > 32 || m > by_smem || m > by_threads) continue;
+				if (std::find(seen.begin(), seen.end(), m) != seen.end()) continue;
+				seen.push_back(m);
 				Candidate c;
 				c.knobs = best;
 				c.knobs.minb = m;

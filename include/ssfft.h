@@ -94,6 +94,10 @@ typedef struct ssfft_plan_options {
                                  * resident CTAs: 0 = planner default (4: one wave), -1 = off */
     int fuse_split;        /* RealFFT split fused into the last forward / first inverse pass:
                             * 0 planner default (from 256 reals), 1 wherever possible, -1 never */
+    int cluster_split;     /* complex FP32 transforms run by a cluster of two CTAs (four-step inside
+                            * the cluster, half a transform per CTA): 0 planner default (off),
+                            * -1 never, k > 0 with `radices` given: its first k radices are the
+                            * first phase (their product n1 and n / n1 both even) */
 } ssfft_plan_options;
 /* SSFFT_PRECISION_SPLIT_BF16 (complex FP32 plans that run in one CTA): the first radix pass
  * (radix <= 16) runs as tensor-core matrix products (tcgen05) on FP32 values split into three

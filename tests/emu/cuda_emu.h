@@ -15,6 +15,7 @@
 #define __global__
 #define __forceinline__ inline
 #define __launch_bounds__(...)
+#define __cluster_dims__(...)
 #define __shared__
 #define __align__(x)
 

@@ -1,5 +1,8 @@
 // tests/emu/emu_main.cpp -- runs one emulated kernel launch.  Compiled together with a generated
-// case table (emu_cases.inc: `{name, &ssfft_cl::batch<...>, cta_threads, smem_bytes},` lines).
+// case table (emu_cases.inc: `{name, &ssfft_cl::batch<...>, cta_threads, smem_bytes[, cluster]},`
+// lines).  Cluster kernels (cluster = 2) run their two CTAs at once, each with its own
+// shared-memory array; reads of a CTA's shared memory through the cluster window are
+// bounds-checked.
 // argv: case index, grid, raw input file, raw output file (pre-filled), table file, batch,
 //       in_dist, out_dist (scalars), scalar bytes, input bytes per transform (staged kernels).
 // The table file holds tw, roots, rtw, rot back to back in the kernel's dtype, preceded by four
@@ -17,8 +20,21 @@
 thread_local EmuIdx threadIdx, blockIdx, gridDim;
 thread_local std::barrier<> *emu_barrier;
 std::atomic<int> emu_or_acc{0};
+static size_t emu_smem_bytes = 0;
 namespace ssfft_cl {
 alignas(1024) unsigned char smem_raw[232 * 1024];
+thread_local unsigned char *emu_cta_smem = nullptr, *emu_peer_smem = nullptr;
+thread_local std::barrier<> *emu_cluster_barrier = nullptr;
+float2 emu_cluster_load(ClusterSmem s, int i) {
+	const unsigned char *p = reinterpret_cast<const unsigned char *>(s.base + i);
+	const bool own = p >= emu_cta_smem && p + sizeof(float2) <= emu_cta_smem + emu_smem_bytes;
+	const bool peer = p >= emu_peer_smem && p + sizeof(float2) <= emu_peer_smem + emu_smem_bytes;
+	if (i < 0 || !(own || peer)) {
+		std::fprintf(stderr, "cluster shared-memory read out of bounds: index %d\n", i);
+		std::abort();
+	}
+	return s.base[i];
+}
 float emu_tmem[128][32];
 // BF16 round to nearest even (finite inputs) and widening
 unsigned short f2bf(float x) {
@@ -40,6 +56,7 @@ struct Case {
 	void (*fn)(const ssfft_cl::Args);
 	int cta_threads;
 	size_t smem;
+	int cluster;  // 0 / 1: one CTA at a time; 2: two CTAs of a cluster at once
 };
 static const Case kCases[] = {
 #include "emu_cases.inc"
@@ -74,6 +91,40 @@ int main(int argc, char **argv) {
 	a.in_bytes = (unsigned)std::atoi(argv[10]);
 	// tensor-core kernels: the first pass's DFT matrix follows the four tables when present
 	a.tcb = reinterpret_cast<const float *>(base + (cnt[0] + cnt[1] + cnt[2] + cnt[3]) * sb);
+	if (c.cluster == 2) {
+		emu_smem_bytes = c.smem;
+		for (int b = 0; b + 1 < grid; b += 2) {
+			// guard bytes around each CTA's array, checked afterwards (writes out of bounds)
+			constexpr size_t kGuard = 4096;
+			std::vector<unsigned char> sm[2] = {std::vector<unsigned char>(c.smem + 2 * kGuard, 0xA5),
+			                                    std::vector<unsigned char>(c.smem + 2 * kGuard, 0xA5)};
+			std::barrier<> cbar(2 * c.cta_threads), bar0(c.cta_threads), bar1(c.cta_threads);
+			std::vector<std::thread> th;
+			for (int q = 0; q < 2; ++q)
+				for (int t = 0; t < c.cta_threads; ++t)
+					th.emplace_back([&, t, q] {
+						threadIdx.x = (unsigned)t;
+						blockIdx.x = (unsigned)(b + q);
+						gridDim.x = (unsigned)grid;
+						emu_barrier = q ? &bar1 : &bar0;
+						ssfft_cl::emu_cluster_barrier = &cbar;
+						ssfft_cl::emu_cta_smem = sm[q].data() + kGuard;
+						ssfft_cl::emu_peer_smem = sm[1 - q].data() + kGuard;
+						c.fn(a);
+					});
+			for (auto &x : th) x.join();
+			for (int q = 0; q < 2; ++q)
+				for (size_t i = 0; i < kGuard; ++i)
+					if (sm[q][i] != 0xA5 || sm[q][kGuard + c.smem + i] != 0xA5) {
+						std::fprintf(stderr, "shared-memory write outside the CTA's %zu bytes\n", c.smem);
+						return 4;
+					}
+		}
+		if (err) return 3;
+		std::ofstream f(argv[4], std::ios::binary);
+		f.write(out.data(), (std::streamsize)out.size());
+		return 0;
+	}
 	for (int b = 0; b < grid; ++b) {
 		std::barrier<> bar(c.cta_threads);
 		std::vector<std::thread> th;

@@ -47,6 +47,13 @@ TC_CASES = [(64, "f32", "complex", 40, 40), (1920, "f32", "complex", 3, 3), (16,
             (112, "f32", "complex", 5, 5), (7, "f32", "complex", 130, 130), (4096, "f32", "complex", 1, 1),
             (480, "f32", "complex", 9, 9), (3, "f32", "complex", 1, 1)]
 TC_TOL = 2e-6
+# two-CTA cluster (pair) schedules: (n, plan batch, exec batch, radices, phase-A radix count);
+# the default complex cases above of 8192+ points run the bulk-copy kernel.
+PAIR_CASES = [(16384, 1, 1, [16, 8, 16, 8], 2), (12288, 2, 2, [32, 16, 24], 1), (9216, 1, 1, [16, 6, 12, 8], 2),
+              (15360, 1, 1, [8, 15, 16, 8], 2), (8192, 3, 3, [8, 16, 4, 16], 2), (4000, 2, 2, [10, 20, 20], 1)]
+VARIANTS = {"default": {"fuse_split": 1}, "tc": {"precision": "split_bf16"}}
+for _c in PAIR_CASES:
+    VARIANTS[f"pair{_c[0]}"] = ({"cluster_split": _c[4], "radices": _c[3]} if _c[3] else {})
 
 
 def tc_matrix(r0):
@@ -81,17 +88,20 @@ def emulator(staged_schedules, tmp_path_factory):
     d = tmp_path_factory.mktemp("emu")
     lines = []
     index = {}
-    for case, tc in [(c, False) for c in CASES] + [(c, True) for c in TC_CASES]:
+    cases = [(c, "default") for c in CASES] + [(c, "tc") for c in TC_CASES]
+    cases += [((c[0], "f32", "complex", c[1], c[2]), f"pair{c[0]}") for c in PAIR_CASES]
+    for case, var in cases:
         (n, dt, kind, pb, _) = case
-        F.schedule_options(**({"precision": "split_bf16"} if tc else {"fuse_split": 1}))
+        F.schedule_options(**VARIANTS[var])
         for inv in (False, True):
             # a RealFFT plan may run a different radix order per direction (fused split)
             F.schedule_direction(inv)
             info = F.schedule_info(n, dt, kind, pb)
             name = F.schedule_name(n, dt, kind, pb, inv)
-            index[(n, dt, kind, pb, inv, tc)] = (len(lines), info)
+            index[(n, dt, kind, pb, inv, var)] = (len(lines), info)
+            cluster = 2 if name.startswith("ssfft_cl::pair<") else 1
             lines.append(f'{{"{n}-{dt}-{kind}-{int(inv)}", &{name}, {info["threads"] * info["per_cta"]}, '
-                         f'{info["smem_bytes"]}}},')
+                         f'{info["smem_bytes"]}, {cluster}}},')
         F.schedule_options()
         F.schedule_direction(False)
     (d / "emu_cases.inc").write_text("\n".join(lines) + "\n")
@@ -103,10 +113,11 @@ def emulator(staged_schedules, tmp_path_factory):
     return exe, index, d
 
 
-def _run(emulator, n, dt, kind, pb, eb, inv, x, tc=False):
+def _run(emulator, n, dt, kind, pb, eb, inv, x, tc=False, var=None):
     exe, index, d = emulator
-    ci, info = index[(n, dt, kind, pb, inv, tc)]
-    F.schedule_options(**({"precision": "split_bf16"} if tc else {"fuse_split": 1}))
+    var = var or ("tc" if tc else "default")
+    ci, info = index[(n, dt, kind, pb, inv, var)]
+    F.schedule_options(**VARIANTS[var])
     F.schedule_direction(inv)
     sdt = np.float32 if dt == "f32" else np.float64
     real = kind != "complex"
@@ -132,8 +143,9 @@ def _run(emulator, n, dt, kind, pb, eb, inv, x, tc=False):
     fo.write_bytes(out.tobytes())
     ft.write_bytes(blob)
     groups = -(-eb // info["per_cta"])
-    # persistent (staged) kernels: fewer CTAs than groups, so each CTA walks several groups
-    grid = max(1, groups // 2) if "batch_staged" in name else groups
+    # persistent (staged) kernels: fewer CTAs than groups, so each CTA walks several groups;
+    # cluster (pair) kernels: two CTAs per transform
+    grid = max(1, groups // 2) if "batch_staged" in name else 2 * eb if name.startswith("ssfft_cl::pair<") else groups
     in_bytes = in_dist * np.dtype(sdt).itemsize
     subprocess.run([str(exe), str(ci), str(grid), str(fi), str(fo), str(ft), str(eb), str(in_dist), str(out_dist),
                     str(np.dtype(sdt).itemsize), str(in_bytes)], check=True, timeout=300)
@@ -182,3 +194,21 @@ def test_emulated_tensor_core_kernel_matches_oracle(emulator, case):
         got = _run(emulator, n, dt, kind, pb, eb, inv, x, tc=True).view(np.complex64)
         ref = np.stack([oracle.fft(r.astype(np.complex128), inv) for r in x])
         assert rel_l2(got, ref) <= TC_TOL, (inv, rel_l2(got, ref))
+
+
+@pytest.mark.parametrize("case", PAIR_CASES, ids=lambda c: f"pair-{c[0]}")
+def test_emulated_pair_kernel_matches_oracle(emulator, case):
+    """Two-CTA cluster kernel: both CTAs of a cluster run at once, the second phase reads half of
+    each row from the other CTA's shared memory."""
+    n, pb, eb, rad, split = case
+    var = f"pair{n}"
+    F.schedule_options(**VARIANTS[var])
+    name = F.schedule_name(n, "f32", "complex", pb)
+    F.schedule_options()
+    assert name.startswith("ssfft_cl::pair<"), name
+    rng = np.random.default_rng(n * 13)
+    x = (rng.uniform(-1, 1, (eb, n)) + 1j * rng.uniform(-1, 1, (eb, n))).astype(np.complex64)
+    for inv in (False, True):
+        got = _run(emulator, n, "f32", "complex", pb, eb, inv, x, var=var).view(np.complex64)
+        ref = np.stack([oracle.fft(r.astype(np.complex128), inv) for r in x])
+        assert rel_l2(got, ref) <= 1e-6, (inv, rel_l2(got, ref))
