@@ -106,6 +106,7 @@ struct Plan {
 	LargePlan *large = nullptr;
 	HostStage *stage = nullptr;
 	Knobs knobs;              // schedule choices in force (explicit or tuned)
+	Knobs knobs_inv;          // the inverse's (equal to knobs unless the autotuner chose apart)
 	std::string tune_log;     // candidates the autotuner timed when this plan was made
 	int autotune = 0;         // 0 off, 1 quick (threads / CTA shape), 2 full (also radix order)
 	std::mutex stage_mutex;
@@ -131,7 +132,7 @@ void radix_candidates(int n, std::vector<std::vector<int>> &out, bool real_split
 bool pair_schedule(int n, Schedule &s, const Knobs *knobs);
 void tc_matrix(int r0, std::vector<float> &bt);
 // autotuner (ssfft_tune.cu): picks knobs for a single-CTA plan, cached per device and shape
-ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log);
+ssfft_status autotune_single(Plan *p, int level, Knobs &best, Knobs &best_inv, std::string &log);
 // prefetch distance in CTAs for a schedule with `resident` CTAs on the GPU at once
 long long prefetch_distance(const Schedule &s, const Knobs &k, long long resident);
 long long resident_ctas(CUfunction fwd, CUfunction inv, const Schedule &s, int device);

@@ -233,7 +233,13 @@ bool choose_radices(int n, std::vector<int> &radices, bool large_composites, boo
 	};
 	if (large_composites && rest.empty()) {
 		const int max_radix = n >= 8192 ? 45 : radices.size() >= 4 ? 25 : 0;
-		if (max_radix && fewest_passes(a, b, c, max_radix, fewest) && cost(fewest) < cost(radices))
+		// (below 8192 points a RealFFT tie between a four-pass fusable list and three passes plus
+		// the split goes to the three passes: RealFFT 15360 16-24-20 46% of the copy bandwidth,
+		// 8-8-15-8 fused 42%; at 16384 points the fused four passes measured 2-4% faster)
+		const bool tie_to_fewest = real_split && radices.size() >= 4 && n < 8192;
+		if (max_radix && fewest_passes(a, b, c, max_radix, fewest) &&
+		    (cost(fewest) < cost(radices) || (tie_to_fewest && cost(fewest) == cost(radices) &&
+		                                      fewest.size() < radices.size())))
 			radices = fewest;
 		// a RealFFT list whose fewest passes have no radix <= 8: the same number of passes with
 		// one fusable radix (8192 = 32 32 8 instead of 32 16 16) saves the split's round trip
@@ -247,6 +253,14 @@ bool choose_radices(int n, std::vector<int> &radices, bool large_composites, boo
 				sub.push_back(f.r);
 				if (cost(sub) < cost(radices)) radices = sub;
 			}
+		}
+		// three passes from 8192 points (radices <= 32): the smallest radix in the middle
+		// (measured on GB300, complex 16384 32-16-32 58.7% of the copy bandwidth against 55.4%
+		// for 32-32-16, 10000 25-16-25 2-3% faster than 16-25-25; 15360 40-16-24 was slower than
+		// 16-40-24)
+		if (n >= 8192 && !real_split && radices.size() == 3 && *std::max_element(radices.begin(), radices.end()) <= 32) {
+			std::sort(radices.begin(), radices.end());
+			radices = {radices[2], radices[0], radices[1]};
 		}
 	}
 	return radices.size() <= 24;
@@ -787,19 +801,22 @@ static ssfft_status plan_build_single(Plan *p) {
 	Schedule &s = p->main.sch;
 	// the default schedule decides whether n runs in one CTA; explicit or tuned knobs refine it
 	if (!plan_single_cta(p->n, p->dtype, p->kind)) return SSFFT_ERR_UNSUPPORTED;
+	p->knobs_inv = p->knobs;
 	if (p->autotune > 0 && p->knobs.empty()) {
-		Knobs best;
-		ssfft_status st = autotune_single(p, p->autotune, best, p->tune_log);
+		Knobs best, best_inv;
+		ssfft_status st = autotune_single(p, p->autotune, best, best_inv, p->tune_log);
 		if (st != SSFFT_SUCCESS) return st;
 		p->knobs = best;
+		p->knobs_inv = best_inv;
 	}
 	Schedule &si = p->main.sch_inv;
 	if (!single_schedule(p->n, p->dtype, p->kind, p->batch, s, &p->knobs, 1, 0) ||
-	    !single_schedule(p->n, p->dtype, p->kind, p->batch, si, &p->knobs, 1, 1))
+	    !single_schedule(p->n, p->dtype, p->kind, p->batch, si, &p->knobs_inv, 1, 1))
 		return SSFFT_ERR_INVALID_VALUE;  // explicit knobs that do not fit this size
 	const size_t smem_limit = device_smem_limit(p->device);
 	if (s.smem_bytes > smem_limit || si.smem_bytes > smem_limit) return SSFFT_ERR_UNSUPPORTED;
-	const bool split = si.radices != s.radices;  // inverse has its own pass tables
+	// the inverse has its own pass tables when its passes differ
+	const bool split = si.radices != s.radices || si.pair != s.pair;
 	std::vector<double> tw, roots, rtw, rot, tw_i, roots_i, unused_rtw, unused_rot;
 	single_tables(s, p->n, tw, roots, rtw, rot);
 	if (split) single_tables(si, p->n, tw_i, roots_i, unused_rtw, unused_rot);
@@ -851,7 +868,7 @@ static ssfft_status plan_build_single(Plan *p) {
 		const long long resident_i = resident_ctas(fns[1], fns[1], si, p->device);
 		if (s.staged) p->main.grid_cap = (int)std::min(resident, resident_i);
 		p->main.pf_dist = prefetch_distance(s, p->knobs, resident);
-		p->main.pf_dist_inv = prefetch_distance(si, p->knobs, resident_i);
+		p->main.pf_dist_inv = prefetch_distance(si, p->knobs_inv, resident_i);
 	}
 	p->launches_per_exec = 1;
 	return SSFFT_SUCCESS;
@@ -1098,7 +1115,9 @@ ssfft_status ssfft_plan_tuning(ssfft_plan_t plan, char *choice, size_t choice_le
 		std::memcpy(dst, src.data(), k);
 		dst[k] = 0;
 	};
-	put(p->large ? std::string("multi-pass") : p->knobs.str(), choice, choice_len);
+	std::string ch = p->knobs.str();
+	if (p->knobs_inv.str() != ch) ch += " | inverse: " + p->knobs_inv.str();
+	put(p->large ? std::string("multi-pass") : ch, choice, choice_len);
 	put(p->tune_log, log, log_len);
 	return SSFFT_SUCCESS;
 }

@@ -7,7 +7,10 @@
 //   level 2: radix order (the planner's list, its permutations, the alternative grouping);
 //   level 1 and 2: values per thread {8, 16, 32}, then CTA size {32, 64, 128, 256, 512};
 //   level 2: L2 prefetch distance (1/2, 1, 2 waves of resident CTAs), then register caps
-//   (launch bounds for at most 48 or 40 registers a thread).
+//   (launch bounds for at most 128 ... 40 registers a thread, as shared memory allows);
+//   a default two-CTA cluster schedule is first timed against the one-CTA schedules.
+// Every candidate runs in both directions; the stages follow the joint (forward + inverse)
+// time, and the plan takes the fastest forward and the fastest inverse candidate seen.
 // Candidates of one stage compile concurrently (NVRTC), and are timed one at a time under a
 // process-wide lock so concurrent plan creations do not disturb each other's timings.  The
 // winner is cached per (device name, kernel source, n, dtype, kind, batch range, level) in memory
@@ -238,9 +241,10 @@ ssfft_status time_one(const Plan *p, size_t tb, Scratch &sc, Candidate &c) {
 
 }  // namespace
 
-ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log) {
+ssfft_status autotune_single(Plan *p, int level, Knobs &best, Knobs &best_inv, std::string &log) {
 	best = Knobs();
 	best.precision = p->knobs.precision;
+	best_inv = best;
 	log.clear();
 	const bool real = p->kind != SSFFT_COMPLEX;
 	const int cn = (int)(real ? p->n / 2 : p->n);
@@ -260,6 +264,8 @@ ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log) 
 		auto it = g_cache.find(key);
 		if (it != g_cache.end()) {
 			best = it->second;
+			auto ii = g_cache.find(key + "|inverse");
+			best_inv = ii != g_cache.end() ? ii->second : best;
 			return SSFFT_SUCCESS;
 		}
 	}
@@ -276,7 +282,17 @@ ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log) 
 	if (e == cudaSuccess) e = cudaEventCreate(&sc.ev[1]);
 	if (e != cudaSuccess) return cuda_fail(e, "tune scratch");
 
-	std::map<std::string, double> timed;  // kernel name -> total us (identical schedules are timed once)
+	// kernel names -> forward and inverse us (identical schedules are timed once)
+	std::map<std::string, std::pair<double, double>> timed;
+	// every candidate is timed in both directions: besides the joint choice that steers the
+	// stages, the fastest forward and the fastest inverse seen are kept (a RealFFT inverse often
+	// prefers another register cap or CTA shape than its forward)
+	double best_f = 1e300, best_i = 1e300;
+	Knobs kf = best, ki = best;
+	auto note = [&](const Candidate &c) {
+		if (c.fwd_us < best_f) best_f = c.fwd_us, kf = c.knobs;
+		if (c.inv_us < best_i) best_i = c.inv_us, ki = c.knobs;
+	};
 	auto run_stage = [&](std::vector<Candidate> &cs) -> ssfft_status {
 		compile_all(p, tb, cs);
 		std::lock_guard<std::mutex> lock(g_time_mu);
@@ -285,13 +301,14 @@ ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log) 
 			const std::string nm = c.sch.name(false) + "|" + c.sch_inv.name(true) + "|pf" + std::to_string(c.knobs.prefetch);
 			auto it = timed.find(nm);
 			if (it != timed.end()) {
-				c.fwd_us = it->second;
-				c.inv_us = 0;
+				c.fwd_us = it->second.first;
+				c.inv_us = it->second.second;
 				continue;
 			}
 			ssfft_status st = time_one(p, tb, sc, c);
 			if (st != SSFFT_SUCCESS) return st;
-			timed[nm] = c.total();
+			timed[nm] = {c.fwd_us, c.inv_us};
+			note(c);
 			char line[256];
 			std::snprintf(line, sizeof line, "%s threads=%dx%d fwd=%.2fus inv=%.2fus\n", c.knobs.str().c_str(),
 			              c.sch.threads, c.sch.per_cta, c.fwd_us, c.inv_us);
@@ -323,7 +340,10 @@ ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log) 
 				st = run_stage(cm);
 				if (st != SSFFT_SUCCESS) return st;
 				std::lock_guard<std::mutex> lock(g_cache_mu);
-				store_locked(key, best);
+				store_locked(key, kf);
+				store_locked(key + "|inverse", ki);
+				best = kf;
+				best_inv = ki;
 				return SSFFT_SUCCESS;
 			}
 		}
@@ -407,7 +427,10 @@ ssfft_status autotune_single(Plan *p, int level, Knobs &best, std::string &log) 
 		}
 	}
 	std::lock_guard<std::mutex> lock(g_cache_mu);
-	store_locked(key, best);
+	store_locked(key, kf);
+	store_locked(key + "|inverse", ki);
+	best = kf;
+	best_inv = ki;
 	return SSFFT_SUCCESS;
 }
 

@@ -115,3 +115,33 @@ def test_fused_split_on_and_off(F, n, fuse):
     """The RealFFT split fused into the last forward / first inverse pass (mirror-paired
     butterflies, odd and even unit counts) and the unfused kernels give the oracle's result."""
     _real_case(F, n, 33, fuse_split=fuse)
+
+
+@pytest.mark.parametrize("n,kind,batch", [(2048, "real", 8192), (1024, "real", 8192), (16384, "complex", 512),
+                                          (3840, "real", 4096)])
+def test_autotuned_directions_match_oracle(F, n, kind, batch):
+    """The tuner keeps the fastest forward and the fastest inverse candidate (the two directions may
+    run different shapes and register caps): both directions and a round trip against the oracle."""
+    import torch
+    p = F.Plan(n, "f32", kind, batch, autotune=2)
+    rng = np.random.default_rng(n)
+    if kind == "complex":
+        x = (rng.uniform(-1, 1, (batch, n)) + 1j * rng.uniform(-1, 1, (batch, n))).astype(np.complex64)
+        xi = torch.from_numpy(x).cuda()
+        y = torch.empty_like(xi)
+        z = torch.empty_like(xi)
+    else:
+        x = rng.standard_normal((batch, n)).astype(np.float32)
+        xi = torch.from_numpy(x).cuda()
+        y = torch.empty((batch, n // 2), dtype=torch.complex64, device="cuda")
+        z = torch.empty_like(xi)
+    p.exec(False, xi.data_ptr(), y.data_ptr(), 0)
+    p.exec(True, y.data_ptr(), z.data_ptr(), 0)
+    torch.cuda.synchronize()
+    ys = y[:32].cpu().numpy()
+    ref = oracle.batch(x[:32].astype(np.float64 if kind == "real" else np.complex128), n, real=kind == "real",
+                       inverse=False)
+    assert rel_l2(ys, ref) <= F32_TOL
+    refi = oracle.batch(ref, n, real=kind == "real", inverse=True)
+    assert rel_l2(z[:32].cpu().numpy(), refi) <= F32_TOL
+    assert rel_l2(z[:32].cpu().numpy() / n, x[:32]) <= F32_TOL
