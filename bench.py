@@ -49,9 +49,15 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the host-buffer leg (default: steps/10)")
     ap.add_argument("--workload", default="realfft",
-                    choices=["realfft", "fp64", "large", "serve", "uneven", "precision"],
+                    choices=["realfft", "fp64", "large", "serve", "uneven", "precision", "sizes"],
                     help="realfft: the batched RealFFT<float> line (default); fp64: FFT<double> N=1024 x256; "
-                         "large: single FP32 transforms of 2^24, 3^15, 2^12 3^4 5^2; serve: request serving sweep")
+                         "large: single FP32 transforms of 2^24, 3^15, 2^12 3^4 5^2; serve: request serving sweep; "
+                         "sizes: per-size batched FP32 kernel sweep (--sizes, --kinds, --sweep-mb, --plan-options)")
+    ap.add_argument("--sizes", default="256,512,1024,2048,4096,8192,16384",
+                    help="sizes workload: comma-separated transform lengths")
+    ap.add_argument("--kinds", default="complex,real", help="sizes workload: complex and/or real")
+    ap.add_argument("--sweep-mb", type=int, default=512, help="sizes workload: MiB of input + output per launch")
+    ap.add_argument("--plan-options", default="{}", help="sizes workload: JSON keyword options of fft_gb300.Plan")
     ap.add_argument("--serve-duration", type=float, default=3.0)
     ap.add_argument("--tune", type=int, default=2, choices=[0, 1, 2],
                     help="autotune level of the plans (0 planner defaults, 1 CTA shape, 2 also radix order)")
@@ -604,6 +610,44 @@ def run_precision(args):
                       "peak_GB_s": peak, "peak_source": kind, **out}), flush=True)
 
 
+def run_sizes(args):
+    """Per-size kernel sweep: batched FP32 transforms (complex and/or real) of each size, sized to
+    --sweep-mb MiB of algorithmic traffic per launch (larger than L2), forward and inverse timed
+    with CUDA events over 10 back-to-back launches each.  One JSON line per (size, kind)."""
+    import torch
+    import fft_gb300 as F
+    peak, kind_src = measured_peak_hbm()
+    opts = json.loads(args.plan_options)
+    sh = int(torch.cuda.current_stream().cuda_stream)
+    for kind in args.kinds.split(","):
+        for n in (int(v) for v in args.sizes.split(",")):
+            per = 16 * n if kind == "complex" else 8 * n  # algorithmic bytes per transform / frame
+            batch = max(1, (args.sweep_mb << 20) // per)
+            try:
+                p = F.Plan(n, "f32", kind, batch, **opts)  # planner defaults unless --plan-options says
+            except Exception as e:  # a size / option combination the planner refuses
+                print(json.dumps({"n": n, "kind": kind, "error": str(e)}), flush=True)
+                continue
+            if kind == "complex":
+                x = torch.randn(batch, n, dtype=torch.complex64, device="cuda")
+                y = torch.empty_like(x)
+            else:
+                x = torch.randn(batch, n, device="cuda")
+                y = torch.empty(batch, n // 2, dtype=torch.complex64, device="cuda")
+            res = {}
+            for inv, (a, b) in ((False, (x, y)), (True, (y, x))):
+                t = _time_device(lambda: p.exec(inv, a.data_ptr(), b.data_ptr(), sh), 10, 3)
+                res["inverse" if inv else "forward"] = {"us": round(t * 1e6, 1),
+                                                        "GB_s": round(batch * per / t / 1e9),
+                                                        "frac": round(batch * per / t / 1e9 / peak, 3)}
+            d = p.describe()
+            print(json.dumps({"n": n, "kind": kind, "batch": batch, **res, "peak_GB_s": peak, "peak_source": kind_src,
+                              "radices": d["radices"], "threads": d["threads"], "per_cta": d["per_cta"],
+                              "schedule": p.tuning()["choice"]}), flush=True)
+            del x, y, p
+            torch.cuda.empty_cache()
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -616,7 +660,7 @@ def main():
         fb.build()
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         {"fp64": run_fp64, "large": run_large, "serve": run_serve, "uneven": run_uneven,
-         "precision": run_precision}[args.workload](args)
+         "precision": run_precision, "sizes": run_sizes}[args.workload](args)
     else:
         run_gpu(args, rank, world if "WORLD_SIZE" in os.environ else 1)
 

@@ -521,30 +521,37 @@ __device__ __forceinline__ void gstore(const Ctx<T, KIND, CIN, COUT> &c, int e, 
 
 // ------------------------------------------------------------------ one pass
 
-// Twiddle rows stored for a pass of radix R: exponents 1, 2, 4, 8, 16 (< R) for the register
-// butterflies, 1..R-1 for the direct passes.
-template <int R>
+// Twiddle rows stored for a pass of radix R: FP32 register butterflies store exponents 1, 2, 4, 8,
+// 16 (< R); FP64 passes (bound by FP64 arithmetic, not memory) and direct passes store every
+// exponent 1..R-1.
+template <typename T, int R>
 struct TwRows {
-	static constexpr int value =
-	    Specialised<R>::value ? (R > 32 ? 6 : R > 16 ? 5 : R > 8 ? 4 : R > 4 ? 3 : R > 2 ? 2 : 1) : R - 1;
+	static constexpr bool kPow2 = Specialised<R>::value && sizeof(T) == 4;
+	static constexpr int value = kPow2 ? (R > 32 ? 6 : R > 16 ? 5 : R > 8 ? 4 : R > 4 ? 3 : R > 2 ? 2 : 1) : R - 1;
 };
 
-// v[r] *= W_{NS R}^{m r}: rows W^{m}, W^{2m}, W^{4m}, W^{8m}, W^{16m} are loaded, the other powers
-// are products w_r = w_{r - lowbit(r)} * w_{lowbit(r)} (at most 4 products deep); a quarter to a
-// half of the twiddle loads, which were most of the L1 traffic.
+// v[r] *= W_{NS R}^{m r}.  FP32: rows W^{m}, W^{2m}, W^{4m}, W^{8m}, W^{16m} are loaded, the other
+// powers are products w_r = w_{r - lowbit(r)} * w_{lowbit(r)} (at most 4 products deep): a quarter
+// to a half of the twiddle loads, which were most of the L1 traffic of the memory-bound FP32
+// kernels.  FP64: every power is loaded (the products would cost FP64 arithmetic, the bound).
 template <typename T, int R, int NS, int TWO>
 __device__ __forceinline__ void apply_twiddles(typename Cx<T>::C (&v)[R], const typename Cx<T>::C *tw, int m) {
 	using C = typename Cx<T>::C;
-	C pw[TwRows<R>::value];
+	if constexpr (!TwRows<T, R>::kPow2) {
 #pragma unroll
-	for (int b = 0; b < TwRows<R>::value; ++b) pw[b] = __ldg(tw + TWO + b * NS + m);
-	C w[R];
+		for (int r = 1; r < R; ++r) v[r] = mul(v[r], __ldg(tw + TWO + (r - 1) * NS + m));
+	} else {
+		C pw[TwRows<T, R>::value];
 #pragma unroll
-	for (int r = 1; r < R; ++r) {
-		const int lb = r & -r;
-		const int b = lb == 1 ? 0 : lb == 2 ? 1 : lb == 4 ? 2 : lb == 8 ? 3 : lb == 16 ? 4 : 5;
-		w[r] = r == lb ? pw[b] : mul(w[r - lb], pw[b]);
-		v[r] = mul(v[r], w[r]);
+		for (int b = 0; b < TwRows<T, R>::value; ++b) pw[b] = __ldg(tw + TWO + b * NS + m);
+		C w[R];
+#pragma unroll
+		for (int r = 1; r < R; ++r) {
+			const int lb = r & -r;
+			const int b = lb == 1 ? 0 : lb == 2 ? 1 : lb == 4 ? 2 : lb == 8 ? 3 : lb == 16 ? 4 : 5;
+			w[r] = r == lb ? pw[b] : mul(w[r - lb], pw[b]);
+			v[r] = mul(v[r], w[r]);
+		}
 	}
 }
 
@@ -640,9 +647,9 @@ __device__ __forceinline__ void pass(const Ctx<T, KIND, CIN, COUT> &c, const typ
 // Twiddle slots used by a pass of radix R after NS points (none for the first pass): rows of
 // the exponents 1, 2, 4, 8 below R for register butterflies, every exponent 1..R-1 for direct
 // passes.
-template <int R, int NS>
+template <typename T, int R, int NS>
 struct TwCount {
-	static constexpr int value = NS > 1 ? NS * TwRows<R>::value : 0;
+	static constexpr int value = NS > 1 ? NS * TwRows<T, R>::value : 0;
 };
 template <int R>
 struct RootCount {
@@ -831,7 +838,7 @@ __device__ __forceinline__ void passes(const Ctx<T, KIND, CIN, COUT> &c, const t
 	else pass<T, N, THREADS, R, NS, TWO, ROOTS, SRC, DST, KIND, CIN, COUT, ODD, EMAX>(c, tw, roots);
 	if constexpr (NS == 1) after_first();
 	if constexpr (!last)
-		passes<T, N, THREADS, NS * R, TWO + TwCount<R, NS>::value, ROOTS + RootCount<R>::value, FIRST_SRC, LAST_DST,
+		passes<T, N, THREADS, NS * R, TWO + TwCount<T, R, NS>::value, ROOTS + RootCount<R>::value, FIRST_SRC, LAST_DST,
 		       KIND, CIN, COUT, ODD, EMAX, Rest...>(c, tw, roots, NoHook());
 }
 
@@ -1640,7 +1647,7 @@ struct TwTotal {
 };
 template <int NS, int R, int... Rs>
 struct TwTotal<NS, R, Rs...> {
-	static constexpr int value = TwCount<R, NS>::value + TwTotal<NS * R, Rs...>::value;
+	static constexpr int value = TwCount<float, R, NS>::value + TwTotal<NS * R, Rs...>::value;
 };
 template <class L>
 struct RadixList;
@@ -1837,7 +1844,7 @@ __device__ __forceinline__ void pair_passes(const PairCtx<T> &c, const typename 
 	if constexpr (B) pair_b_pass<T, N1, N2, THREADS, INV, EMAX, R, NS, TWO, FIRST, LAST>(c, tw);
 	else pair_a_pass<T, N1, N2, THREADS, INV, EMAX, R, NS, TWO, FIRST, LAST>(c, tw);
 	if constexpr (!LAST)
-		pair_passes<T, N1, N2, THREADS, INV, EMAX, B, NS * R, TWO + TwCount<R, NS>::value, Rest...>(c, tw);
+		pair_passes<T, N1, N2, THREADS, INV, EMAX, B, NS * R, TWO + TwCount<T, R, NS>::value, Rest...>(c, tw);
 }
 template <class L>
 struct PairPhase;

@@ -525,10 +525,10 @@ void schedule_twiddles(const Schedule &s, std::vector<double> &tw, std::vector<d
 	}
 	long long ns = 1;
 	for (int R : s.radices) {
-		// register butterflies store the rows of exponents 1, 2, 4, 8 (< R) and form the other
-		// powers by products; direct passes store every exponent 1..R-1
+		// FP32 register butterflies store the rows of exponents 1, 2, 4, 8, 16 (< R) and form the
+		// other powers by products; FP64 passes and direct passes store every exponent 1..R-1
 		std::vector<int> exps;
-		if (specialised(R))
+		if (specialised(R) && s.dtype == SSFFT_F32)
 			for (int e = 1; e < R; e *= 2) exps.push_back(e);
 		else
 			for (int r = 1; r < R; ++r) exps.push_back(r);
