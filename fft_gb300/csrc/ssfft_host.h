@@ -83,7 +83,7 @@ struct LargePlan;
 
 // Buffers and streams for ssfft_exec_host's copy/compute pipeline.
 struct HostStage {
-	static constexpr int kStreams = 3;
+	static constexpr int kStreams = 4;  // at most; three by default
 	cudaStream_t stream[kStreams] = {};
 	void *d_in[kStreams] = {};
 	void *d_out[kStreams] = {};

@@ -40,17 +40,24 @@ void plan_release(Plan *p) {
 	if (prev >= 0) cudaSetDevice(prev);
 }
 
-// Chunk of ~16 MiB of input per stream (at least one transform).
+// Chunk of ~32 MiB of input per stream (at least one transform), three streams (measured on
+// GB300 with the RealFFT headline frames: 16 MiB 1027-1037, 32-96 MiB 1050-1074 GFLOP/s end to
+// end, 4-8 MiB 861-968; a fourth stream no better).  Experiment switches, read when a plan first
+// runs on host buffers: SSFFT_STAGE_MB (chunk MiB), SSFFT_STAGE_STREAMS (1..4).
 static ssfft_status stage_init(Plan *p) {
 	if (p->stage) return SSFFT_SUCCESS;
 	HostStage *st = new HostStage();
 	const size_t per_in = std::max(plan_in_bytes(p, 0, 1), plan_in_bytes(p, 1, 1));
 	const size_t per_out = std::max(plan_out_bytes(p, 0, 1), plan_out_bytes(p, 1, 1));
-	size_t chunk = std::max<size_t>(1, (16u << 20) / std::max<size_t>(per_in, 1));
+	const char *mb_env = std::getenv("SSFFT_STAGE_MB");
+	const size_t mb = mb_env && std::atoi(mb_env) > 0 ? (size_t)std::atoi(mb_env) : 32;
+	size_t chunk = std::max<size_t>(1, (mb << 20) / std::max<size_t>(per_in, 1));
 	chunk = std::min(chunk, p->batch);
 	st->chunk = chunk;
+	const char *ns_env = std::getenv("SSFFT_STAGE_STREAMS");
+	const int ns = ns_env && std::atoi(ns_env) > 0 ? std::min(HostStage::kStreams, std::atoi(ns_env)) : 3;
 	// multi-pass plans share one scratch buffer, so their chunks run on a single stream
-	st->streams = p->large ? 1 : HostStage::kStreams;
+	st->streams = p->large ? 1 : ns;
 	for (int i = 0; i < st->streams; ++i) {
 		cudaError_t e = cudaStreamCreateWithFlags(&st->stream[i], cudaStreamNonBlocking);
 		if (e == cudaSuccess) e = cudaMalloc(&st->d_in[i], per_in * chunk);
