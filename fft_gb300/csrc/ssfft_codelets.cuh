@@ -673,16 +673,22 @@ struct NoHook {
 // with the reference's formulas; the self-paired bin H/2 gets the reference's surviving write.
 
 // Forward split of the pair (i, H - i), 1 <= i <= H/2, from Z[i] and Z[H - i].
+// (w = rtw[i], loaded by the caller ahead of its stores)
 template <typename T, int H>
-__device__ __forceinline__ void split_pair(typename Cx<T>::C *out, const typename Cx<T>::C *rtw, int i,
-                                           typename Cx<T>::C zi, typename Cx<T>::C zci) {
+__device__ __forceinline__ void split_pair_w(typename Cx<T>::C *out, int i, typename Cx<T>::C w, typename Cx<T>::C zi,
+                                             typename Cx<T>::C zci) {
 	using C = typename Cx<T>::C;
 	const C zc = conj(zci);
 	const C odd = scale(add(zi, zc), T(0.5));
 	const C even = scale(sub(zi, zc), T(0.5));
-	const C e = mul(even, __ldg(rtw + i));
+	const C e = mul(even, w);
 	if (2 * i != H) __stcs(out + i, add(odd, e));
 	__stcs(out + (H - i), conj(sub(odd, e)));
+}
+template <typename T, int H>
+__device__ __forceinline__ void split_pair(typename Cx<T>::C *out, const typename Cx<T>::C *rtw, int i,
+                                           typename Cx<T>::C zi, typename Cx<T>::C zci) {
+	split_pair_w<T, H>(out, i, __ldg(rtw + i), zi, zci);
 }
 
 // Inverse pre-twiddle of the pair (i, H - i), 1 <= i <= H/2: the (conjugated) first-pass inputs
@@ -733,11 +739,20 @@ __device__ __forceinline__ void pass_last_r2c(const Ctx<T, KIND, CIN, COUT> &c, 
 		if (c.valid && u < U) {
 			const int j1 = u, j2 = u == 0 ? NS / 2 : NS - u;
 			const bool has2 = u != 0 || NS % 2 == 0;
-			C v1[R], v2[R];
+			C v1[R], v2[R], w[R];
 #pragma unroll
 			for (int r = 0; r < R; ++r) {
 				v1[r] = c.sm[pidx<PS>(j1 + r * NS)];
 				v2[r] = has2 ? c.sm[pidx<PS>(j2 + r * NS)] : v1[r];
+			}
+			// the split twiddles of the pairs, loaded ahead of the stores (which could alias them
+			// as far as the compiler can tell)
+			if (u != 0) {
+#pragma unroll
+				for (int r = 0; r < R; ++r) {
+					const int k = j1 + r * NS, mk = H - k;
+					w[r] = __ldg(c.rtw + (k < mk ? k : mk));
+				}
 			}
 			if constexpr (NS > 1) {
 				apply_twiddles<T, R, NS, TWO>(v1, tw, j1);
@@ -749,8 +764,8 @@ __device__ __forceinline__ void pass_last_r2c(const Ctx<T, KIND, CIN, COUT> &c, 
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
 					const int k = j1 + r * NS, mk = H - k;
-					if (k < mk) split_pair<T, H>(out, c.rtw, k, v1[r], v2[R - 1 - r]);
-					else split_pair<T, H>(out, c.rtw, mk, v2[R - 1 - r], v1[r]);
+					if (k < mk) split_pair_w<T, H>(out, k, w[r], v1[r], v2[R - 1 - r]);
+					else split_pair_w<T, H>(out, mk, w[r], v2[R - 1 - r], v1[r]);
 				}
 			} else {
 				split_self<T, H, R, NS>(out, c.rtw, 0, v1);
@@ -792,31 +807,41 @@ __device__ __forceinline__ void pass_first_c2r(const Ctx<T, KIND, CIN, COUT> &c)
 	constexpr int NB = H / R, U = (NB + 1) / 2, UPT = (U + THREADS - 1) / THREADS;
 	static_assert(Specialised<R>::value && NB * R == H, "fused pre-twiddle needs a register butterfly first");
 	const C *in = reinterpret_cast<const C *>(c.gin);
+	// every unit's HBM loads first: the shared-memory stores could alias them as far as the
+	// compiler can tell, which would otherwise serialise one HBM round trip per unit
+	C v1[UPT][R], v2[UPT][R];
+#pragma unroll
+	for (int q = 0; q < UPT; ++q) {
+		const int u = c.t + q * THREADS;
+		if (c.valid && u < U) {
+			const int j1 = u;
+			const bool has2 = u != 0 || NB % 2 == 0;
+			if (u != 0) {
+#pragma unroll
+				for (int r = 0; r < R; ++r) {
+					const int k = j1 + r * NB, mk = H - k;
+					if (k < mk) pretwiddle_pair<T, H>(in, c.rtw, k, v1[q][r], v2[q][R - 1 - r]);
+					else pretwiddle_pair<T, H>(in, c.rtw, mk, v2[q][R - 1 - r], v1[q][r]);
+				}
+			} else {
+				pretwiddle_self<T, H, R, NB>(in, c.rtw, 0, v1[q]);
+				if (has2) pretwiddle_self<T, H, R, NB>(in, c.rtw, NB / 2, v2[q]);
+			}
+		}
+	}
 #pragma unroll
 	for (int q = 0; q < UPT; ++q) {
 		const int u = c.t + q * THREADS;
 		if (c.valid && u < U) {
 			const int j1 = u, j2 = u == 0 ? NB / 2 : NB - u;
 			const bool has2 = u != 0 || NB % 2 == 0;
-			C v1[R], v2[R];
-			if (u != 0) {
+			dft<R>(v1[q]);
 #pragma unroll
-				for (int r = 0; r < R; ++r) {
-					const int k = j1 + r * NB, mk = H - k;
-					if (k < mk) pretwiddle_pair<T, H>(in, c.rtw, k, v1[r], v2[R - 1 - r]);
-					else pretwiddle_pair<T, H>(in, c.rtw, mk, v2[R - 1 - r], v1[r]);
-				}
-			} else {
-				pretwiddle_self<T, H, R, NB>(in, c.rtw, 0, v1);
-				if (has2) pretwiddle_self<T, H, R, NB>(in, c.rtw, NB / 2, v2);
-			}
-			dft<R>(v1);
-#pragma unroll
-			for (int r = 0; r < R; ++r) c.sm[pidx<PS>(j1 * R + r)] = v1[r];
+			for (int r = 0; r < R; ++r) c.sm[pidx<PS>(j1 * R + r)] = v1[q][r];
 			if (has2) {
-				dft<R>(v2);
+				dft<R>(v2[q]);
 #pragma unroll
-				for (int r = 0; r < R; ++r) c.sm[pidx<PS>(j2 * R + r)] = v2[r];
+				for (int r = 0; r < R; ++r) c.sm[pidx<PS>(j2 * R + r)] = v2[q][r];
 			}
 		}
 	}
@@ -859,25 +884,41 @@ __device__ __forceinline__ void real_post(const Ctx<T, KIND, CIN, COUT> &c, cons
 	constexpr int PS = Cx<T>::kPadShift;
 	constexpr bool MOD = KIND == kRealHalfShift;
 	constexpr int S = MOD ? 0 : 1, LAST = H / 2, NPAIRS = LAST - S + 1;
+	constexpr int PPT = NPAIRS > THREADS ? (NPAIRS + THREADS - 1) / THREADS : 1;  // pairs a thread takes
 	C *out = reinterpret_cast<C *>(c.gout);
 	if (!c.valid) return;
 	if (!MOD && c.t == 0) {
 		const C z0 = c.sm[0];
 		__stcs(out, mkc(z0.x + z0.y, z0.x - z0.y));
 	}
-#pragma unroll 4
-	for (int p = c.t; p < NPAIRS; p += THREADS) {
-		const int i = S + p;
-		const int ci = MOD ? H - 1 - i : H - i;
-		const C zi = c.sm[pidx<PS>(i)];
-		const C zc = conj(c.sm[pidx<PS>(ci)]);
-		const C odd = scale(add(zi, zc), T(0.5));
-		const C even = scale(sub(zi, zc), T(0.5));
-		const C e = mul(even, __ldg(rtw + i));
-		bool wi, wci;
-		pair_writes(i, ci, S, LAST, wi, wci);
-		if (wi) __stcs(out + i, add(odd, e));
-		if (wci) __stcs(out + ci, conj(sub(odd, e)));
+	// every load of the thread first: the stores below could alias them as far as the compiler
+	// can tell, which would otherwise serialise the pairs
+	C zi[PPT], zc[PPT], w[PPT];
+#pragma unroll
+	for (int q = 0; q < PPT; ++q) {
+		const int p = c.t + q * THREADS;
+		if (p < NPAIRS) {
+			const int i = S + p;
+			const int ci = MOD ? H - 1 - i : H - i;
+			zi[q] = c.sm[pidx<PS>(i)];
+			zc[q] = conj(c.sm[pidx<PS>(ci)]);
+			w[q] = __ldg(rtw + i);
+		}
+	}
+#pragma unroll
+	for (int q = 0; q < PPT; ++q) {
+		const int p = c.t + q * THREADS;
+		if (p < NPAIRS) {
+			const int i = S + p;
+			const int ci = MOD ? H - 1 - i : H - i;
+			const C odd = scale(add(zi[q], zc[q]), T(0.5));
+			const C even = scale(sub(zi[q], zc[q]), T(0.5));
+			const C e = mul(even, w[q]);
+			bool wi, wci;
+			pair_writes(i, ci, S, LAST, wi, wci);
+			if (wi) __stcs(out + i, add(odd, e));
+			if (wci) __stcs(out + ci, conj(sub(odd, e)));
+		}
 	}
 }
 
@@ -889,25 +930,39 @@ __device__ __forceinline__ void real_pre(const Ctx<T, KIND, CIN, COUT> &c, const
 	constexpr int PS = Cx<T>::kPadShift;
 	constexpr bool MOD = KIND == kRealHalfShift;
 	constexpr int S = MOD ? 0 : 1, LAST = H / 2, NPAIRS = LAST - S + 1;
+	constexpr int PPT = NPAIRS > THREADS ? (NPAIRS + THREADS - 1) / THREADS : 1;  // pairs a thread takes
 	const C *in = STAGED ? c.st : reinterpret_cast<const C *>(c.gin);
 	if (c.valid) {
-		if (!MOD && c.t == 0) {
-			const C v = STAGED ? in[0] : __ldcs(in);
-			c.sm[0] = conj(mkc(v.x + v.y, v.x - v.y));
+		// every HBM load of the thread first: the shared-memory stores below could alias them as
+		// far as the compiler can tell, which would otherwise serialise one HBM round trip per pair
+		C v[PPT], v2c[PPT], w[PPT], v0;
+		if (!MOD && c.t == 0) v0 = STAGED ? in[0] : __ldcs(in);
+#pragma unroll
+		for (int q = 0; q < PPT; ++q) {
+			const int p = c.t + q * THREADS;
+			if (p < NPAIRS) {
+				const int i = S + p;
+				const int ci = MOD ? H - 1 - i : H - i;
+				v[q] = STAGED ? in[i] : __ldcs(in + i);
+				v2c[q] = conj(STAGED ? in[ci] : __ldcs(in + ci));
+				w[q] = __ldg(rtw + i);
+			}
 		}
-#pragma unroll 4
-		for (int p = c.t; p < NPAIRS; p += THREADS) {
-			const int i = S + p;
-			const int ci = MOD ? H - 1 - i : H - i;
-			const C v = STAGED ? in[i] : __ldcs(in + i);
-			const C v2c = conj(STAGED ? in[ci] : __ldcs(in + ci));
-			const C odd = add(v, v2c);
-			const C even = mulc(sub(v, v2c), __ldg(rtw + i));
-			bool wi, wci;
-			pair_writes(i, ci, S, LAST, wi, wci);
-			// stored conjugated: the passes run forward on conj(data)
-			if (wi) c.sm[pidx<PS>(i)] = conj(add(odd, even));
-			if (wci) c.sm[pidx<PS>(ci)] = sub(odd, even);
+		if (!MOD && c.t == 0) c.sm[0] = conj(mkc(v0.x + v0.y, v0.x - v0.y));
+#pragma unroll
+		for (int q = 0; q < PPT; ++q) {
+			const int p = c.t + q * THREADS;
+			if (p < NPAIRS) {
+				const int i = S + p;
+				const int ci = MOD ? H - 1 - i : H - i;
+				const C odd = add(v[q], v2c[q]);
+				const C even = mulc(sub(v[q], v2c[q]), w[q]);
+				bool wi, wci;
+				pair_writes(i, ci, S, LAST, wi, wci);
+				// stored conjugated: the passes run forward on conj(data)
+				if (wi) c.sm[pidx<PS>(i)] = conj(add(odd, even));
+				if (wci) c.sm[pidx<PS>(ci)] = sub(odd, even);
+			}
 		}
 	}
 	__syncthreads();
@@ -1580,17 +1635,27 @@ __global__ void __launch_bounds__(THREADS *G) strided(const StridedArgs a) {
 		}
 	}
 	if constexpr (SLOAD) {
-		// G-element segments: consecutive threads take consecutive u0 of the same element
-#pragma unroll 4
-		for (int idx = threadIdx.x; idx < G * N; idx += CTA) {
+		// G-element segments: consecutive threads take consecutive u0 of the same element.  Every
+		// HBM load of the thread is issued before its shared-memory stores (interleaved, each
+		// store waited for its load: one HBM round trip per element)
+		constexpr int IT = (G * N + CTA - 1) / CTA;
+		C v[IT];
+#pragma unroll
+		for (int q = 0; q < IT; ++q) {
+			const int idx = threadIdx.x + q * CTA;
 			const int gg = idx % G, e = idx / G;
-			if (u00 + gg < a.U0) {
+			if (idx < G * N && u00 + gg < a.U0) {
 				const long long off = ib + (u00 + gg) * a.is0 + (long long)e * a.in_es;
-				C v = __ldcs(in + off);
-				if constexpr (CIN) v = conj(v);
-				if constexpr (ROT == 1) v = mul(v, __ldg(c.rot + (off - u2 * a.rot_in_stride2)));
-				sm_all[gg * STRIDE + pidx<PS>(e)] = v;
+				v[q] = __ldcs(in + off);
+				if constexpr (CIN) v[q] = conj(v[q]);
+				if constexpr (ROT == 1) v[q] = mul(v[q], __ldg(c.rot + (off - u2 * a.rot_in_stride2)));
 			}
+		}
+#pragma unroll
+		for (int q = 0; q < IT; ++q) {
+			const int idx = threadIdx.x + q * CTA;
+			const int gg = idx % G, e = idx / G;
+			if (idx < G * N && u00 + gg < a.U0) sm_all[gg * STRIDE + pidx<PS>(e)] = v[q];
 		}
 		__syncthreads();
 	}

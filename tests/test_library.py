@@ -62,6 +62,17 @@ def test_plan_kernels_compile_for_sm103a(n, dt, kind, batch):
     assert F.jit_check(n, dt, kind, batch, "sm_103a") > 0
 
 
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 6, 7, 8, 9, 12, 30, 98, 512])
+def test_small_and_odd_kernels_compile_for_sm103a(n):
+    """Degenerate shapes (a single bin, no split pairs, odd real lengths, direct passes) compile
+    under NVRTC too: it refuses constructs the host compiler accepts (zero-length arrays)."""
+    for dt in ("f32", "f64"):
+        for kind in ("complex", "real", "real_halfshift"):
+            if kind != "complex" and n < 2:
+                continue
+            assert F.jit_check(n, dt, kind, 3, "sm_103a") > 0, (n, dt, kind)
+
+
 @pytest.mark.parametrize("n, dt, kind", [(1024, "f32", "complex"), (3840, "f32", "real"), (1024, "f64", "complex")])
 def test_staged_kernels_compile_for_sm103a(n, dt, kind, monkeypatch):
     """The bulk-copy staged variant (opt-in) and the failure-detection launch use it."""
