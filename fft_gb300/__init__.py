@@ -259,7 +259,13 @@ def jit_check(n: int, dtype="f32", kind="complex", batch: int = 1, arch: str = "
 # ------------------------------------------------------------------ plans
 
 class Plan:
-    """One ``ssfft_plan_t``: ``batch`` transforms of size ``n`` (complex or real)."""
+    """One ``ssfft_plan_t``: ``batch`` transforms of size ``n`` (complex or real).
+
+    Keyword options map onto ``ssfft_plan_options`` (0 = planner default): ``autotune`` (1, 2),
+    ``radices`` (explicit pass order), ``cta_threads``, ``values_per_thread``,
+    ``min_ctas_per_sm`` (register cap), ``precision`` ("fp32" / "split_bf16"),
+    ``prefetch_quarter_waves``, ``fuse_split`` (1 / -1) and ``cluster_split`` (-1 never, k > 0
+    with ``radices``: the first k radices as the first phase of the two-CTA cluster kernel)."""
 
     def __init__(self, n: int, dtype="f32", kind="complex", batch: int = 1, *, autotune: int = 0, radices=None,
                  cta_threads: int = 0, values_per_thread: int = 0, min_ctas_per_sm: int = 0, precision="fp32",
