@@ -465,6 +465,13 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	if (!s.staged && dtype == SSFFT_F32 && s.emax == 2 * kElemsPerThread && s.per_cta * s.threads <= 256 &&
 	    2 * s.smem_bytes <= 227 * 1024)
 		mb = 2;
+	// One transform of 16 values a thread per 256-thread CTA (2304-4096 complex points, RealFFT
+	// 4608-8192): the compiler's 72 registers leave 3 CTAs per SM; capped at 5 (51 registers, a
+	// few bytes of spills) more CTAs overlap their HBM phases (complex 4096 83% -> 88% of the copy
+	// bandwidth, RealFFT 8192 67% -> 72%; caps of 7 or more spill heavily).
+	if (!s.staged && !s.tc && dtype == SSFFT_F32 && s.emax == kElemsPerThread && s.per_cta == 1 &&
+	    s.threads == 256 && 5 * s.smem_bytes <= 227 * 1024)
+		mb = 5;
 	if (minb_env > 0) mb = minb_env;
 	if (knobs && knobs->minb > 0) mb = knobs->minb;
 	s.minb = std::max(1, mb);
