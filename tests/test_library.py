@@ -90,3 +90,41 @@ def test_schedules_respect_register_and_thread_budget():
         assert info["smem_bytes"] <= 227 * 1024
         r = info["radices"]
         assert int(np.prod(r)) == n
+
+
+def _minb(name: str) -> int:
+    # batch<T, N, THREADS, PER_CTA, STRIDE, KIND, INV, ODD, EMAX, MINB, FUSE, radices...>
+    return int(name.split("<", 1)[1].split(", ")[9])
+
+
+def test_planner_policies_for_long_and_mid_transforms(monkeypatch):
+    """The measured planner rules stay in force: register caps of two CTAs per SM (32 values a
+    thread, <= 256 threads) and of five CTAs per SM (16 values, one transform per 256-thread CTA),
+    fusable RealFFT lists, the smallest radix in the middle of long three-pass lists, and the
+    cluster kernel off unless asked for."""
+    assert _minb(F.schedule_name(8192, "f32", "complex", 4096)) == 2
+    assert _minb(F.schedule_name(4096, "f32", "complex", 4096)) == 5
+    assert _minb(F.schedule_name(8192, "f32", "real", 4096)) == 5
+    assert _minb(F.schedule_name(2048, "f32", "complex", 4096)) == 1  # 128-thread CTAs: no cap
+    assert _minb(F.schedule_name(4096, "f64", "complex", 4096)) == 1  # FP64: no cap
+    assert F.schedule_info(16384, "f32", "real", 64)["radices"] == [32, 32, 8]
+    assert ", true, 32, 32, 8>" in F.schedule_name(16384, "f32", "real", 64)  # split fused
+    assert F.schedule_info(16384, "f32", "complex", 64)["radices"] == [32, 16, 32]
+    assert F.schedule_info(15360, "f32", "real", 64)["radices"] == [16, 24, 20]
+    # the headline RealFFT schedules
+    assert F.schedule_info(3840, "f32", "real", 16384)["radices"] == [16, 15, 8]
+    assert F.schedule_info(480, "f32", "real", 16384)["radices"] == [16, 15]
+    assert not F.schedule_name(16384, "f32", "complex", 64).startswith("ssfft_cl::pair<")
+    monkeypatch.setenv("SSFFT_PAIR_MIN", "8193")
+    assert F.schedule_name(16384, "f32", "complex", 64).startswith("ssfft_cl::pair<")
+    assert not F.schedule_name(8192, "f32", "complex", 64).startswith("ssfft_cl::pair<")
+
+
+def test_fp64_tables_hold_every_twiddle_power():
+    """FP64 passes load every power W^m .. W^{(R-1)m} (their bound is FP64 arithmetic); FP32
+    register butterflies store the power-of-two rows and form the rest by products."""
+    assert F.schedule_info(1024, "f64", "complex", 1)["radices"] == [16, 8, 8]
+    assert F.schedule_info(1024, "f32", "complex", 1)["radices"] == [16, 8, 8]
+    # passes 2 and 3 (radix 8 after 16 and 128 points): 7 rows (FP64) or 3 rows (FP32)
+    assert F.schedule_tables(1024, "f64", "complex", 1)["tw"].size == 2 * 7 * (16 + 128)
+    assert F.schedule_tables(1024, "f32", "complex", 1)["tw"].size == 2 * 3 * (16 + 128)
