@@ -248,6 +248,22 @@ def diag_staged_timeout(n: int = 1024, spin_limit: int = 1000) -> int:
     return flags.value
 
 
+def large_spec(n: int, dtype="f32", kind="complex") -> tuple:
+    """The multi-pass plan of n points (no GPU): (launch records as a dict, table bytes)."""
+    import json as _json
+    nb = _sz()
+    l = lib()
+    l.ssfft_diag_large_spec.argtypes = [_sz, _int, _int, ctypes.c_char_p, _sz, _vp, ctypes.POINTER(_sz)]
+    l.ssfft_diag_large_spec.restype = _int
+    buf = ctypes.create_string_buffer(1 << 16)
+    check(l.ssfft_diag_large_spec(n, _dtype_code(dtype), _kind_code(kind), buf, 1 << 16, None, ctypes.byref(nb)),
+          f"large_spec(n={n})")
+    blob = (ctypes.c_ubyte * nb.value)()
+    check(l.ssfft_diag_large_spec(n, _dtype_code(dtype), _kind_code(kind), None, 0, ctypes.cast(blob, _vp),
+                                  ctypes.byref(nb)), f"large_spec(n={n})")
+    return _json.loads(buf.value.decode()), bytes(blob)
+
+
 def jit_check(n: int, dtype="f32", kind="complex", batch: int = 1, arch: str = "sm_103a") -> int:
     """Compile (no GPU needed) the kernels a plan would use; returns the cubin size."""
     nbytes = _sz()

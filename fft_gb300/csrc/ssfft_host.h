@@ -167,5 +167,7 @@ ssfft_status launch_large(Plan *p, int inverse, const void *in, void *out, size_
 void large_release(LargePlan *lp);
 ssfft_status large_jit_check(size_t n, ssfft_dtype dtype, ssfft_kind kind, const char *arch, size_t *image_bytes);
 bool large_describe(size_t n, ssfft_dtype dtype, ssfft_kind kind, std::vector<long long> &F);
+ssfft_status large_spec(size_t n, ssfft_dtype dtype, ssfft_kind kind, std::string &json,
+                        std::vector<unsigned char> &blob);
 
 }  // namespace ssfft

@@ -395,31 +395,28 @@ static ssfft_status launch_bluestein(LargePlan *lp, ssfft_dtype dtype, const voi
 	return st;
 }
 
-ssfft_status plan_build_large(Plan *p) {
-	LargePlan *lp = new LargePlan();
-	p->large = lp;
-	LargeTables tabs;
-	ssfft_status st0 = large_schedule(p->n, p->dtype, p->kind, device_smem_limit(p->device), lp, tabs);
-	if (st0 != SSFFT_SUCCESS) return st0;
-	if (lp->M) return plan_build_bluestein(p, lp);
+// The pass tables of a multi-pass plan in one blob (pass twiddles, roots and the two-level
+// inter-pass twiddles of every pass, then the real split twiddles and half-shift rotations), in
+// the plan's dtype; sets the offsets in *lp.
+static void large_blob(LargePlan *lp, LargeTables &tabs, size_t n, ssfft_dtype dtype, std::vector<unsigned char> &blob) {
 	const bool real = lp->real;
 	const long long N = lp->N;
 	const int P = (int)lp->pass.size();
-	const size_t eb = p->dtype == SSFFT_F32 ? 8 : 16, sb = eb / 2;
+	const size_t eb = dtype == SSFFT_F32 ? 8 : 16, sb = eb / 2;
 	auto &tw = tabs.tw, &roots = tabs.roots, &twlo = tabs.twlo, &twhi = tabs.twhi;
 	std::vector<double> rtw, rot;
 	if (real) {
 		for (long long i = 0; i <= N / 2; ++i) {
 			double re, im;
-			if (lp->modified) unit_root(2 * i + 1, 2 * (unsigned long long)p->n, &re, &im);
-			else unit_root(i, p->n, &re, &im);
+			if (lp->modified) unit_root(2 * i + 1, 2 * (unsigned long long)n, &re, &im);
+			else unit_root(i, n, &re, &im);
 			rtw.push_back(im);
 			rtw.push_back(-re);
 		}
 		if (lp->modified)
 			for (long long i = 0; i < N; ++i) {
 				double re, im;
-				unit_root(i, p->n, &re, &im);
+				unit_root(i, n, &re, &im);
 				rot.push_back(re);
 				rot.push_back(im);
 			}
@@ -441,7 +438,7 @@ ssfft_status plan_build_large(Plan *p) {
 	off = align_up(off + rtw.size() * sb, 256);
 	lp->off_rot = off;
 	off = align_up(off + rot.size() * sb, 256);
-	std::vector<unsigned char> blob(std::max<size_t>(off, 256), 0);
+	blob.assign(std::max<size_t>(off, 256), 0);
 	for (int i = 0; i < P; ++i) {
 		const LargePass &ps = lp->pass[i];
 		if (sb == 4) {
@@ -463,6 +460,21 @@ ssfft_status plan_build_large(Plan *p) {
 		put<double>(blob, lp->off_rtw, rtw);
 		put<double>(blob, lp->off_rot, rot);
 	}
+}
+
+ssfft_status plan_build_large(Plan *p) {
+	LargePlan *lp = new LargePlan();
+	p->large = lp;
+	LargeTables tabs;
+	ssfft_status st0 = large_schedule(p->n, p->dtype, p->kind, device_smem_limit(p->device), lp, tabs);
+	if (st0 != SSFFT_SUCCESS) return st0;
+	if (lp->M) return plan_build_bluestein(p, lp);
+	const bool real = lp->real;
+	const long long N = lp->N;
+	const int P = (int)lp->pass.size();
+	const size_t eb = p->dtype == SSFFT_F32 ? 8 : 16;
+	std::vector<unsigned char> blob;
+	large_blob(lp, tabs, p->n, p->dtype, blob);
 	cudaError_t e = cudaMalloc(&lp->d_tables, blob.size());
 	if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(large tables)");
 	e = cudaMemcpy(lp->d_tables, blob.data(), blob.size(), cudaMemcpyHostToDevice);
@@ -573,6 +585,40 @@ ssfft_status launch_large(Plan *p, int inverse, const void *in, void *out, size_
 			if (st != SSFFT_SUCCESS) return st;
 		}
 	}
+	return SSFFT_SUCCESS;
+}
+
+// The multi-pass plan of n points as launch records (no GPU needed): a JSON object with the
+// passes' kernel names (forward, inverse), CTA shape, shared memory, groups and StridedArgs
+// strides and table offsets, and the table blob the passes read.  Bluestein lengths are refused.
+ssfft_status large_spec(size_t n, ssfft_dtype dtype, ssfft_kind kind, std::string &json,
+                        std::vector<unsigned char> &blob) {
+	LargePlan lp;
+	LargeTables t;
+	ssfft_status st = large_schedule(n, dtype, kind, 227 * 1024, &lp, t);
+	if (st != SSFFT_SUCCESS) return st;
+	if (lp.M) return SSFFT_ERR_UNSUPPORTED;
+	large_blob(&lp, t, n, dtype, blob);
+	const std::vector<std::string> names = large_kernel_names(&lp, dtype);
+	auto num = [](long long v) { return std::to_string(v); };
+	json = "{\"N\": " + num(lp.N) + ", \"real\": " + num(lp.real) + ", \"modified\": " + num(lp.modified) +
+	       ", \"off_rtw\": " + num((long long)lp.off_rtw) + ", \"off_rot\": " + num((long long)lp.off_rot) +
+	       ", \"passes\": [";
+	for (size_t i = 0; i < lp.pass.size(); ++i) {
+		const LargePass &ps = lp.pass[i];
+		json += std::string(i ? ", " : "") + "{\"fwd\": \"" + names[2 * i] + "\", \"inv\": \"" + names[2 * i + 1] +
+		        "\", \"cta\": " + num(ps.sub.cta_threads()) + ", \"smem\": " + num((long long)ps.sub.smem_bytes) +
+		        ", \"G\": " + num(ps.sub.per_cta) + ", \"U0\": " + num(ps.U0) + ", \"U1\": " + num(ps.U1) +
+		        ", \"is0\": " + num(ps.is0) + ", \"is1\": " + num(ps.is1) + ", \"in_es\": " + num(ps.in_es) +
+		        ", \"os0\": " + num(ps.os0) + ", \"os1\": " + num(ps.os1) + ", \"out_es\": " + num(ps.out_es) +
+		        ", \"off_tw\": " + num((long long)ps.off_tw) + ", \"off_roots\": " + num((long long)ps.off_roots) +
+		        ", \"off_twlo\": " + num((long long)ps.off_twlo) + ", \"off_twhi\": " + num((long long)ps.off_twhi) +
+		        "}";
+	}
+	json += "]";
+	if (lp.real) json += ", \"split_fwd\": \"" + names[2 * lp.pass.size()] + "\", \"split_inv\": \"" +
+		                  names[2 * lp.pass.size() + 1] + "\"";
+	json += "}";
 	return SSFFT_SUCCESS;
 }
 

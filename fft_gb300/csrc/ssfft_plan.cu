@@ -1337,6 +1337,25 @@ ssfft_status ssfft_jit_check(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_
 	return jit_compile_only({s.name(false), si.name(true)}, arch ? arch : "sm_103a", image_bytes);
 }
 
+ssfft_status ssfft_diag_large_spec(size_t n, ssfft_dtype dtype, ssfft_kind kind, char *json, size_t json_len,
+                                   void *blob, size_t *blob_bytes) {
+	if (!blob_bytes) return SSFFT_ERR_INVALID_VALUE;
+	std::string j;
+	std::vector<unsigned char> b;
+	const ssfft_status st = large_spec(n, dtype, kind, j, b);
+	if (st != SSFFT_SUCCESS) return st;
+	if (json && json_len) {
+		if (j.size() + 1 > json_len) return SSFFT_ERR_INVALID_VALUE;
+		std::memcpy(json, j.c_str(), j.size() + 1);
+	}
+	if (blob) {
+		if (*blob_bytes < b.size()) return SSFFT_ERR_INVALID_VALUE;
+		std::memcpy(blob, b.data(), b.size());
+	}
+	*blob_bytes = b.size();
+	return SSFFT_SUCCESS;
+}
+
 ssfft_status ssfft_schedule_info(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, int *radices, int cap,
                                  int *npasses, int *threads, int *per_cta, size_t *smem_bytes) {
 	Schedule s;

@@ -1,0 +1,104 @@
+// tests/emu/emu_strided_main.cpp -- runs one emulated launch of a multi-pass (four-step) pass
+// kernel, ssfft_cl::strided.  Compiled together with a generated case table
+// (emu_strided_cases.inc: `{name, &ssfft_cl::strided<...>, cta_threads, smem_bytes},` lines).
+// argv: case index, grid, raw input file, raw output file (pre-filled), table file (the plan's
+//       table bytes), transforms (U2), complex points per transform (the u2 strides), then U0,
+//       U1, is0, is1, in_es, os0, os1, out_es and the table byte offsets of the pass twiddles,
+//       roots, inter-pass twiddles (lo, hi) and half-shift rotations.
+#include "cuda_emu.h"
+#include "ssfft_codelets.cuh"
+
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iterator>
+#include <thread>
+#include <vector>
+
+thread_local EmuIdx threadIdx, blockIdx, gridDim;
+thread_local std::barrier<> *emu_barrier;
+std::atomic<int> emu_or_acc{0};
+namespace ssfft_cl {
+alignas(1024) unsigned char smem_raw[232 * 1024];
+float emu_tmem[128][32];
+thread_local unsigned char *emu_cta_smem = nullptr, *emu_peer_smem = nullptr;
+thread_local std::barrier<> *emu_cluster_barrier = nullptr;
+float2 emu_cluster_load(ClusterSmem s, int i) { return s.base[i]; }
+unsigned short f2bf(float x) {
+	uint32_t b;
+	std::memcpy(&b, &x, 4);
+	b += 0x7FFFu + ((b >> 16) & 1u);
+	return (unsigned short)(b >> 16);
+}
+float bf2f(unsigned short h) {
+	const uint32_t b = (uint32_t)h << 16;
+	float x;
+	std::memcpy(&x, &b, 4);
+	return x;
+}
+}  // namespace ssfft_cl
+
+struct Case {
+	const char *name;
+	void (*fn)(const ssfft_cl::StridedArgs);
+	int cta_threads;
+	size_t smem;
+};
+static const Case kCases[] = {
+#include "emu_strided_cases.inc"
+};
+
+static std::vector<char> slurp(const char *path) {
+	std::ifstream f(path, std::ios::binary);
+	return std::vector<char>((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+}
+
+int main(int argc, char **argv) {
+	if (argc != 21) return 2;
+	const Case &c = kCases[std::atoi(argv[1])];
+	const int grid = std::atoi(argv[2]);
+	std::vector<char> in = slurp(argv[3]), out = slurp(argv[4]), tab = slurp(argv[5]);
+	auto ll = [&](int i) { return std::atoll(argv[i]); };
+	if (c.smem > sizeof ssfft_cl::smem_raw) return 5;
+	ssfft_cl::StridedArgs a{};
+	a.in = in.data();
+	a.out = out.data();
+	a.U2 = ll(6);
+	const long long n = ll(7);
+	a.is2 = a.os2 = n;
+	a.rot_in_stride2 = a.rot_out_stride2 = n;
+	a.U0 = ll(8);
+	a.U1 = ll(9);
+	a.is0 = ll(10);
+	a.is1 = ll(11);
+	a.in_es = ll(12);
+	a.os0 = ll(13);
+	a.os1 = ll(14);
+	a.out_es = ll(15);
+	a.tw = tab.data() + ll(16);
+	a.roots = tab.data() + ll(17);
+	a.twlo = tab.data() + ll(18);
+	a.twhi = tab.data() + ll(19);
+	a.rot = tab.data() + ll(20);
+	a.pf_dist = 0;
+	// one thread per CUDA thread of a CTA, reused for every CTA in turn (the barrier at the end
+	// of a block keeps the CTAs apart: they share the emulated shared memory)
+	std::barrier<> bar(c.cta_threads);
+	std::vector<std::thread> th;
+	th.reserve(c.cta_threads);
+	for (int t = 0; t < c.cta_threads; ++t)
+		th.emplace_back([&, t] {
+			threadIdx.x = (unsigned)t;
+			gridDim.x = (unsigned)grid;
+			emu_barrier = &bar;
+			for (int b = 0; b < grid; ++b) {
+				blockIdx.x = (unsigned)b;
+				c.fn(a);
+				bar.arrive_and_wait();
+			}
+		});
+	for (auto &x : th) x.join();
+	std::ofstream f(argv[4], std::ios::binary);
+	f.write(out.data(), (std::streamsize)out.size());
+	return 0;
+}
