@@ -1,10 +1,14 @@
 // tests/emu/emu_strided_main.cpp -- runs one emulated launch of a multi-pass (four-step) pass
-// kernel, ssfft_cl::strided.  Compiled together with a generated case table
-// (emu_strided_cases.inc: `{name, &ssfft_cl::strided<...>, cta_threads, smem_bytes},` lines).
-// argv: case index, grid, raw input file, raw output file (pre-filled), table file (the plan's
-//       table bytes), transforms (U2), complex points per transform (the u2 strides), then U0,
-//       U1, is0, is1, in_es, os0, os1, out_es and the table byte offsets of the pass twiddles,
+// kernel, ssfft_cl::strided, or of its RealFFT split kernel, ssfft_cl::real_split.  Compiled
+// together with generated case tables (emu_strided_cases.inc: `{name, &ssfft_cl::strided<...>,
+// cta_threads, smem_bytes},` lines; emu_split_cases.inc: `{name, &ssfft_cl::real_split<...>},`).
+// Pass: argv = "p<case>", grid, raw input file, raw output file (pre-filled), table file (the
+//       plan's table bytes), transforms (U2), complex points per transform (the u2 strides), then
+//       U0, U1, is0, is1, in_es, os0, os1, out_es and the table byte offsets of the pass twiddles,
 //       roots, inter-pass twiddles (lo, hi) and half-shift rotations.
+// Split: argv = "s<case>", blocks per transform, raw source file (the inverse's bins), raw buffer
+//       file (pre-filled; split in place / pre-twiddled output), table file, transforms, complex
+//       points per transform, table byte offset of the split twiddles.
 #include "cuda_emu.h"
 #include "ssfft_codelets.cuh"
 
@@ -47,6 +51,16 @@ struct Case {
 static const Case kCases[] = {
 #include "emu_strided_cases.inc"
 };
+struct SplitCase {
+	const char *name;
+	void (*fn)(const ssfft_cl::SplitArgs);
+};
+static const SplitCase kSplitCases[] = {
+#include "emu_split_cases.inc"
+	{nullptr, nullptr}};
+
+// real_split: 256 threads per block (no barriers), blockIdx.y = transform
+static int run_split(int argc, char **argv);
 
 static std::vector<char> slurp(const char *path) {
 	std::ifstream f(path, std::ios::binary);
@@ -54,8 +68,9 @@ static std::vector<char> slurp(const char *path) {
 }
 
 int main(int argc, char **argv) {
-	if (argc != 21) return 2;
-	const Case &c = kCases[std::atoi(argv[1])];
+	if (argc > 1 && argv[1][0] == 's') return run_split(argc, argv);
+	if (argc != 21 || argv[1][0] != 'p') return 2;
+	const Case &c = kCases[std::atoi(argv[1] + 1)];
 	const int grid = std::atoi(argv[2]);
 	std::vector<char> in = slurp(argv[3]), out = slurp(argv[4]), tab = slurp(argv[5]);
 	auto ll = [&](int i) { return std::atoll(argv[i]); };
@@ -100,5 +115,30 @@ int main(int argc, char **argv) {
 	for (auto &x : th) x.join();
 	std::ofstream f(argv[4], std::ios::binary);
 	f.write(out.data(), (std::streamsize)out.size());
+	return 0;
+}
+
+static int run_split(int argc, char **argv) {
+	if (argc != 9) return 2;
+	const SplitCase &c = kSplitCases[std::atoi(argv[1] + 1)];
+	const int blocks = std::atoi(argv[2]);
+	std::vector<char> src = slurp(argv[3]), buf = slurp(argv[4]), tab = slurp(argv[5]);
+	ssfft_cl::SplitArgs a{};
+	a.src = src.data();
+	a.buf = buf.data();
+	a.batch = std::atoll(argv[6]);
+	a.dist = std::atoll(argv[7]);
+	a.rtw = tab.data() + std::atoll(argv[8]);
+	for (long long y = 0; y < a.batch; ++y)
+		for (int b = 0; b < blocks; ++b)
+			for (int t = 0; t < 256; ++t) {
+				threadIdx.x = (unsigned)t;
+				blockIdx.x = (unsigned)b;
+				blockIdx.y = (unsigned)y;
+				gridDim.x = (unsigned)blocks;
+				c.fn(a);
+			}
+	std::ofstream f(argv[4], std::ios::binary);
+	f.write(buf.data(), (std::streamsize)buf.size());
 	return 0;
 }
