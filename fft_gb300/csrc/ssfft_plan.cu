@@ -908,43 +908,48 @@ size_t plan_out_bytes(const Plan *p, int inverse, size_t batch) {
 }
 
 // A staged plan given an input that is not 16-byte aligned runs the plain kernel of the same
-// schedule (compiled on first use).
-static ssfft_status unstaged_kernels(const Plan *p, Schedule &u, std::vector<CUfunction> &fns) {
+// schedule (compiled on first use): u / ui the forward / inverse schedules (each direction with
+// its own knobs, so that its pass tables match), fns their kernels.
+static ssfft_status unstaged_kernels(const Plan *p, Schedule &u, Schedule &ui, std::vector<CUfunction> &fns) {
 	const Schedule &st = p->main.sch;
-	if (!make_schedule(st.dtype, st.n, st.kind, st.odd, p->batch, u, 0, p->knobs.empty() ? nullptr : &p->knobs))
+	if (!make_schedule(st.dtype, st.n, st.kind, st.odd, p->batch, u, 0, p->knobs.empty() ? nullptr : &p->knobs) ||
+	    !make_schedule(st.dtype, st.n, st.kind, st.odd, p->batch, ui, 0,
+	                   p->knobs_inv.empty() ? nullptr : &p->knobs_inv))
 		return SSFFT_ERR_UNSUPPORTED;
-	return jit_kernels({u.name(false), u.name(true)}, u.smem_bytes, fns);
+	return jit_kernels({u.name(false), ui.name(true)}, std::max(u.smem_bytes, ui.smem_bytes), fns);
 }
 
 // Compiles (and loads) what a later launch of `p` may need beyond the plan's own kernels, so that
 // the launch makes no module-loading call (e.g. inside a stream capture).
 ssfft_status plan_prepare_launch(const Plan *p) {
 	if (!p->main.sch.staged) return SSFFT_SUCCESS;
-	Schedule u;
+	Schedule u, ui;
 	std::vector<CUfunction> fns;
-	return unstaged_kernels(p, u, fns);
+	return unstaged_kernels(p, u, ui, fns);
 }
 
 static ssfft_status launch_unstaged(const Plan *p, int inverse, const void *in, void *out, size_t batch,
                                     cudaStream_t s, const long long *offs = nullptr) {
-	Schedule u;
+	Schedule u, ui;
 	std::vector<CUfunction> fns;
-	ssfft_status rc = unstaged_kernels(p, u, fns);
+	ssfft_status rc = unstaged_kernels(p, u, ui, fns);
 	if (rc != SSFFT_SUCCESS) return rc;
+	const Schedule &sch = inverse ? ui : u;
+	const Tables &tab = inverse ? p->main.tab_inv : p->main.tab;
 	ssfft_cl::Args a;
 	std::memset(&a, 0, sizeof a);
 	a.in = in;
 	a.out = out;
 	a.batch = (long long)batch;
 	plan_dists(p, inverse, a.in_dist, a.out_dist);
-	a.tw = p->main.tab.tw;
-	a.rtw = p->main.tab.rtw;
-	a.rot = p->main.tab.rot;
-	a.roots = p->main.tab.roots;
+	a.tw = tab.tw;
+	a.rtw = tab.rtw;
+	a.rot = tab.rot;
+	a.roots = tab.roots;
 	a.offs = offs;
-	const long long grid = ((long long)batch + u.per_cta - 1) / u.per_cta;
+	const long long grid = sch.grid((long long)batch);
 	if (grid > 0x7fffffffLL) return SSFFT_ERR_INVALID_SIZE;
-	return jit_launch(inverse ? fns[1] : fns[0], (unsigned)grid, (unsigned)u.cta_threads(), u.smem_bytes, s, &a);
+	return jit_launch(inverse ? fns[1] : fns[0], (unsigned)grid, (unsigned)sch.cta_threads(), sch.smem_bytes, s, &a);
 }
 
 // Transforms at scattered offsets (d_offs[g] scalars into in and out), for uneven-size batches.
