@@ -128,3 +128,18 @@ def test_fp64_tables_hold_every_twiddle_power():
     # passes 2 and 3 (radix 8 after 16 and 128 points): 7 rows (FP64) or 3 rows (FP32)
     assert F.schedule_tables(1024, "f64", "complex", 1)["tw"].size == 2 * 7 * (16 + 128)
     assert F.schedule_tables(1024, "f32", "complex", 1)["tw"].size == 2 * 3 * (16 + 128)
+
+
+def test_large_spec_describes_multipass_plans_only():
+    """ssfft_diag_large_spec: launch records of a multi-pass plan (no GPU); one-CTA lengths and
+    Bluestein lengths are refused."""
+    spec, blob = F.large_spec(1 << 21, "f32", "complex")
+    assert spec["N"] == 1 << 21 and len(spec["passes"]) == 3 and len(blob) > 0
+    p0, p2 = spec["passes"][0], spec["passes"][-1]
+    assert p0["fwd"].startswith("ssfft_cl::strided<float") and p0["inv"] != p0["fwd"]
+    assert p0["U0"] * 128 == 1 << 21 and p2["out_es"] == (1 << 21) // 128
+    spec, _ = F.large_spec(40000, "f64", "real")
+    assert spec["real"] == 1 and spec["split_fwd"].startswith("ssfft_cl::real_split<double")
+    for n in (1024, 20011):  # one CTA; a prime above 1024 (Bluestein)
+        with pytest.raises(F.SsfftError):
+            F.large_spec(n, "f32", "complex")
