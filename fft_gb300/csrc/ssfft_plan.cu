@@ -1345,6 +1345,7 @@ ssfft_status ssfft_jit_check(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_
 ssfft_status ssfft_diag_large_spec(size_t n, ssfft_dtype dtype, ssfft_kind kind, char *json, size_t json_len,
                                    void *blob, size_t *blob_bytes) {
 	if (!blob_bytes) return SSFFT_ERR_INVALID_VALUE;
+	if (plan_single_cta(n, dtype, kind)) return SSFFT_ERR_UNSUPPORTED;  // not a multi-pass plan
 	std::string j;
 	std::vector<unsigned char> b;
 	const ssfft_status st = large_spec(n, dtype, kind, j, b);
