@@ -292,9 +292,14 @@ ssfft_status large_jit_check(size_t n, ssfft_dtype dtype, ssfft_kind kind, const
 // Bluestein plan: chirp w_k = e^{-i pi k^2 / N} (k^2 reduced mod 2N exactly), the M-point
 // spectrum of b (b_m = conj(w_|m|) for |m| < N, m taken mod M) computed once with the inner
 // plan, and scratch for a chunk of transforms.
-static ssfft_status plan_build_bluestein(Plan *p, LargePlan *lp) {
+// Bluestein tables: the split twiddles (RealFFT), the chirp w_k = e^{-i pi k^2 / N} (k^2 reduced
+// modulo 2N exactly) and b (b_m = conj(w_|m|), |m| < N, zero elsewhere; its M-point spectrum is
+// taken on the device) in the plan's dtype; sets the offsets in *lp.  blob holds everything
+// before the spectrum, bb the values of b.
+static size_t blue_tables(LargePlan *lp, size_t n, ssfft_dtype dtype, std::vector<unsigned char> &blob,
+                          std::vector<unsigned char> &bb) {
 	const long long N = lp->N, M = lp->M;
-	const size_t eb = p->dtype == SSFFT_F32 ? 8 : 16, sb = eb / 2;
+	const size_t eb = dtype == SSFFT_F32 ? 8 : 16, sb = eb / 2;
 	std::vector<double> chirp, rtw, b((size_t)M * 2, 0.0);
 	chirp.reserve((size_t)N * 2);
 	for (long long k = 0; k < N; ++k) {
@@ -314,7 +319,7 @@ static ssfft_status plan_build_bluestein(Plan *p, LargePlan *lp) {
 	if (lp->real)
 		for (long long i = 0; i <= N / 2; ++i) {
 			double re, im;
-			unit_root(i, p->n, &re, &im);
+			unit_root(i, n, &re, &im);
 			rtw.push_back(im);
 			rtw.push_back(-re);
 		}
@@ -322,7 +327,7 @@ static ssfft_status plan_build_bluestein(Plan *p, LargePlan *lp) {
 	lp->off_chirp = align_up(rtw.size() * sb, 256);
 	lp->off_bhat = align_up(lp->off_chirp + chirp.size() * sb, 256);
 	const size_t total = align_up(lp->off_bhat + (size_t)M * eb, 256);
-	std::vector<unsigned char> blob(lp->off_bhat, 0);
+	blob.assign(lp->off_bhat, 0);
 	if (sb == 4) {
 		put<float>(blob, lp->off_rtw, rtw);
 		put<float>(blob, lp->off_chirp, chirp);
@@ -330,9 +335,17 @@ static ssfft_status plan_build_bluestein(Plan *p, LargePlan *lp) {
 		put<double>(blob, lp->off_rtw, rtw);
 		put<double>(blob, lp->off_chirp, chirp);
 	}
-	std::vector<unsigned char> bb((size_t)M * eb);
+	bb.assign((size_t)M * eb, 0);
 	if (sb == 4) put<float>(bb, 0, b);
 	else put<double>(bb, 0, b);
+	return total;
+}
+
+static ssfft_status plan_build_bluestein(Plan *p, LargePlan *lp) {
+	const long long M = lp->M;
+	const size_t eb = p->dtype == SSFFT_F32 ? 8 : 16;
+	std::vector<unsigned char> blob, bb;
+	const size_t total = blue_tables(lp, p->n, p->dtype, blob, bb);
 	cudaError_t e = cudaMalloc(&lp->d_tables, total);
 	if (e == cudaSuccess) e = cudaMemcpy(lp->d_tables, blob.data(), blob.size(), cudaMemcpyHostToDevice);
 	unsigned char *bhat = static_cast<unsigned char *>(lp->d_tables) + lp->off_bhat;
@@ -590,17 +603,34 @@ ssfft_status launch_large(Plan *p, int inverse, const void *in, void *out, size_
 
 // The multi-pass plan of n points as launch records (no GPU needed): a JSON object with the
 // passes' kernel names (forward, inverse), CTA shape, shared memory, groups and StridedArgs
-// strides and table offsets, and the table blob the passes read.  Bluestein lengths are refused.
+// strides and table offsets, and the table blob the passes read; for Bluestein lengths the
+// element-wise kernels, M and the table offsets instead.
 ssfft_status large_spec(size_t n, ssfft_dtype dtype, ssfft_kind kind, std::string &json,
                         std::vector<unsigned char> &blob) {
 	LargePlan lp;
 	LargeTables t;
 	ssfft_status st = large_schedule(n, dtype, kind, 227 * 1024, &lp, t);
 	if (st != SSFFT_SUCCESS) return st;
-	if (lp.M) return SSFFT_ERR_UNSUPPORTED;
-	large_blob(&lp, t, n, dtype, blob);
 	const std::vector<std::string> names = large_kernel_names(&lp, dtype);
 	auto num = [](long long v) { return std::to_string(v); };
+	if (lp.M) {
+		// Bluestein: the element-wise kernels, the tables with b (not its spectrum: the device
+		// takes that with the M-point plan when the plan is made) at off_bhat
+		std::vector<unsigned char> bb;
+		blob.clear();
+		const size_t total = blue_tables(&lp, n, dtype, blob, bb);
+		blob.resize(total, 0);
+		std::memcpy(blob.data() + lp.off_bhat, bb.data(), bb.size());
+		json = "{\"N\": " + num(lp.N) + ", \"M\": " + num(lp.M) + ", \"real\": " + num(lp.real) +
+		       ", \"modified\": 0, \"off_rtw\": " + num((long long)lp.off_rtw) + ", \"off_chirp\": " +
+		       num((long long)lp.off_chirp) + ", \"off_bhat\": " + num((long long)lp.off_bhat) + ", \"blue\": [";
+		for (int i = 0; i < 5; ++i) json += std::string(i ? ", " : "") + "\"" + names[i] + "\"";
+		json += "], \"passes\": []";
+		if (lp.real) json += ", \"split_fwd\": \"" + names[5] + "\", \"split_inv\": \"" + names[6] + "\"";
+		json += "}";
+		return SSFFT_SUCCESS;
+	}
+	large_blob(&lp, t, n, dtype, blob);
 	json = "{\"N\": " + num(lp.N) + ", \"real\": " + num(lp.real) + ", \"modified\": " + num(lp.modified) +
 	       ", \"off_rtw\": " + num((long long)lp.off_rtw) + ", \"off_rot\": " + num((long long)lp.off_rot) +
 	       ", \"passes\": [";

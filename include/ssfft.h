@@ -255,10 +255,11 @@ ssfft_status ssfft_schedule_direction(int inverse);
  * 128 x 32, all host memory); *flags receives the kernel's error flag.  No reference
  * counterpart. */
 ssfft_status ssfft_diag_tc_tile(const float *a, const float *bt, float *d, unsigned *flags);
-/* The multi-pass (four-step) plan of n points as launch records: `json` receives the passes'
- * kernel names, CTA shapes, shared memory, groups, strides and table offsets; `blob` the table
- * bytes the passes read (NULL: only *blob_bytes is set).  Host only; lengths that run in one CTA
- * or through Bluestein's algorithm return SSFFT_ERR_UNSUPPORTED.  No reference counterpart. */
+/* The plan of n points beyond one CTA as launch records: `json` receives the multi-pass
+ * kernel names, CTA shapes, shared memory, groups, strides and table offsets (or, for lengths
+ * that run Bluestein's algorithm, its element-wise kernels, M and the offsets of the chirp and
+ * of b); `blob` the table bytes (NULL: only *blob_bytes is set).  Host only; lengths that run in
+ * one CTA return SSFFT_ERR_UNSUPPORTED.  No reference counterpart. */
 ssfft_status ssfft_diag_large_spec(size_t n, ssfft_dtype dtype, ssfft_kind kind, char *json, size_t json_len,
                                    void *blob, size_t *blob_bytes);
 ssfft_status ssfft_jit_check(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, const char *arch,

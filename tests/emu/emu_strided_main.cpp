@@ -9,6 +9,10 @@
 // Split: argv = "s<case>", blocks per transform, raw source file (the inverse's bins), raw buffer
 //       file (pre-filled; split in place / pre-twiddled output), table file, transforms, complex
 //       points per transform, table byte offset of the split twiddles.
+// Bluestein element-wise kernels (emu_blue_cases.inc): argv = "b<case>", blocks per transform,
+//       transforms, raw input file, raw output file, raw work file (both written back), table
+//       file, n, m, distance between transforms, table byte offsets of the chirp and of the
+//       spectrum of b.
 #include "cuda_emu.h"
 #include "ssfft_codelets.cuh"
 
@@ -59,8 +63,18 @@ static const SplitCase kSplitCases[] = {
 #include "emu_split_cases.inc"
 	{nullptr, nullptr}};
 
-// real_split: 256 threads per block (no barriers), blockIdx.y = transform
+struct BlueCase {
+	const char *name;
+	void (*fn)(const ssfft_cl::BlueArgs);
+};
+static const BlueCase kBlueCases[] = {
+#include "emu_blue_cases.inc"
+	{nullptr, nullptr}};
+
+// real_split and the Bluestein kernels: 256 threads per block (no barriers), blockIdx.y =
+// transform
 static int run_split(int argc, char **argv);
+static int run_blue(int argc, char **argv);
 
 static std::vector<char> slurp(const char *path) {
 	std::ifstream f(path, std::ios::binary);
@@ -69,6 +83,7 @@ static std::vector<char> slurp(const char *path) {
 
 int main(int argc, char **argv) {
 	if (argc > 1 && argv[1][0] == 's') return run_split(argc, argv);
+	if (argc > 1 && argv[1][0] == 'b') return run_blue(argc, argv);
 	if (argc != 21 || argv[1][0] != 'p') return 2;
 	const Case &c = kCases[std::atoi(argv[1] + 1)];
 	const int grid = std::atoi(argv[2]);
@@ -140,5 +155,36 @@ static int run_split(int argc, char **argv) {
 			}
 	std::ofstream f(argv[4], std::ios::binary);
 	f.write(buf.data(), (std::streamsize)buf.size());
+	return 0;
+}
+
+static int run_blue(int argc, char **argv) {
+	if (argc != 13) return 2;
+	const BlueCase &c = kBlueCases[std::atoi(argv[1] + 1)];
+	const int blocks = std::atoi(argv[2]);
+	std::vector<char> in = slurp(argv[4]), out = slurp(argv[5]), work = slurp(argv[6]), tab = slurp(argv[7]);
+	ssfft_cl::BlueArgs a{};
+	a.in = in.data();
+	a.out = out.data();
+	a.work = work.data();
+	a.batch = std::atoll(argv[3]);
+	a.n = std::atoll(argv[8]);
+	a.m = std::atoll(argv[9]);
+	a.dist = std::atoll(argv[10]);
+	a.chirp = tab.data() + std::atoll(argv[11]);
+	a.bhat = tab.data() + std::atoll(argv[12]);
+	for (long long y = 0; y < a.batch; ++y)
+		for (int b = 0; b < blocks; ++b)
+			for (int t = 0; t < 256; ++t) {
+				threadIdx.x = (unsigned)t;
+				blockIdx.x = (unsigned)b;
+				blockIdx.y = (unsigned)y;
+				gridDim.x = (unsigned)blocks;
+				c.fn(a);
+			}
+	std::ofstream fo(argv[5], std::ios::binary);
+	fo.write(out.data(), (std::streamsize)out.size());
+	std::ofstream fw(argv[6], std::ios::binary);
+	fw.write(work.data(), (std::streamsize)work.size());
 	return 0;
 }

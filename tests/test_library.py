@@ -131,8 +131,8 @@ def test_fp64_tables_hold_every_twiddle_power():
 
 
 def test_large_spec_describes_multipass_plans_only():
-    """ssfft_diag_large_spec: launch records of a multi-pass plan (no GPU); one-CTA lengths and
-    Bluestein lengths are refused."""
+    """ssfft_diag_large_spec: launch records of a multi-pass or Bluestein plan (no GPU); one-CTA
+    lengths are refused."""
     spec, blob = F.large_spec(1 << 21, "f32", "complex")
     assert spec["N"] == 1 << 21 and len(spec["passes"]) == 3 and len(blob) > 0
     p0, p2 = spec["passes"][0], spec["passes"][-1]
@@ -140,6 +140,8 @@ def test_large_spec_describes_multipass_plans_only():
     assert p0["U0"] * 128 == 1 << 21 and p2["out_es"] == (1 << 21) // 128
     spec, _ = F.large_spec(40000, "f64", "real")
     assert spec["real"] == 1 and spec["split_fwd"].startswith("ssfft_cl::real_split<double")
-    for n in (1024, 20011):  # one CTA; a prime above 1024 (Bluestein)
-        with pytest.raises(F.SsfftError):
-            F.large_spec(n, "f32", "complex")
+    spec, blob = F.large_spec(20011, "f32", "complex")  # a prime above 1024: Bluestein
+    assert spec["M"] >= 2 * 20011 - 1 and spec["blue"][0] == "ssfft_cl::blue_pre<float, false>"
+    assert len(blob) >= spec["off_bhat"] + 8 * spec["M"]
+    with pytest.raises(F.SsfftError):
+        F.large_spec(1024, "f32", "complex")  # one CTA
