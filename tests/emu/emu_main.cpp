@@ -4,7 +4,8 @@
 // shared-memory array; reads of a CTA's shared memory through the cluster window are
 // bounds-checked.
 // argv: case index, grid, raw input file, raw output file (pre-filled), table file, batch,
-//       in_dist, out_dist (scalars), scalar bytes, input bytes per transform (staged kernels).
+//       in_dist, out_dist (scalars), scalar bytes, input bytes per transform (staged kernels)
+//       [, offset-table file: int64 scalar offsets of each transform in input and output].
 // The table file holds tw, roots, rtw, rot back to back in the kernel's dtype, preceded by four
 // uint64 element counts (scalars).
 #include "cuda_emu.h"
@@ -68,7 +69,7 @@ static std::vector<char> slurp(const char *path) {
 }
 
 int main(int argc, char **argv) {
-	if (argc != 11) return 2;
+	if (argc != 11 && argc != 12) return 2;
 	const Case &c = kCases[std::atoi(argv[1])];
 	const int grid = std::atoi(argv[2]);
 	std::vector<char> in = slurp(argv[3]), out = slurp(argv[4]), tab = slurp(argv[5]);
@@ -89,6 +90,11 @@ int main(int argc, char **argv) {
 	a.err = &err;
 	a.spin_limit = 1;
 	a.in_bytes = (unsigned)std::atoi(argv[10]);
+	std::vector<char> offs;
+	if (argc == 12) {
+		offs = slurp(argv[11]);
+		a.offs = reinterpret_cast<const long long *>(offs.data());
+	}
 	// tensor-core kernels: the first pass's DFT matrix follows the four tables when present
 	a.tcb = reinterpret_cast<const float *>(base + (cnt[0] + cnt[1] + cnt[2] + cnt[3]) * sb);
 	if (c.cluster == 2) {

@@ -51,7 +51,12 @@ TC_TOL = 2e-6
 # the default complex cases above of 8192+ points run the bulk-copy kernel.
 PAIR_CASES = [(16384, 1, 1, [16, 8, 16, 8], 2), (12288, 2, 2, [32, 16, 24], 1), (9216, 1, 1, [16, 6, 12, 8], 2),
               (15360, 1, 1, [8, 15, 16, 8], 2), (8192, 3, 3, [8, 16, 4, 16], 2), (4000, 2, 2, [10, 20, 20], 1)]
-VARIANTS = {"default": {"fuse_split": 1}, "tc": {"precision": "split_bf16"}}
+# transforms at scattered offsets (the offset-table launches of uneven batches): (case, variant);
+# "offs" compiles the plain kernel of the case (not the staged one this module's plans pick)
+OFFS_CASES = [((240, "f32", "complex", 2, 2), "offs"), ((64, "f32", "complex", 300, 300), "offs"),
+              ((1920, "f32", "complex", 1, 1), "offs"), ((4096, "f32", "complex", 1, 1), "offs"),
+              ((16384, "f32", "complex", 1, 1), "pair16384"), ((1024, "f64", "complex", 7, 7), "offs")]
+VARIANTS = {"default": {"fuse_split": 1}, "tc": {"precision": "split_bf16"}, "offs": {}}
 for _c in PAIR_CASES:
     VARIANTS[f"pair{_c[0]}"] = ({"cluster_split": _c[4], "radices": _c[3]} if _c[3] else {})
 
@@ -90,8 +95,11 @@ def emulator(staged_schedules, tmp_path_factory):
     index = {}
     cases = [(c, "default") for c in CASES] + [(c, "tc") for c in TC_CASES]
     cases += [((c[0], "f32", "complex", c[1], c[2]), f"pair{c[0]}") for c in PAIR_CASES]
+    cases += [(c, "offs") for c, v in OFFS_CASES if v == "offs"]
     for case, var in cases:
         (n, dt, kind, pb, _) = case
+        # offset-table launches run the plain kernel (the library routes them off the staged one)
+        os.environ["SSFFT_STAGED"] = "0" if var == "offs" else "1"
         F.schedule_options(**VARIANTS[var])
         for inv in (False, True):
             # a RealFFT plan may run a different radix order per direction (fused split)
@@ -104,6 +112,7 @@ def emulator(staged_schedules, tmp_path_factory):
                          f'{info["smem_bytes"]}, {cluster}}},')
         F.schedule_options()
         F.schedule_direction(False)
+    os.environ["SSFFT_STAGED"] = "1"
     (d / "emu_cases.inc").write_text("\n".join(lines) + "\n")
     exe = d / "emu"
     cmd = ["g++", "-std=c++20", "-O1", "-pthread", "-w", "-I", str(d), "-I", os.path.join(ROOT, "tests", "emu"),
@@ -212,3 +221,49 @@ def test_emulated_pair_kernel_matches_oracle(emulator, case):
         got = _run(emulator, n, "f32", "complex", pb, eb, inv, x, var=var).view(np.complex64)
         ref = np.stack([oracle.fft(r.astype(np.complex128), inv) for r in x])
         assert rel_l2(got, ref) <= 1e-6, (inv, rel_l2(got, ref))
+
+
+
+
+@pytest.mark.parametrize("case,var", OFFS_CASES, ids=lambda c: str(c[0]) if isinstance(c, tuple) else c)
+def test_emulated_offset_table(emulator, case, var):
+    """Each transform read and written at its own offset (odd gaps between them): every transform
+    matches the oracle and nothing outside the transforms is written."""
+    exe, index, d = emulator
+    n, dt, kind, pb, eb = case
+    sdt = np.float32 if dt == "f32" else np.float64
+    cdt = np.complex64 if dt == "f32" else np.complex128
+    ci, info = index[(n, dt, kind, pb, False, var)]
+    os.environ["SSFFT_STAGED"] = "0" if var == "offs" else "1"
+    F.schedule_options(**VARIANTS[var])
+    name = F.schedule_name(n, dt, kind, pb)
+    tabs = F.schedule_tables(n, dt, kind, pb)
+    F.schedule_options()
+    os.environ["SSFFT_STAGED"] = "1"
+    assert "batch_staged" not in name, name
+    gap = 3
+    offs = np.array([g * (n + gap) + 1 for g in range(eb)], dtype=np.int64)  # complex units
+    total = int(offs[-1]) + n + gap
+    rng = np.random.default_rng(n + eb)
+    x = (rng.uniform(-1, 1, (eb, n)) + 1j * rng.uniform(-1, 1, (eb, n))).astype(cdt)
+    buf = np.full(total, np.nan, dtype=cdt)
+    for g in range(eb):
+        buf[offs[g]:offs[g] + n] = x[g]
+    blob = np.array([tabs[k].size for k in ("tw", "roots", "rtw", "rot")], dtype=np.uint64).tobytes()
+    blob += b"".join(tabs[k].astype(sdt).tobytes() for k in ("tw", "roots", "rtw", "rot"))
+    fi, fo, ft, fs = d / f"oin{ci}", d / f"oout{ci}", d / f"otab{ci}", d / f"offs{ci}"
+    fi.write_bytes(buf.tobytes())
+    fo.write_bytes(np.full(total, np.nan, dtype=cdt).tobytes())
+    ft.write_bytes(blob)
+    fs.write_bytes((2 * offs).tobytes())  # scalars
+    groups = -(-eb // info["per_cta"])
+    grid = 2 * eb if name.startswith("ssfft_cl::pair<") else groups
+    subprocess.run([str(exe), str(ci), str(grid), str(fi), str(fo), str(ft), str(eb), str(2 * n), str(2 * n),
+                    str(np.dtype(sdt).itemsize), str(2 * n * np.dtype(sdt).itemsize), str(fs)], check=True, timeout=300)
+    out = np.frombuffer(fo.read_bytes(), dtype=cdt)
+    inside = np.zeros(total, dtype=bool)
+    for g in range(eb):
+        inside[offs[g]:offs[g] + n] = True
+        ref = oracle.fft(x[g].astype(np.complex128))
+        assert rel_l2(out[offs[g]:offs[g] + n], ref) <= (1e-6 if dt == "f32" else 1e-13), g
+    assert np.all(np.isnan(out[~inside])), "nothing written outside the transforms"
