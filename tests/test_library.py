@@ -145,3 +145,21 @@ def test_large_spec_describes_multipass_plans_only():
     assert len(blob) >= spec["off_bhat"] + 8 * spec["M"]
     with pytest.raises(F.SsfftError):
         F.large_spec(1024, "f32", "complex")  # one CTA
+
+
+def test_cluster_split_options_in_the_planner():
+    """The two-CTA cluster schedule from explicit options (no GPU): a valid split runs the pair
+    kernel with its phases, an odd first phase or a split with no second phase is refused, and
+    cluster_split=-1 keeps the one-CTA kernel."""
+    try:
+        F.schedule_options(radices=[16, 8, 16, 8], cluster_split=2)
+        name = F.schedule_name(16384, "f32", "complex", 8)
+        assert name.startswith("ssfft_cl::pair<float, 128, 128,") and "Radices<16, 8>, ssfft_cl::Radices<16, 8>>" in name
+        assert F.jit_check(16384, "f32", "complex", 8) > 0
+        F.schedule_options(radices=[25, 16, 25], cluster_split=1)
+        with pytest.raises(F.SsfftError):
+            F.schedule_name(10000, "f32", "complex", 8)
+        F.schedule_options(cluster_split=-1)
+        assert F.schedule_name(16384, "f32", "complex", 8).startswith("ssfft_cl::batch<")
+    finally:
+        F.schedule_options()
