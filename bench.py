@@ -59,6 +59,16 @@ def parse():
     ap.add_argument("--sweep-mb", type=int, default=512, help="sizes workload: MiB of input + output per launch")
     ap.add_argument("--plan-options", default="{}", help="sizes workload: JSON keyword options of fft_gb300.Plan")
     ap.add_argument("--serve-duration", type=float, default=3.0)
+    ap.add_argument("--passes", type=int, default=0,
+                    help="passes of the workload per timed step (0: enough for a timed region of >= --min-timed-s)")
+    ap.add_argument("--min-timed-s", type=float, default=1.5,
+                    help="default line: the timed region lasts at least this long (clock samples under load)")
+    ap.add_argument("--no-served", action="store_true", help="default line: skip the served block")
+    ap.add_argument("--no-uneven", action="store_true", help="default line: skip the uneven-batch block")
+    ap.add_argument("--served-duration", type=float, default=1.0,
+                    help="default line: seconds of offered load per point of the served sweep")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+                    help="CPU baseline: seconds of CPU work in the bounded sample")
     ap.add_argument("--tune", type=int, default=2, choices=[0, 1, 2],
                     help="autotune level of the plans (0 planner defaults, 1 CTA shape, 2 also radix order)")
     ap.add_argument("--streams", type=int, default=4,
@@ -174,21 +184,34 @@ def traffic_for(kernel: str):
     return None
 
 
-def cpu_leg(frames: int, threads: int, kind: str = "port", seed: int = 7) -> dict:
+CPU_KIND = "port_native"  # the oracle's C restatement built -O3 with the host's vector ISA (timing only)
+
+
+def cpu_leg(frames: int, threads: int, kind: str = CPU_KIND, seed: int = 7, min_seconds: float = 0.0) -> dict:
     """Time the reference algorithm on the host cores: forward + inverse of every size over
-    `frames` frames, one plan instance per thread."""
+    `frames` frames, one plan instance per thread; repeated until `min_seconds` of work."""
     import oracle
-    total_t, total_f = 0.0, 0.0
+    data = []
     for i, n in enumerate(SIZES):
         x = frames_for(n, frames, seed + i)
-        spec = np.empty((frames, n // 2), dtype=np.complex64)
-        back = np.empty((frames, n), dtype=np.float32)
-        t0 = time.perf_counter()
-        oracle.batch(x, n, real=True, inverse=False, threads=threads, out=spec, kind=kind)
-        oracle.batch(spec, n, real=True, inverse=True, threads=threads, out=back, kind=kind)
-        total_t += time.perf_counter() - t0
-        total_f += 2 * frames * 2.5 * n * math.log2(n)
-    return {"gflops": total_f / total_t / 1e9, "seconds": total_t}
+        data.append((n, x, np.empty((frames, n // 2), dtype=np.complex64), np.empty((frames, n), dtype=np.float32)))
+    total_t, total_f, reps = 0.0, 0.0, 0
+    while True:
+        for n, x, spec, back in data:
+            t0 = time.perf_counter()
+            oracle.batch(x, n, real=True, inverse=False, threads=threads, out=spec, kind=kind)
+            oracle.batch(spec, n, real=True, inverse=True, threads=threads, out=back, kind=kind)
+            total_t += time.perf_counter() - t0
+            total_f += 2 * frames * 2.5 * n * math.log2(n)
+        reps += 1
+        if total_t >= min_seconds:
+            break
+    return {"gflops": total_f / total_t / 1e9, "seconds": total_t, "reps": reps}
+
+
+def cpu_build_note() -> str:
+    import oracle
+    return f"oracle/ssfft_oracle.c built `{oracle.native_flags()}` (oracle/Makefile target native)"
 
 
 def run_reference(args, rank: int, world: int):
@@ -207,13 +230,14 @@ def run_reference(args, rank: int, world: int):
     for _ in range(args.steps):
         t += cpu_leg(frames, threads)["seconds"]
     value = flops_per_step(frames) * args.steps / t / 1e9
-    sample = f"{frames} frames per size per step (of {args.frames}), forward+inverse of N in {list(SIZES)}"
+    sample = (f"{frames} frames per size per step (of {args.frames}), forward+inverse of N in {list(SIZES)}; "
+              f"{cpu_build_note()}; one plan instance per thread")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "RealFFT<float> N in {480,960,1920,3840}, 16384 frames each, fwd+inv",
-                   "frames_per_step": frames, "host": os.uname().machine},
+                   "frames": args.frames, "frames_timed_per_step": frames, "host": os.uname().machine},
         "cpu_baseline": {"value": value, "unit": "GFLOP/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -275,6 +299,23 @@ def run_gpu(args, rank: int, world: int):
         step()
     torch.cuda.synchronize()
 
+    # passes per timed step: each step runs the whole workload `passes` times back to back, so
+    # that the timed region lasts >= --min-timed-s and the clock sampler sees it under load
+    passes = args.passes
+    if passes <= 0:
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(5):
+            step()
+        b.record(stream)
+        torch.cuda.synchronize()
+        per = a.elapsed_time(b) / 1e3 / 5
+        passes = max(1, math.ceil(args.min_timed_s / (per * max(1, args.steps))))
+    if dist:
+        pt = torch.tensor([passes], dtype=torch.int64, device="cuda")
+        dist.all_reduce(pt, op=dist.ReduceOp.MAX)
+        passes = int(pt.item())
+
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.25)
@@ -285,14 +326,15 @@ def run_gpu(args, rank: int, world: int):
     t1 = torch.cuda.Event(enable_timing=True)
     t0.record(stream)
     for k in range(args.steps):
-        step()
+        for _ in range(passes):
+            step()
     t1.record(stream)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     clk = clocks.stop()
     elapsed = max_over_ranks(t0.elapsed_time(t1) / 1e3, dist, "cuda")
-    value = flops_per_step(frames) * args.steps * world / elapsed / 1e9
+    value = flops_per_step(frames) * passes * args.steps * world / elapsed / 1e9
 
     # per-kernel durations for the roofline: each kernel timed alone on the launching stream,
     # CUDA events around `reps` back-to-back launches of it (idempotent: same input and output),
@@ -320,7 +362,7 @@ def run_gpu(args, rank: int, world: int):
     kernels = {names[j]: {"ms": round(kt[j] * 1e3, 4), "GB_s": round(alg[j] / kt[j] / 1e9, 1),
                           "frac": round(alg[j] / kt[j] / 1e9 / peak, 3)} for j in range(nl)}
     agg_bytes = sum(alg)
-    agg_gbs = agg_bytes / (elapsed / args.steps) / 1e9 / world
+    agg_gbs = agg_bytes / (elapsed / (args.steps * passes)) / 1e9
 
     # numerics of what was timed: 64 frames of every size, forward spectrum and inverse output,
     # against the FP64 oracle (relL2, the FP32 bar is 1e-6)
@@ -373,10 +415,17 @@ def run_gpu(args, rank: int, world: int):
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         sample = min(frames, 4096)
-        c = cpu_leg(sample, threads)
+        c = cpu_leg(sample, threads, min_seconds=args.cpu_seconds)
         cpu = {"value": c["gflops"], "unit": "GFLOP/s", "cores": threads, "kind": "port",
-               "sample": f"{sample} frames per size, forward+inverse of N in {list(SIZES)} "
-                         f"({c['seconds']:.1f} s wall), oracle/ssfft_oracle.c built -O3"}
+               "sample": f"{sample} frames per size x {c['reps']} repetitions, forward+inverse of N in "
+                         f"{list(SIZES)} ({c['seconds']:.1f} s of CPU work on {threads} threads, one plan "
+                         f"instance per thread); {cpu_build_note()}"}
+
+    served = uneven = None
+    if rank == 0 and not args.no_served:
+        served = served_block(args)
+    if rank == 0 and not args.no_uneven:
+        uneven = uneven_block(args, steps=50)
 
     if rank == 0:
         line = {
@@ -385,9 +434,12 @@ def run_gpu(args, rank: int, world: int):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "RealFFT<float> N in {480,960,1920,3840}, 16384 frames each, fwd+inv",
                        "frames": frames, "parallelism": f"replicas x{world}", "streams": nstreams,
-                       "l2": "each step streams ~1.9 GB (> 129 MB L2), no flush",
+                       "passes_per_step": passes,
+                       "step": f"{passes} back-to-back passes of the workload (forward + inverse of every size)",
+                       "timed_region_s": elapsed,
+                       "l2": "each pass streams ~1.9 GB (> 129 MB L2), no flush",
                        "autotune": args.tune, "schedules": schedules},
-            "gpu_launches": nl * args.steps,
+            "gpu_launches": nl * args.steps * passes,
             "relL2_vs_fp64_oracle": rel, "relL2_per_size": rel_sizes,
             "roofline": {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": peak,
                          "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
@@ -396,9 +448,11 @@ def run_gpu(args, rank: int, world: int):
                          "aggregate_GB_s": agg_gbs, "aggregate_frac": agg_gbs / peak},
             "kernels": kernels,
             "e2e": e2e,
-            "gpu_launches_note": "per step: forward + inverse of each of the 4 sizes, one launch each",
+            "gpu_launches_note": "per pass: forward + inverse of each of the 4 sizes, one launch each",
             "cpu_baseline": cpu,
             "clocks": clk,
+            "served": served,
+            "uneven": uneven,
         }
         print(json.dumps(line), flush=True)
     if dist:
@@ -494,6 +548,110 @@ def run_large(args):
                       "peak_source": kind}), flush=True)
 
 
+SERVE_LOADS = (1e4, 1e5, 5e5, 1e6, 1.5e6, 2e6)
+P99_BOUND_US = 2000.0  # a load is "sustained" when the batched p99 stays within this and it keeps up
+
+
+def _serve_point(srv, rate: float, duration: float, seed: int) -> dict:
+    st = srv.loadgen(offered_rate=rate, duration_s=duration, seed=seed)
+    span = st["span_seconds"]
+    tps = st["frames"] / span if span else 0.0
+    return {"p50_us": st["p50_latency_us"], "p99_us": st["p99_latency_us"], "transforms_per_s": tps,
+            "GFLOP_s": st["flops"] / span / 1e9 if span else 0.0, "requests": st["completed"],
+            "failed": st["failed"], "waves": st["waves"], "launches": st["launches"], "span_s": span,
+            "keeps_up": bool(tps >= 0.9 * rate)}
+
+
+def _serve_relerr(F) -> dict:
+    """relL2 of served results against the FP64 oracle: a burst of mixed requests (complex and
+    real, both directions, one- and multi-pass sizes) submitted together to the batched server,
+    so that they are coalesced into shared waves."""
+    import oracle
+    rng = np.random.default_rng(321)
+    srv = F.Server(hbm_budget_bytes=1 << 30, waves=4, max_requests_per_wave=256, coalesce=True)
+    shapes = [(256, "real"), (480, "complex"), (1920, "real"), (3840, "real"), (4096, "complex"),
+              (15625, "complex"), (20480, "complex"), (65536, "real"), (62500, "real"), (65536, "complex")]
+    jobs = []
+    for i in range(40):
+        n, kind = shapes[i % len(shapes)]
+        inv = bool(i % 2)
+        frames = int(rng.integers(1, 5))
+        if kind == "complex":
+            x = (rng.standard_normal((frames, n)) + 1j * rng.standard_normal((frames, n))).astype(np.complex64)
+            y = np.empty_like(x)
+        elif not inv:
+            x = rng.standard_normal((frames, n)).astype(np.float32)
+            y = np.empty((frames, n // 2), dtype=np.complex64)
+        else:
+            x = (rng.standard_normal((frames, n // 2)) + 1j * rng.standard_normal((frames, n // 2))).astype(np.complex64)
+            y = np.empty((frames, n), dtype=np.float32)
+        t = srv.submit(n, kind, inv, x, y, frames)
+        jobs.append((t, n, kind, inv, x, y))
+    worst = 0.0
+    for t, n, kind, inv, x, y in jobs:
+        srv.wait(t)
+        if kind == "complex":
+            ref = oracle.batch(x.astype(np.complex128), n, real=False, inverse=inv)
+        else:
+            ref = oracle.batch(x.astype(np.complex128 if inv else np.float64), n, real=True, inverse=inv)
+        worst = max(worst, float(np.linalg.norm(y - ref) / np.linalg.norm(ref)))
+    srv.close()
+    return {"worst_relL2": worst, "requests": len(jobs),
+            "sample": "40 requests (1-4 frames; complex and RealFFT, forward and inverse, N 256-65536) "
+                      "submitted together to the batched server, against the FP64 oracle"}
+
+
+def served_block(args) -> dict:
+    """Serving configuration: open-loop Poisson requests of 1-64 frames of one size, log-uniform
+    over the 2^a 3^b 5^c sizes in [256, 65536], 70% RealFFT / 30% complex, 50/50 forward/inverse,
+    FP32, N(0,1) inputs in pinned host memory, 16 GB HBM budget.  At each offered load: p50/p99
+    latency and throughput of the continuous-batching server and of plain per-request execution
+    (one synchronous copy-in / launch / copy-out per request) on the same GPU."""
+    import fft_gb300 as F
+    t0 = time.perf_counter()
+    batched = F.Server(hbm_budget_bytes=16 << 30, waves=4, max_requests_per_wave=256, coalesce=True)
+    plain = F.Server(hbm_budget_bytes=16 << 30, coalesce=False)
+    sweep = []
+    for i, rate in enumerate(SERVE_LOADS):
+        row = {"offered_transforms_per_s": rate,
+               "batched": _serve_point(batched, rate, args.served_duration, 100 + i),
+               "plain": _serve_point(plain, rate, args.served_duration, 100 + i)}
+        b, p = row["batched"], row["plain"]
+        row["throughput_ratio"] = b["transforms_per_s"] / p["transforms_per_s"] if p["transforms_per_s"] else None
+        sweep.append(row)
+        print(json.dumps({"served_point": row}), file=sys.stderr, flush=True)
+    batched.close()
+    plain.close()
+    ok = [r for r in sweep if r["batched"]["keeps_up"] and r["batched"]["p99_us"] <= P99_BOUND_US]
+    best = max(ok, key=lambda r: r["offered_transforms_per_s"]) if ok else None
+    sat_b = max(sweep, key=lambda r: r["batched"]["transforms_per_s"])
+    sat_p = max(sweep, key=lambda r: r["plain"]["transforms_per_s"])
+    out = {
+        "workload": "open-loop Poisson, 1-64 frames/request, N log-uniform over 2^a3^b5^c in [256,65536], "
+                    "70% real / 30% complex, 50/50 fwd/inv, FP32, pinned host buffers, 16 GB HBM budget",
+        "duration_s_per_load": args.served_duration,
+        "p99_bound_us": P99_BOUND_US,
+        "max_sustained_load": best["offered_transforms_per_s"] if best else None,
+        "at_max_sustained_load": ({"GFLOP_s": best["batched"]["GFLOP_s"],
+                                   "transforms_per_s": best["batched"]["transforms_per_s"],
+                                   "p50_us": best["batched"]["p50_us"], "p99_us": best["batched"]["p99_us"],
+                                   "plain_transforms_per_s": best["plain"]["transforms_per_s"],
+                                   "plain_p99_us": best["plain"]["p99_us"],
+                                   "throughput_ratio_vs_plain": best["throughput_ratio"]} if best else None),
+        "saturation": {"batched_GFLOP_s": sat_b["batched"]["GFLOP_s"],
+                       "batched_transforms_per_s": sat_b["batched"]["transforms_per_s"],
+                       "plain_GFLOP_s": sat_p["plain"]["GFLOP_s"],
+                       "plain_transforms_per_s": sat_p["plain"]["transforms_per_s"],
+                       "ratio": (sat_b["batched"]["transforms_per_s"] / sat_p["plain"]["transforms_per_s"]
+                                 if sat_p["plain"]["transforms_per_s"] else None)},
+        "sweep": sweep,
+        "relL2": _serve_relerr(F),
+        "wall_s": None,
+    }
+    out["wall_s"] = time.perf_counter() - t0
+    return out
+
+
 def run_serve(args):
     """Open-loop Poisson request stream (1-64 frames of one size, log-uniform over 2^a 3^b 5^c
     sizes in [256, 65536], 70% real / 30% complex, 50/50 forward/inverse, FP32, 16 GB HBM budget):
@@ -523,6 +681,10 @@ def run_serve(args):
 
 
 def run_uneven(args):
+    print(json.dumps(uneven_block(args)), flush=True)
+
+
+def uneven_block(args, steps: int | None = None) -> dict:
     """One submission of 32768 complex FP32 transforms, sizes log-uniform over the 175 sizes
     2^a 3^b 5^c in [64, 16384], U[-1,1): the CUDA-graph batch against one plain launch per size."""
     import torch
@@ -547,12 +709,14 @@ def run_uneven(args):
     sample = list(range(0, 32768, 128))
     refs = {i: oracle.fft(xs[offs[i]:offs[i + 1]].astype(np.complex128)) for i in sample}
 
+    reps = steps or max(args.steps // 4, 50)
+
     def variant(precision):
         t0 = time.perf_counter()
         m = F.Multi(sizes, "f32", autotune=min(args.tune, 1), precision=precision)
         build_s = time.perf_counter() - t0
-        tg = _time_device(lambda: m.exec(False, x.data_ptr(), y.data_ptr(), sh), max(args.steps // 4, 50), 5)
-        tp = _time_device(lambda: m.exec_plain(False, x.data_ptr(), y.data_ptr(), sh), max(args.steps // 4, 50), 5)
+        tg = _time_device(lambda: m.exec(False, x.data_ptr(), y.data_ptr(), sh), reps, 5)
+        tp = _time_device(lambda: m.exec_plain(False, x.data_ptr(), y.data_ptr(), sh), reps, 5)
         m.exec(False, x.data_ptr(), y.data_ptr(), sh)
         torch.cuda.synchronize()
         ys = y.cpu().numpy()
@@ -566,15 +730,20 @@ def run_uneven(args):
                 "speedup_vs_plain": tp / tg, "plan_build_s": build_s, "worst_relL2_sampled": worst,
                 "distinct_sizes": m.info()["distinct_sizes"]}
 
+    t_all = time.perf_counter()
     fp32 = variant("fp32")
     bf16 = variant("split_bf16")
-    print(json.dumps({"workload": "32768 complex FP32 transforms, uneven sizes in [64,16384]",
-                      "alg_bytes": alg, "autotune": min(args.tune, 1), "peak_GB_s": peak, "peak_source": kind,
-                      "relL2_sample": f"{len(sample)} transforms (every 128th) against the FP64 oracle",
-                      "fp32_fma": fp32,
-                      "split_bf16": dict(bf16, note="first radix pass (radix <= 16) on tcgen05 tensor cores, "
-                                                    "three BF16 parts per operand, FP32 accumulation")}),
-          flush=True)
+    out = {"workload": "32768 complex FP32 transforms, uneven sizes log-uniform over 2^a3^b5^c in [64,16384]",
+           "alg_bytes": alg, "autotune": min(args.tune, 1), "peak_GB_s": peak, "peak_source": kind,
+           "relL2_sample": f"{len(sample)} transforms (every 128th) against the FP64 oracle",
+           "timing": f"CUDA events around {reps} back-to-back submissions, mean",
+           "fp32_fma": fp32,
+           "split_bf16": dict(bf16, note="first radix pass (radix <= 16) on tcgen05 tensor cores, "
+                                         "three BF16 parts per operand, FP32 accumulation"),
+           "wall_s": time.perf_counter() - t_all}
+    del x, y
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_precision(args):

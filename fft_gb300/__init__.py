@@ -106,9 +106,13 @@ def _declare(l):
     l.ssfft_status_string.argtypes = [_int]
     l.ssfft_status_string.restype = ctypes.c_char_p
     l.ssfft_last_cuda_error.restype = ctypes.c_char_p
-    for name in ("ssfft_size_minimum", "ssfft_size_maximum", "ssfft_real_size_minimum", "ssfft_real_size_maximum"):
+    for name in ("ssfft_size_minimum", "ssfft_size_maximum", "ssfft_real_size_minimum", "ssfft_real_size_maximum",
+                 "ssfft_size_minimum_smooth", "ssfft_size_maximum_smooth", "ssfft_real_size_minimum_smooth",
+                 "ssfft_real_size_maximum_smooth"):
         getattr(l, name).argtypes = [_sz]
         getattr(l, name).restype = _sz
+    l.ssfft_plans_created.argtypes = []
+    l.ssfft_plans_created.restype = _sz
     l.ssfft_plan_create.argtypes = [ctypes.POINTER(_vp), _sz, _int, _int, _sz]
     l.ssfft_plan_destroy.argtypes = [_vp]
     l.ssfft_plan_create_ex.argtypes = [ctypes.POINTER(_vp), _sz, _int, _int, _sz, ctypes.POINTER(PlanOptions)]
@@ -204,6 +208,31 @@ def real_size_minimum(n: int) -> int:
 def real_size_maximum(n: int) -> int:
     """RealFFT<V>::sizeMaximum (signalsmith-fft.h:406-408)."""
     return int(lib().ssfft_real_size_maximum(n))
+
+
+def size_minimum_smooth(n: int) -> int:
+    """Smallest 2^a 3^b 5^c >= n (opt-in; the reference's sizeMinimum never picks a 5)."""
+    return int(lib().ssfft_size_minimum_smooth(n))
+
+
+def size_maximum_smooth(n: int) -> int:
+    """Largest 2^a 3^b 5^c <= n (opt-in; the reference's sizeMaximum never picks a 5)."""
+    return int(lib().ssfft_size_maximum_smooth(n))
+
+
+def real_size_minimum_smooth(n: int) -> int:
+    """Smallest even m >= n whose half is 2^a 3^b 5^c."""
+    return int(lib().ssfft_real_size_minimum_smooth(n))
+
+
+def real_size_maximum_smooth(n: int) -> int:
+    """Largest even m <= n whose half is 2^a 3^b 5^c (0 when n < 2)."""
+    return int(lib().ssfft_real_size_maximum_smooth(n))
+
+
+def plans_created() -> int:
+    """Plans this process has created so far (monotonic)."""
+    return int(lib().ssfft_plans_created())
 
 
 def schedule_info(n: int, dtype="f32", kind="complex", batch: int = 1) -> dict:
@@ -457,6 +486,8 @@ class FFT:
 
     sizeMinimum = staticmethod(size_minimum)
     sizeMaximum = staticmethod(size_maximum)
+    sizeMinimumSmooth = staticmethod(size_minimum_smooth)
+    sizeMaximumSmooth = staticmethod(size_maximum_smooth)
 
     def set_size(self, size: int) -> int:
         if size != self._size:
@@ -506,12 +537,19 @@ class RealFFT:
 
     sizeMinimum = staticmethod(real_size_minimum)
     sizeMaximum = staticmethod(real_size_maximum)
+    sizeMinimumSmooth = staticmethod(real_size_minimum_smooth)
+    sizeMaximumSmooth = staticmethod(real_size_maximum_smooth)
 
     def set_size(self, size: int) -> int:
-        self._n = int(size)
-        kind = "real_halfshift" if self.modified else "real"
-        self._plan = Plan(self._n, self._dtype, kind, 1)
-        return self.size()
+        """Returns the complex half size, size // 2, as the reference's RealFFT::setSize does
+        (``return complexFft.setSize(size/2)``, signalsmith-fft.h:434); an unchanged size keeps
+        the plan."""
+        size = int(size)
+        if size != self._n or self._plan is None:
+            self._n = size
+            kind = "real_halfshift" if self.modified else "real"
+            self._plan = Plan(self._n, self._dtype, kind, 1) if size // 2 else None
+        return self._n // 2
 
     def set_size_minimum(self, size: int) -> int:
         return self.set_size(real_size_minimum(size))

@@ -115,10 +115,17 @@ struct Plan {
 // errors
 ssfft_status cuda_fail(cudaError_t e, const char *what);
 
+// Developer switches.  Every schedule experiment the library supports is read from ONE
+// environment variable, SSFFT_DEBUG, a comma-separated list of key=value pairs (e.g.
+// "staged=1,prefetch=0"); no other environment variable changes what the library computes or
+// how.  Read each time a plan (or host-buffer call) asks, so a process can change it between
+// plans.  Returns `dflt` when the key is absent or its value is not an integer.
+long long debug_knob(const char *key, long long dflt);
+
 // roots of unity, schedules and tables
 void unit_root(unsigned long long k, unsigned long long L, double *re, double *im);
 bool choose_radices(int n, std::vector<int> &radices, bool large_composites = true, bool real_split = false);
-// allow_staged: 0 never, 1 when SSFFT_STAGED=1, 2 always (where the size allows it)
+// allow_staged: 0 never, 1 when the debug switch staged=1 is set, 2 always (where the size allows it)
 bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, Schedule &s, int allow_staged = 1,
                    const Knobs *knobs = nullptr, int fuse = 0);
 // dir: -1 the direction-independent base schedule, 0 forward, 1 inverse (RealFFT plans may fuse

@@ -160,7 +160,7 @@ ssfft_status compile(const std::vector<std::string> &names, const std::string &a
 	for (const auto &n : names) nvrtcAddNameExpression(prog, n.c_str());
 	const std::string archopt = "--gpu-architecture=" + arch;
 	std::vector<const char *> opts = {archopt.c_str(), "-std=c++17", "-lineinfo"};
-	const bool verbose = std::getenv("SSFFT_JIT_VERBOSE") != nullptr;
+	const bool verbose = debug_knob("jit_verbose", 0) != 0;
 	if (verbose) opts.push_back("--ptxas-options=-v");
 	r = nvrtcCompileProgram(prog, (int)opts.size(), opts.data());
 	size_t log_size = 0;

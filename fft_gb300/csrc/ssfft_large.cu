@@ -190,9 +190,9 @@ static ssfft_status large_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind,
 		if (!make_schedule(dtype, (int)Fi, 0, false, 1, s, false)) return SSFFT_ERR_UNSUPPORTED;
 		// G sub-transforms per CTA: 128-256 B segments, <= 1024 threads, <= ~100 KiB smem
 		const long long U0 = last ? F[0] : R;
-		// SSFFT_LARGE_GROUP overrides the group size (experiments; read when the plan is made)
-		const char *ge = std::getenv("SSFFT_LARGE_GROUP");
-		const int group = ge && std::atoi(ge) > 0 ? std::min(64, std::atoi(ge)) : kGroup;
+		// the debug switch large_group overrides the group size (experiments; read when the plan is made)
+		const long long ge = debug_knob("large_group", 0);
+		const int group = ge > 0 ? (int)std::min(64ll, ge) : kGroup;
 		int G = (int)std::min<long long>(group, U0);
 		while (G > 1 && (G * s.threads > kMaxCtaThreads || (size_t)G * s.smem_stride * eb > 100 * 1024)) --G;
 		s.per_cta = G;
@@ -508,8 +508,7 @@ ssfft_status plan_build_large(Plan *p) {
 	std::vector<CUfunction> fns;
 	ssfft_status st = jit_kernels(names, smem_max, fns);
 	if (st != SSFFT_SUCCESS) return st;
-	const char *pf_env = std::getenv("SSFFT_PREFETCH");
-	const bool prefetch = !(pf_env && pf_env[0] == '0');
+	const bool prefetch = debug_knob("prefetch", 1) != 0;
 	for (int i = 0; i < P; ++i) {
 		LargePass &ps = lp->pass[i];
 		ps.fwd = fns[2 * i];

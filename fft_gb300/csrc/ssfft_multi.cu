@@ -56,7 +56,7 @@ struct MultiPlan {
 	size_t total = 0;
 	std::vector<Group> groups;
 	cudaStream_t cap = nullptr;
-	int branches = 8;  // parallel graph branches (SSFFT_MULTI_BRANCHES overrides, up to 32)
+	int branches = 8;  // parallel graph branches (debug switch multi_branches overrides, up to 32)
 	cudaStream_t branch[kMaxBranches] = {};
 	cudaEvent_t fork = nullptr, join[kMaxBranches] = {};
 	std::mutex mu;
@@ -184,8 +184,8 @@ ssfft_status ssfft_multi_create_ex(ssfft_multi_t *out, const size_t *sizes, size
 	for (size_t i = 0; i < order.size(); ++i) order[i] = i;
 	std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return m->groups[a].work > m->groups[b].work; });
 	{
-		const char *env = std::getenv("SSFFT_MULTI_BRANCHES");
-		if (env && std::atoi(env) > 0) m->branches = std::min(kMaxBranches, std::atoi(env));
+		const long long nb_dbg = debug_knob("multi_branches", 0);
+		if (nb_dbg > 0) m->branches = (int)std::min<long long>(kMaxBranches, nb_dbg);
 	}
 	const int nb = m->branches;
 	double load[kMaxBranches] = {};

@@ -113,6 +113,17 @@ ssfft_status noalloc_scratch(float2 **ptr) {
 		void *p = nullptr;
 		e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
 		if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(noalloc scratch)");
+		// Load every kernel of this entry point now: under CUDA's lazy module loading each one
+		// would otherwise be loaded by the first call whose size needs it, which may come later
+		// on a time-critical thread or inside a stream capture.
+		const void *kernels[] = {(const void *)noalloc_pass<2>, (const void *)noalloc_pass<3>,
+		                         (const void *)noalloc_pass<4>, (const void *)noalloc_pass<5>,
+		                         (const void *)noalloc_copy};
+		for (const void *k : kernels) {
+			cudaFuncAttributes fa;
+			e = cudaFuncGetAttributes(&fa, k);
+			if (e != cudaSuccess) return cuda_fail(e, "cudaFuncGetAttributes(noalloc kernels)");
+		}
 		g_noalloc_ptr[dev] = static_cast<float2 *>(p);
 	}
 	*ptr = g_noalloc_ptr[dev];
@@ -127,9 +138,13 @@ using namespace ssfft;
 extern "C" size_t ssfft_fft_noalloc_max_size(void) { return kNoAllocMaxN; }
 
 extern "C" ssfft_status ssfft_fft_noalloc_f32(const void *d_in, void *d_out, size_t n, int inverse, void *stream) {
-	if (!d_in || !d_out || d_in == d_out) return SSFFT_ERR_INVALID_VALUE;
+	if (!d_in || !d_out) return SSFFT_ERR_INVALID_VALUE;
 	if ((uintptr_t)d_in % 8 || (uintptr_t)d_out % 8) return SSFFT_ERR_INVALID_VALUE;
 	if (n == 0 || n > kNoAllocMaxN) return SSFFT_ERR_INVALID_SIZE;
+	// the buffers must not overlap at all: with an odd number of passes the first pass reads
+	// `in` while it writes `out`
+	const uintptr_t a0 = (uintptr_t)d_in, b0 = (uintptr_t)d_out, bytes = (uintptr_t)n * sizeof(float2);
+	if (a0 < b0 + bytes && b0 < a0 + bytes) return SSFFT_ERR_INVALID_VALUE;
 	int rad[64];
 	const int P = noalloc_radices(n, rad);
 	if (P < 0) return SSFFT_ERR_UNSUPPORTED;

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <functional>
 #include <cstdio>
@@ -27,6 +28,24 @@ namespace ssfft {
 // ------------------------------------------------------------------ error plumbing
 
 static thread_local std::string g_last_error;
+
+long long debug_knob(const char *key, long long dflt) {
+	const char *env = std::getenv("SSFFT_DEBUG");
+	if (!env || !*env) return dflt;
+	const size_t klen = std::strlen(key);
+	for (const char *p = env; *p;) {
+		const char *end = std::strchr(p, ',');
+		if (!end) end = p + std::strlen(p);
+		const char *eq = static_cast<const char *>(std::memchr(p, '=', (size_t)(end - p)));
+		if (eq && (size_t)(eq - p) == klen && std::strncmp(p, key, klen) == 0) {
+			char *num_end = nullptr;
+			const long long v = std::strtoll(eq + 1, &num_end, 10);
+			return num_end != eq + 1 ? v : dflt;
+		}
+		p = *end ? end + 1 : end;
+	}
+	return dflt;
+}
 
 ssfft_status cuda_fail(cudaError_t e, const char *what) {
 	char buf[256];
@@ -72,6 +91,54 @@ size_t size_maximum(size_t size) {
 	return p2 * size;
 }
 
+// 5-smooth sizes (2^a 3^b 5^c), which the reference's helpers never return (its fast remainders
+// are 2^a 3^b with b <= 2, :317-325) but which run at full speed here (radix-5 butterflies in
+// registers).  Walks every 3^b 5^c <= limit and rounds each to its nearest power-of-two
+// multiple: O(log^2 n) candidates.
+static bool smooth_scale_up(size_t odd, size_t n, size_t &out) {
+	// smallest odd * 2^a >= n; false if it overflows size_t
+	size_t v = odd;
+	while (v < n) {
+		if (v > SIZE_MAX / 2) return false;
+		v *= 2;
+	}
+	out = v;
+	return true;
+}
+
+size_t smooth_minimum(size_t n) {
+	if (n <= 1) return n;
+	size_t best = 0;
+	for (size_t t = 1;; ) {
+		for (size_t f = t;; ) {
+			size_t v;
+			if (smooth_scale_up(f, n, v) && (best == 0 || v < best)) best = v;
+			if (f >= n || f > SIZE_MAX / 5) break;
+			f *= 5;
+		}
+		if (t >= n || t > SIZE_MAX / 3) break;
+		t *= 3;
+	}
+	return best;  // 0 only when no 5-smooth size >= n fits in size_t
+}
+
+size_t smooth_maximum(size_t n) {
+	if (n <= 1) return n;
+	size_t best = 1;
+	for (size_t t = 1; t <= n; ) {
+		for (size_t f = t; f <= n; ) {
+			size_t v = f;
+			while (v <= n / 2) v *= 2;
+			if (v > best) best = v;
+			if (f > n / 5) break;
+			f *= 5;
+		}
+		if (t > n / 3) break;
+		t *= 3;
+	}
+	return best;
+}
+
 // ------------------------------------------------------------------ FP64 roots of unity
 
 // e^{-2 pi i k / L} in double.  The angle is reduced to the first octant by exact integer
@@ -112,14 +179,10 @@ static bool specialised(int r) {
 }
 
 // Largest radix whose mirror-paired pass (2R values a thread) carries the fused RealFFT split:
-// 8 (SSFFT_FUSE_RADIX overrides for experiments, read once).
+// 8 (debug switch fuse_radix overrides it for experiments).
 static int fuse_radix_limit() {
-	static const int v = [] {
-		const char *e = std::getenv("SSFFT_FUSE_RADIX");
-		const int x = e ? std::atoi(e) : 0;
-		return x >= 2 && x <= 16 ? x : 8;
-	}();
-	return v;
+	const long long x = debug_knob("fuse_radix", 8);
+	return x >= 2 && x <= 16 ? (int)x : 8;
 }
 
 // Fewest passes for 2^a 3^b 5^c over the register radices including the large composites
@@ -407,13 +470,10 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	if (s.smem_stride % 2 == 0) s.smem_stride += 1;  // neighbouring transforms start on other banks
 	const size_t per = (size_t)s.smem_stride * eb;
 	if (per > 227 * 1024) return false;
-	// about 128 threads per CTA (SSFFT_CTA_THREADS overrides), at most 48 KiB of shared memory
-	// unless one transform needs more
-	static const int cta_target = [] {
-		const char *e = std::getenv("SSFFT_CTA_THREADS");
-		const int v = e ? std::atoi(e) : 0;
-		return v > 0 ? v : 128;  // 128 measured best on GB300 (vs 256 / 512)
-	}();
+	// about 128 threads per CTA (debug switch cta_threads overrides), at most 48 KiB of shared
+	// memory unless one transform needs more
+	const long long cta_dbg = debug_knob("cta_threads", 0);
+	const int cta_target = cta_dbg > 0 && cta_dbg <= kMaxCtaThreads ? (int)cta_dbg : 128;  // 128 measured best on GB300
 	int g = std::max(1, (knobs && knobs->cta_threads > 0 ? knobs->cta_threads : cta_target) / t);
 	const size_t soft = std::max<size_t>(per, 48 * 1024);
 	while (g > 1 && (size_t)g * per > soft) --g;
@@ -435,10 +495,9 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	// a whole number of 16-byte units and a group of them fits the copy and shared-memory limits.
 	const size_t sb = eb / 2;
 	const size_t in_bytes = kind == 0 ? (size_t)n * eb : (size_t)2 * n * sb;  // real: n_real = 2h reals or h bins
-	// Opt-in (SSFFT_STAGED=1, read when a plan is made): measured slower than the unstaged
+	// Opt-in (debug switch staged=1, read when a plan is made): measured slower than the unstaged
 	// kernel on GB300 so far.
-	const char *staged_env = std::getenv("SSFFT_STAGED");
-	const bool staged_enabled = staged_env && staged_env[0] == '1';
+	const bool staged_enabled = debug_knob("staged", 0) == 1;
 	if (((allow_staged == 1 && staged_enabled) || allow_staged == 2) && !s.tc && !odd && in_bytes % 16 == 0 && n >= 16) {
 		int gs = s.per_cta;
 		auto staged_smem = [&](int gg) { return (((size_t)gg * in_bytes + 127) & ~(size_t)127) + (size_t)gg * per; };
@@ -450,16 +509,13 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 			s.smem_bytes = staged_smem(gs);
 		}
 	}
-	static const int minb_env = [] {
-		const char *e = std::getenv("SSFFT_MINB");
-		return e ? std::atoi(e) : 0;
-	}();
+	const int minb_env = (int)debug_knob("minb", 0);
 	// Measured on GB300: forcing more resident CTAs (register caps with small spills) did not
 	// beat the compiler's own allocation for the plain kernel of small transforms; the staged
 	// kernel's loop needs a cap of two CTAs.  A FP32 transform holding 32 values a thread in a CTA
 	// of at most 256 threads (8192 points and up) compiles to 128-170 registers, one CTA per SM:
 	// capped at two CTAs (128 registers, no spills) it overlaps one CTA's HBM phase with the
-	// other's arithmetic (complex 8192: 51% -> 74% of the copy bandwidth).  SSFFT_MINB overrides
+	// other's arithmetic (complex 8192: 51% -> 74% of the copy bandwidth).  debug switch minb overrides
 	// for experiments.
 	int mb = s.staged ? 2 : 1;
 	if (!s.staged && dtype == SSFFT_F32 && s.emax == 2 * kElemsPerThread && s.per_cta * s.threads <= 256 &&
@@ -669,11 +725,10 @@ bool pair_schedule(int n, Schedule &s, const Knobs *knobs) {
 // Whether the planner's default for a complex FP32 transform of n points is the two-CTA cluster
 // schedule: off (measured on GB300 slower than the one-CTA schedules at 8192-16384 points:
 // complex 16384 46-53% of the copy bandwidth against 55%, the cluster barriers and
-// distributed-shared-memory reads cost more than the second CTA per SM gains).  SSFFT_PAIR_MIN
+// distributed-shared-memory reads cost more than the second CTA per SM gains).  debug switch pair_min
 // sets the smallest such n for plans made while it is set.
 static bool pair_default(int n) {
-	const char *e = std::getenv("SSFFT_PAIR_MIN");
-	const long long lo = e ? std::atoll(e) : 0;
+	const long long lo = debug_knob("pair_min", 0);
 	return lo > 0 && n >= lo;
 }
 
@@ -700,12 +755,11 @@ bool single_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch,
 	if (dir < 0) return true;
 	// RealFFT (not half-shift), even length, plain kernel, two passes or more, a register radix
 	// <= 8: fuse the split into the last pass (forward) / the pre-twiddle into the first pass
-	// (inverse), with that radix moved to the end / the front.  SSFFT_FUSE=0 turns it off for
+	// (inverse), with that radix moved to the end / the front.  debug switch fuse=0 turns it off for
 	// plans made while it is set; an explicit radix order keeps the base schedule.
-	const char *env = std::getenv("SSFFT_FUSE");
 	// (below 256 reals the unfused kernel measured faster on GB300)
 	const int fuse_knob = knobs ? knobs->fuse : -1;
-	if ((env && env[0] == '0') || kind != SSFFT_REAL || (n & 1) || (n < 256 && fuse_knob != 1) || s.staged ||
+	if (debug_knob("fuse", 1) == 0 || kind != SSFFT_REAL || (n & 1) || (n < 256 && fuse_knob != 1) || s.staged ||
 	    s.tc || s.radices.size() < 2 || fuse_knob == 0)
 		return true;
 	int best = -1;
@@ -781,12 +835,11 @@ long long resident_ctas(CUfunction fwd, CUfunction inv, const Schedule &s, int d
 
 // The plain batch kernel prefetches into L2 the input of the CTA this many blocks ahead: by
 // default one wave of resident CTAs (measured on GB300: complex N=1024 77% -> 92% of the copy
-// bandwidth, RealFFT N=3840 62% -> 70%).  Knob: quarter waves (0 = off); SSFFT_PREFETCH=0 turns
+// bandwidth, RealFFT N=3840 62% -> 70%).  Knob: quarter waves (0 = off); debug switch prefetch=0 turns
 // it off for plans made while it is set.
 long long prefetch_distance(const Schedule &s, const Knobs &k, long long resident) {
 	if (s.staged || s.tc) return 0;
-	const char *env = std::getenv("SSFFT_PREFETCH");
-	if (env && env[0] == '0') return 0;
+	if (debug_knob("prefetch", 1) == 0) return 0;
 	const int quarters = k.prefetch >= 0 ? k.prefetch : 4;
 	// (cluster-pair schedules count in transforms, two CTAs each)
 	return resident * quarters / 4 / (s.pair ? 2 : 1);
@@ -1043,6 +1096,16 @@ size_t ssfft_size_minimum(size_t n) { return size_minimum(n); }
 size_t ssfft_size_maximum(size_t n) { return size_maximum(n); }
 size_t ssfft_real_size_minimum(size_t n) { return (size_minimum((n - 1) / 2) + 1) * 2; }
 size_t ssfft_real_size_maximum(size_t n) { return size_minimum(n / 2) * 2; }
+size_t ssfft_size_minimum_smooth(size_t n) { return smooth_minimum(n); }
+size_t ssfft_size_maximum_smooth(size_t n) { return smooth_maximum(n); }
+size_t ssfft_real_size_minimum_smooth(size_t n) {
+	if (n == 0) return 0;
+	const size_t h = smooth_minimum(n / 2 + (n & 1));
+	return h && h <= SIZE_MAX / 2 ? 2 * h : 0;
+}
+size_t ssfft_real_size_maximum_smooth(size_t n) { return 2 * smooth_maximum(n / 2); }
+
+static std::atomic<size_t> g_plans_created{0};
 
 ssfft_status ssfft_plan_create(ssfft_plan_t *out, size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch) {
 	return ssfft_plan_create_ex(out, n, dtype, kind, batch, nullptr);
@@ -1064,8 +1127,8 @@ ssfft_status ssfft_plan_create_ex(ssfft_plan_t *out, size_t n, ssfft_dtype dtype
 	p->kind = kind;
 	p->batch = batch;
 	static const int autotune_env = [] {
-		const char *e = std::getenv("SSFFT_AUTOTUNE");
-		return e ? std::max(0, std::min(2, std::atoi(e))) : 0;
+		const long long e = debug_knob("autotune", 0);
+		return (int)std::max(0ll, std::min(2ll, e));
 	}();
 	p->autotune = autotune_env;
 	if (opt) {
@@ -1115,8 +1178,11 @@ ssfft_status ssfft_plan_create_ex(ssfft_plan_t *out, size_t n, ssfft_dtype dtype
 		return st;
 	}
 	*out = reinterpret_cast<ssfft_plan_t>(p);
+	g_plans_created.fetch_add(1, std::memory_order_relaxed);
 	return SSFFT_SUCCESS;
 }
+
+size_t ssfft_plans_created(void) { return g_plans_created.load(std::memory_order_relaxed); }
 
 ssfft_status ssfft_plan_tuning(ssfft_plan_t plan, char *choice, size_t choice_len, char *log, size_t log_len) {
 	if (!plan) return SSFFT_ERR_INVALID_VALUE;

@@ -42,20 +42,20 @@ void plan_release(Plan *p) {
 
 // Chunk of ~32 MiB of input per stream (at least one transform), three streams (measured on
 // GB300 with the RealFFT headline frames: 16 MiB 1027-1037, 32-96 MiB 1050-1074 GFLOP/s end to
-// end, 4-8 MiB 861-968; a fourth stream no better).  Experiment switches, read when a plan first
-// runs on host buffers: SSFFT_STAGE_MB (chunk MiB), SSFFT_STAGE_STREAMS (1..4).
+// end, 4-8 MiB 861-968; a fourth stream no better).  Debug switches, read when a plan first runs
+// on host buffers: stage_mb (chunk MiB), stage_streams (1..4).
 static ssfft_status stage_init(Plan *p) {
 	if (p->stage) return SSFFT_SUCCESS;
 	HostStage *st = new HostStage();
 	const size_t per_in = std::max(plan_in_bytes(p, 0, 1), plan_in_bytes(p, 1, 1));
 	const size_t per_out = std::max(plan_out_bytes(p, 0, 1), plan_out_bytes(p, 1, 1));
-	const char *mb_env = std::getenv("SSFFT_STAGE_MB");
-	const size_t mb = mb_env && std::atoi(mb_env) > 0 ? (size_t)std::atoi(mb_env) : 32;
+	const long long mb_dbg = debug_knob("stage_mb", 32);
+	const size_t mb = mb_dbg > 0 ? (size_t)mb_dbg : 32;
 	size_t chunk = std::max<size_t>(1, (mb << 20) / std::max<size_t>(per_in, 1));
 	chunk = std::min(chunk, p->batch);
 	st->chunk = chunk;
-	const char *ns_env = std::getenv("SSFFT_STAGE_STREAMS");
-	const int ns = ns_env && std::atoi(ns_env) > 0 ? std::min(HostStage::kStreams, std::atoi(ns_env)) : 3;
+	const long long ns_dbg = debug_knob("stage_streams", 3);
+	const int ns = ns_dbg > 0 ? (int)std::min<long long>(HostStage::kStreams, ns_dbg) : 3;
 	// multi-pass plans share one scratch buffer, so their chunks run on a single stream
 	st->streams = p->large ? 1 : ns;
 	for (int i = 0; i < st->streams; ++i) {
@@ -101,10 +101,9 @@ extern "C" ssfft_status ssfft_exec_host(ssfft_plan_t plan, int inverse, const vo
 	int prev = -1;
 	cudaGetDevice(&prev);
 	if (prev != p->device) cudaSetDevice(p->device);
-	// zero copy (SSFFT_ZERO_COPY=1): when both buffers are pinned and mapped, the kernel reads and
-	// writes them over the host link directly; no staging copies
-	const char *zc = std::getenv("SSFFT_ZERO_COPY");
-	if (zc && zc[0] == '1' && !p->large) {
+	// zero copy (debug switch zero_copy=1): when both buffers are pinned and mapped, the kernel
+	// reads and writes them over the host link directly; no staging copies
+	if (debug_knob("zero_copy", 0) == 1 && !p->large) {
 		const void *d_in = mapped_host(h_in, plan_in_bytes(p, inverse, p->batch));
 		void *d_out = mapped_host(h_out, plan_out_bytes(p, inverse, p->batch));
 		if (d_in && d_out) {

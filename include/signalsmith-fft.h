@@ -143,6 +143,10 @@ class FFT {
 public:
 	static size_t sizeMinimum(size_t size) { return ssfft_size_minimum(size); }
 	static size_t sizeMaximum(size_t size) { return ssfft_size_maximum(size); }
+	// Extension (opt-in, new names): nearest 2^a 3^b 5^c sizes, which the reference's helpers
+	// never pick but which run as fast here.
+	static size_t sizeMinimumSmooth(size_t size) { return ssfft_size_minimum_smooth(size); }
+	static size_t sizeMaximumSmooth(size_t size) { return ssfft_size_maximum_smooth(size); }
 
 	FFT(size_t size, int fastDirection = 0) {
 		if (fastDirection > 0) size = sizeMinimum(size);
@@ -218,6 +222,9 @@ public:
 	// RealFFT::sizeMinimum / sizeMaximum (reference :403-408), quirks included.
 	static size_t sizeMinimum(size_t size) { return ssfft_real_size_minimum(size); }
 	static size_t sizeMaximum(size_t size) { return ssfft_real_size_maximum(size); }
+	// Extension (opt-in, new names): nearest even sizes whose half is 2^a 3^b 5^c.
+	static size_t sizeMinimumSmooth(size_t size) { return ssfft_real_size_minimum_smooth(size); }
+	static size_t sizeMaximumSmooth(size_t size) { return ssfft_real_size_maximum_smooth(size); }
 
 	RealFFT(size_t size, int fastDirection = 0) {
 		if (fastDirection > 0) size = sizeMinimum(size);
@@ -225,14 +232,21 @@ public:
 		setSize(size);
 	}
 
+	// Returns the size of the complex transform inside, size/2, as the reference does
+	// (`return complexFft.setSize(size/2)`, :434); setSizeMinimum / setSizeMaximum return the
+	// same (:436-441).  An unchanged size keeps the plans (the reference's FFT::setSize is a no-op
+	// then, :357); the real length itself is the key, because the split twiddles depend on it
+	// (:420-425), so 6 and 7 are different plans with the same half size.
 	size_t setSize(size_t size) {
-		_n = size;
-		stage_real.assign(size, V());
-		stage_bins.assign(size / 2, complex());
-		host_plan.reset();
-		device_plan.reset();
-		if (size / 2) host_plan.get(size, gpu_detail::DType<V>::value, kind, 1);
-		return this->size();
+		if (size != _n) {
+			_n = size;
+			stage_real.assign(size, V());
+			stage_bins.assign(size / 2, complex());
+			host_plan.reset();
+			device_plan.reset();
+			if (size / 2) host_plan.get(size, gpu_detail::DType<V>::value, kind, 1);
+		}
+		return _n / 2;
 	}
 	size_t setSizeMinimum(size_t size) { return setSize(sizeMinimum(size)); }
 	size_t setSizeMaximum(size_t size) { return setSize(sizeMaximum(size)); }

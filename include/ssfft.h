@@ -67,6 +67,17 @@ size_t ssfft_size_minimum(size_t n);       /* FFT<V>::sizeMinimum      signalsmi
 size_t ssfft_size_maximum(size_t n);       /* FFT<V>::sizeMaximum      signalsmith-fft.h:338-348 */
 size_t ssfft_real_size_minimum(size_t n);  /* RealFFT<V>::sizeMinimum  signalsmith-fft.h:403-405 */
 size_t ssfft_real_size_maximum(size_t n);  /* RealFFT<V>::sizeMaximum  signalsmith-fft.h:406-408 */
+/* Opt-in 5-smooth variants.  The reference's helpers above never pick a factor of 5 (their fast
+ * remainders are 2^a 3^b with b <= 2, signalsmith-fft.h:317-348); these return the nearest
+ * 2^a 3^b 5^c instead, which this library runs as fast (radix-5 butterflies in registers):
+ *   ssfft_size_minimum_smooth(n): smallest 2^a 3^b 5^c >= n (0 -> 0; 0 if none fits in size_t);
+ *   ssfft_size_maximum_smooth(n): largest 2^a 3^b 5^c <= n (0 -> 0);
+ *   ssfft_real_size_minimum_smooth(n): smallest even m >= n with m/2 5-smooth (0 -> 0);
+ *   ssfft_real_size_maximum_smooth(n): largest even m <= n with m/2 5-smooth (0 if n < 2). */
+size_t ssfft_size_minimum_smooth(size_t n);
+size_t ssfft_size_maximum_smooth(size_t n);
+size_t ssfft_real_size_minimum_smooth(size_t n);
+size_t ssfft_real_size_maximum_smooth(size_t n);
 
 /* ---------------------------------------------------------------- plans
  * Replaces FFT<V>(size) / setSize (signalsmith-fft.h:350-363, setPlan :139-185) and
@@ -77,6 +88,9 @@ size_t ssfft_real_size_maximum(size_t n);  /* RealFFT<V>::sizeMaximum  signalsmi
  * real kinds).  Plans are bound to the device that was current at creation. */
 ssfft_status ssfft_plan_create(ssfft_plan_t *plan, size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch);
 ssfft_status ssfft_plan_destroy(ssfft_plan_t plan);
+/* Plans created successfully by this process so far (a monotonic count; diagnostics, e.g. to
+ * check that a front end reuses its plans).  No reference counterpart. */
+size_t ssfft_plans_created(void);
 
 /* Schedule options for ssfft_plan_create_ex (zero-initialise; 0 = planner default).  No reference
  * counterpart: the reference's plan is fixed by its factorisation (setPlan :139-185). */
@@ -229,10 +243,11 @@ ssfft_status ssfft_server_loadgen(ssfft_server_t srv, const ssfft_loadgen_config
  * the process exits.  It creates no plan and calls no allocator.
  *   - n must be 2^a 3^b 5^c and at most ssfft_fft_noalloc_max_size() (= 1048576); larger sizes
  *     return SSFFT_ERR_INVALID_SIZE, other prime factors SSFFT_ERR_UNSUPPORTED;
- *   - d_in and d_out are distinct, 8-byte aligned device buffers of n complex floats; inverse != 0
- *     computes the unnormalised inverse, as ssfft_exec does;
- *   - the first call on each device looks up the scratch array's device address; make that first
- *     call before any stream capture;
+ *   - d_in and d_out are 8-byte aligned device buffers of n complex floats that do not overlap
+ *     (SSFFT_ERR_INVALID_VALUE otherwise); inverse != 0 computes the unnormalised inverse, as
+ *     ssfft_exec does;
+ *   - the first call on each device looks up the scratch array's device address and loads all of
+ *     this entry point's kernels; make that first call before any stream capture;
  *   - every call uses the same array: calls that can overlap on the GPU (other streams, other
  *     host threads) race, so the caller must serialise them.  Nothing needs clearing between
  *     calls: a call reads only scratch values it wrote itself. */

@@ -4,7 +4,9 @@ Two CPU implementations sit behind one numpy-level interface:
 
 * ``port``      -- ``oracle/liboracle.so``, the plain-C restatement of the reference header
   signalsmith-fft.h in ``oracle/ssfft_oracle.c`` (builds on any host; it is what the GPU
-  host runs as checker and CPU baseline).
+  host runs as checker).
+* ``port_native`` -- ``oracle/liboracle_native.so``, the same source built for speed (host vector
+  ISA, FP contraction allowed): the CPU baseline's timing build, never a checker.
 * ``reference`` -- ``oracle/_ref/libssref.so``, the unmodified reference header compiled behind a
   C shim (``oracle/ref_shim.cpp``); only exists where the reference checkout was available.
 
@@ -27,6 +29,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "liboracle.so")
+NATIVE_SO = os.path.join(HERE, "liboracle_native.so")
 REF_SO = os.path.join(HERE, "_ref", "libssref.so")
 _lock = threading.Lock()
 _libs: dict = {}
@@ -36,12 +39,23 @@ _c_int = ctypes.c_int
 _vp = ctypes.c_void_p
 
 
-def build(reference: bool = False) -> None:
-    """Compile liboracle.so (and, if asked and the reference checkout exists, the reference shim)."""
-    targets = ["all"]
+def build(reference: str | None = None) -> None:
+    """Compile liboracle.so; with `reference` (the directory of a reference checkout, holding
+    signalsmith-fft.h) also the reference shim oracle/_ref/libssref.so."""
+    subprocess.run(["make", "-s", "-C", HERE, "all", "native"], check=True)
     if reference:
-        targets.append("ref")
-    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_DIR={reference}"], check=True)
+
+
+def reference_dir() -> str | None:
+    """The reference checkout used to build the shim: $REF_DIR, else a checkout named `reference`
+    beside this repository, if it holds signalsmith-fft.h; None otherwise (e.g. on hosts that only
+    carry this repository)."""
+    cands = [os.environ.get("REF_DIR"), os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")]
+    for c in cands:
+        if c and os.path.exists(os.path.join(c, "signalsmith-fft.h")):
+            return c
+    return None
 
 
 def reference_available() -> bool:
@@ -75,6 +89,11 @@ def lib(kind: str = "port"):
             if not os.path.exists(PORT_SO):
                 build()
             l = _bind(ctypes.CDLL(PORT_SO), "oracle_")
+        elif kind == "port_native":
+            # the same restatement built for speed (timing legs only; never a checker)
+            if not os.path.exists(NATIVE_SO):
+                build()
+            l = _bind(ctypes.CDLL(NATIVE_SO), "oracle_")
         elif kind == "reference":
             if not os.path.exists(REF_SO):
                 raise FileNotFoundError("oracle/_ref/libssref.so was not built (no reference checkout here)")
@@ -86,7 +105,13 @@ def lib(kind: str = "port"):
 
 
 def _prefix(kind: str) -> str:
-    return "oracle_" if kind == "port" else "ref_"
+    return "ref_" if kind == "reference" else "oracle_"
+
+
+def native_flags() -> str:
+    """Compiler command line of the timing build (liboracle_native.so)."""
+    r = subprocess.run(["make", "-s", "-C", HERE, "flags"], capture_output=True, text=True)
+    return r.stdout.strip()
 
 
 def _sfx(dtype) -> str:

@@ -87,6 +87,19 @@ int run_batch(int real, int modified, int inverse, size_t n, size_t batch, const
 	return 0;
 }
 
+// Return values of the size-setting members on a fresh object of class `cls` (0 FFT<double>,
+// 1 RealFFT<double>, 2 ModifiedRealFFT<double>) made with size `first`: out[0] = setSize(n),
+// out[1] = size() after it, out[2] = setSizeMinimum(n), out[3] = setSizeMaximum(n),
+// out[4] = size() after that.
+template <class T>
+void setsize_returns(size_t first, size_t n, size_t *out) {
+	T f(first);
+	out[0] = f.setSize(n);
+	out[1] = f.size();
+	out[2] = f.setSizeMinimum(n);
+	out[3] = f.setSizeMaximum(n);
+	out[4] = f.size();
+}
 }  // namespace
 
 extern "C" {
@@ -105,6 +118,14 @@ int ref_batch_f64(int real, int modified, int inverse, size_t n, size_t batch, c
 int ref_batch_f32(int real, int modified, int inverse, size_t n, size_t batch, const float *in, float *out,
                   int nthreads, size_t repeats) {
 	return run_batch<float>(real, modified, inverse, n, batch, in, out, nthreads, repeats);
+}
+int ref_setsize_returns(int cls, size_t first, size_t n, size_t *out) {
+	switch (cls) {
+	case 0: setsize_returns<signalsmith::FFT<double>>(first, n, out); return 0;
+	case 1: setsize_returns<signalsmith::RealFFT<double>>(first, n, out); return 0;
+	case 2: setsize_returns<signalsmith::ModifiedRealFFT<double>>(first, n, out); return 0;
+	}
+	return -1;
 }
 size_t ref_size_minimum(size_t n) { return signalsmith::FFT<double>::sizeMinimum(n); }
 size_t ref_size_maximum(size_t n) { return signalsmith::FFT<double>::sizeMaximum(n); }

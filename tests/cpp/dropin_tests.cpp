@@ -155,6 +155,50 @@ static void real_vs_complex() {
 	}
 }
 
+// Return values of setSize / setSizeMinimum / setSizeMaximum and size(), against the table the
+// reference itself produced (tests/golden, passed in as a text file: one case per line,
+// "class first n setSize size setSizeMinimum setSizeMaximum size"; class 0 FFT, 1 RealFFT,
+// 2 ModifiedRealFFT).  RealFFT returns the complex half size (reference :434-441).
+template <class T>
+static void setsize_case(size_t first, size_t n, const size_t *want, int cls) {
+	T f(first);
+	size_t got[5];
+	got[0] = f.setSize(n);
+	got[1] = f.size();
+	got[2] = f.setSizeMinimum(n);
+	got[3] = f.setSizeMaximum(n);
+	got[4] = f.size();
+	for (int k = 0; k < 5; ++k)
+		CHECK(got[k] == want[k], "setSize returns: class %d first %zu n %zu item %d: %zu != %zu", cls, first, n, k,
+		      got[k], want[k]);
+}
+
+static void setsize_returns(const char *path) {
+	FILE *fp = std::fopen(path, "r");
+	CHECK(fp != nullptr, "cannot open %s", path);
+	if (!fp) return;
+	int cls;
+	size_t first, n, w[5];
+	int cases = 0;
+	while (std::fscanf(fp, "%d %zu %zu %zu %zu %zu %zu %zu", &cls, &first, &n, &w[0], &w[1], &w[2], &w[3], &w[4]) == 8) {
+		if (cls == 0) setsize_case<signalsmith::FFT<double>>(first, n, w, cls);
+		if (cls == 1) setsize_case<signalsmith::RealFFT<double>>(first, n, w, cls);
+		if (cls == 2) setsize_case<signalsmith::ModifiedRealFFT<double>>(first, n, w, cls);
+		++cases;
+	}
+	std::fclose(fp);
+	CHECK(cases > 0, "no setSize cases read");
+	// an unchanged size keeps the plans (reference FFT::setSize :357 is a no-op then)
+	signalsmith::RealFFT<float> r(3840);
+	signalsmith::FFT<float> c(1024);
+	const size_t before = ssfft_plans_created();
+	CHECK(r.setSize(3840) == 1920, "RealFFT setSize return");
+	CHECK(c.setSize(1024) == 1024, "FFT setSize return");
+	CHECK(ssfft_plans_created() == before, "unchanged setSize made %zu new plans", ssfft_plans_created() - before);
+	r.setSize(3842);
+	CHECK(ssfft_plans_created() == before + 1, "changed setSize must plan once");
+}
+
 static void device_overloads() {
 	const size_t n = 1920, batch = 64;
 	vector<complex<float>> h(n * batch), back(n * batch), one(n);
@@ -181,7 +225,8 @@ static void device_overloads() {
 	cudaFree(d_out);
 }
 
-int main() {
+int main(int argc, char **argv) {
+	if (argc > 1) setsize_returns(argv[1]);
 	individual_bins<double>(1e-6);
 	individual_bins<float>(1e-6);
 	linearity<double>(1e-6);

@@ -31,7 +31,22 @@ def test_dropin_header_compiles_cxx11(tmp_path):
 
 
 @pytest.mark.gpu
-def test_dropin_reference_suite_on_gpu(tmp_path):
+def test_dropin_reference_suite_on_gpu(tmp_path, golden):
+    """The reference suite's checks, plus the setSize family's return values against the table
+    the reference produced (RealFFT returns the half size) and plan reuse on an unchanged size."""
     exe = build_dropin(tmp_path)
-    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=900)
+    cases = tmp_path / "setsize.txt"
+    cases.write_text("\n".join(" ".join(str(int(v)) for v in row) for row in golden["setsize_returns"]) + "\n")
+    r = subprocess.run([str(exe), str(cases)], capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stdout[-4000:] + r.stderr[-2000:]
+
+
+def test_golden_setsize_table_is_the_reference_contract(golden):
+    """The fixture's RealFFT rows return the half size (reference :434) and FFT rows the size."""
+    t = golden["setsize_returns"]
+    assert len(t) >= 30
+    for cls, first, n, r_set, size1, r_min, r_max, size2 in t:
+        if cls == 0:
+            assert r_set == n and size1 == n and r_max == size2
+        else:
+            assert r_set == n // 2 and size1 == 2 * (n // 2) and size2 == 2 * r_max

@@ -76,14 +76,14 @@ def tc_matrix(r0):
 @pytest.fixture(scope="module", autouse=True)
 def staged_schedules():
     """The emulator covers both the plain and the bulk-copy staged kernels: plans made while this
-    module runs may pick the staged kernel (SSFFT_STAGED=1); the setting is restored afterwards."""
-    old = os.environ.get("SSFFT_STAGED")
-    os.environ["SSFFT_STAGED"] = "1"
+    module runs may pick the staged kernel (SSFFT_DEBUG=staged=1); the setting is restored afterwards."""
+    old = os.environ.get("SSFFT_DEBUG")
+    os.environ["SSFFT_DEBUG"] = "staged=1"
     yield
     if old is None:
-        os.environ.pop("SSFFT_STAGED", None)
+        os.environ.pop("SSFFT_DEBUG", None)
     else:
-        os.environ["SSFFT_STAGED"] = old
+        os.environ["SSFFT_DEBUG"] = old
 
 
 @pytest.fixture(scope="module")
@@ -99,7 +99,7 @@ def emulator(staged_schedules, tmp_path_factory):
     for case, var in cases:
         (n, dt, kind, pb, _) = case
         # offset-table launches run the plain kernel (the library routes them off the staged one)
-        os.environ["SSFFT_STAGED"] = "0" if var == "offs" else "1"
+        os.environ["SSFFT_DEBUG"] = "staged=0" if var == "offs" else "staged=1"
         F.schedule_options(**VARIANTS[var])
         for inv in (False, True):
             # a RealFFT plan may run a different radix order per direction (fused split)
@@ -112,7 +112,7 @@ def emulator(staged_schedules, tmp_path_factory):
                          f'{info["smem_bytes"]}, {cluster}}},')
         F.schedule_options()
         F.schedule_direction(False)
-    os.environ["SSFFT_STAGED"] = "1"
+    os.environ["SSFFT_DEBUG"] = "staged=1"
     (d / "emu_cases.inc").write_text("\n".join(lines) + "\n")
     exe = d / "emu"
     cmd = ["g++", "-std=c++20", "-O1", "-pthread", "-w", "-I", str(d), "-I", os.path.join(ROOT, "tests", "emu"),
@@ -234,12 +234,12 @@ def test_emulated_offset_table(emulator, case, var):
     sdt = np.float32 if dt == "f32" else np.float64
     cdt = np.complex64 if dt == "f32" else np.complex128
     ci, info = index[(n, dt, kind, pb, False, var)]
-    os.environ["SSFFT_STAGED"] = "0" if var == "offs" else "1"
+    os.environ["SSFFT_DEBUG"] = "staged=0" if var == "offs" else "staged=1"
     F.schedule_options(**VARIANTS[var])
     name = F.schedule_name(n, dt, kind, pb)
     tabs = F.schedule_tables(n, dt, kind, pb)
     F.schedule_options()
-    os.environ["SSFFT_STAGED"] = "1"
+    os.environ["SSFFT_DEBUG"] = "staged=1"
     assert "batch_staged" not in name, name
     gap = 3
     offs = np.array([g * (n + gap) + 1 for g in range(eb)], dtype=np.int64)  # complex units

@@ -1,4 +1,4 @@
-"""Two-CTA cluster (pair) kernel for long complex FP32 transforms (an option; SSFFT_PAIR_MIN turns
+"""Two-CTA cluster (pair) kernel for long complex FP32 transforms (an option; SSFFT_DEBUG=pair_min=<n> turns
 it on by size): the planner's splits, explicit splits, the single-CTA schedule of the same sizes,
 uneven batches that mix pair and single-CTA sizes, and option validation -- all against the
 oracle."""
@@ -47,7 +47,7 @@ def _complex_case(F, n, batch, expect_pair=True, **opts):
 
 @pytest.mark.parametrize("n", [9000, 10000, 12288, 13824, 15000, 15552, 16000, 16384])
 def test_default_pair_splits(F, n, monkeypatch):
-    monkeypatch.setenv("SSFFT_PAIR_MIN", "8193")  # the planner's split where the pair kernel is on
+    monkeypatch.setenv("SSFFT_DEBUG", "pair_min=8193")  # the planner's split where the pair kernel is on
     _complex_case(F, n, 37)
 
 
@@ -69,13 +69,13 @@ def test_single_cta_schedule_of_pair_sizes(F, n):
 
 
 def test_pair_register_cap(F, monkeypatch):
-    monkeypatch.setenv("SSFFT_PAIR_MIN", "8193")
+    monkeypatch.setenv("SSFFT_DEBUG", "pair_min=8193")
     _complex_case(F, 16384, 23, min_ctas_per_sm=3)
 
 
 def test_uneven_batch_with_pair_sizes(F, monkeypatch):
     import torch
-    monkeypatch.setenv("SSFFT_PAIR_MIN", "8193")
+    monkeypatch.setenv("SSFFT_DEBUG", "pair_min=8193")
     sizes = [16384, 64, 9000, 4096, 12288, 15000, 16384, 100, 13824, 10000] * 3
     rng = np.random.default_rng(5)
     total = sum(sizes)
@@ -95,7 +95,7 @@ def test_uneven_batch_with_pair_sizes(F, monkeypatch):
 
 
 def test_pair_autotune(F, monkeypatch):
-    monkeypatch.setenv("SSFFT_PAIR_MIN", "8193")
+    monkeypatch.setenv("SSFFT_DEBUG", "pair_min=8193")
     _complex_case(F, 16384, 64, expect_pair=None, autotune=1)
 
 

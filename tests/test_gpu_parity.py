@@ -257,16 +257,16 @@ def test_reference_shaped_api(F):
 
 
 def test_staged_kernels_report_no_error(F, monkeypatch):
-    """The bulk-copy staged kernels (SSFFT_STAGED=1 when the plan is made) bound their waits and
+    """The bulk-copy staged kernels (SSFFT_DEBUG=staged=1 when the plan is made) bound their waits and
     report a per-plan flag; after normal runs (aligned and misaligned inputs, partial last
     group) it must read zero, and the results match the oracle."""
     rng = np.random.default_rng(12)
     n, b = 1920, 301
     x = rng.standard_normal((b, n)).astype(np.float32)
-    monkeypatch.setenv("SSFFT_STAGED", "1")
+    monkeypatch.setenv("SSFFT_DEBUG", "staged=1")
     assert "batch_staged" in F.schedule_name(n, "f32", "real", b)
     p = F.Plan(n, "f32", "real", b)
-    monkeypatch.delenv("SSFFT_STAGED")
+    monkeypatch.delenv("SSFFT_DEBUG")
     xi = dev(x)
     out = torch.empty((b, n // 2), dtype=torch.complex64, device="cuda")
     p.exec(False, xi.data_ptr(), out.data_ptr(), 0)

@@ -35,6 +35,62 @@ def test_size_helpers_bit_exact(golden):
     assert F.real_size_maximum(480) == 512 and F.real_size_minimum(480) == 514
 
 
+def _smooth_table(limit: int) -> np.ndarray:
+    """Every 2^a 3^b 5^c <= limit, ascending (brute force)."""
+    out = []
+    a = 1
+    while a <= limit:
+        b = a
+        while b <= limit:
+            c = b
+            while c <= limit:
+                out.append(c)
+                c *= 5
+            b *= 3
+        a *= 2
+    return np.array(sorted(out), dtype=np.int64)
+
+
+def test_smooth_size_helpers_against_brute_force():
+    """Opt-in 5-smooth helpers (no reference counterpart: the reference never picks a 5,
+    signalsmith-fft.h:317-348) against a brute-force table for every n in 1..2^20."""
+    lib = F.lib()
+    top = 1 << 20
+    tab = _smooth_table(4 * top)
+    n = np.arange(1, top + 1, dtype=np.int64)
+    want_min = tab[np.searchsorted(tab, n, side="left")]
+    want_max = tab[np.searchsorted(tab, n, side="right") - 1]
+    fmin, fmax = lib.ssfft_size_minimum_smooth, lib.ssfft_size_maximum_smooth
+    rmin, rmax = lib.ssfft_real_size_minimum_smooth, lib.ssfft_real_size_maximum_smooth
+    got_min = np.fromiter((fmin(int(i)) for i in n), dtype=np.int64, count=top)
+    got_max = np.fromiter((fmax(int(i)) for i in n), dtype=np.int64, count=top)
+    assert np.array_equal(got_min, want_min)
+    assert np.array_equal(got_max, want_max)
+    # real lengths: even m with m/2 5-smooth
+    half_up = (n + 1) // 2
+    want_rmin = 2 * tab[np.searchsorted(tab, half_up, side="left")]
+    half_dn = n // 2
+    want_rmax = np.where(half_dn >= 1, 2 * tab[np.maximum(np.searchsorted(tab, half_dn, side="right") - 1, 0)], 0)
+    sample = n[::7]
+    got_rmin = np.array([rmin(int(i)) for i in sample], dtype=np.int64)
+    got_rmax = np.array([rmax(int(i)) for i in sample], dtype=np.int64)
+    assert np.array_equal(got_rmin, want_rmin[::7])
+    assert np.array_equal(got_rmax, want_rmax[::7])
+    assert fmin(0) == 0 and fmax(0) == 0 and rmin(0) == 0 and rmax(1) == 0 and rmin(1) == 2
+    # large arguments: exact and no overflow
+    for m in ((1 << 62) + 1, (1 << 63) - 1, 3 ** 39 + 2):
+        odd = [3 ** b * 5 ** c for b in range(41) for c in range(28) if 3 ** b * 5 ** c < (1 << 66)]
+        up = min(f << max(0, (m - 1) // f).bit_length() if f < m else f for f in odd)
+        assert fmin(m) == (up if up < (1 << 64) else 0), m
+        lo = max(f << ((m // f).bit_length() - 1) for f in odd if f <= m)
+        assert fmax(m) == lo, m
+    assert fmin(2 ** 63) == 2 ** 63
+    assert fmin(2 ** 64 - 1) == 0  # no 5-smooth size >= 2^64 - 1 fits in size_t
+    # the Python and drop-in names
+    assert F.FFT.sizeMinimumSmooth(481) == 486 and F.FFT.sizeMaximumSmooth(481) == 480
+    assert F.RealFFT.sizeMinimumSmooth(961) == 972 and F.RealFFT.sizeMaximumSmooth(961) == 960
+
+
 def test_status_strings():
     lib = F.lib()
     for code in range(10):
@@ -76,10 +132,10 @@ def test_small_and_odd_kernels_compile_for_sm103a(n):
 @pytest.mark.parametrize("n, dt, kind", [(1024, "f32", "complex"), (3840, "f32", "real"), (1024, "f64", "complex")])
 def test_staged_kernels_compile_for_sm103a(n, dt, kind, monkeypatch):
     """The bulk-copy staged variant (opt-in) and the failure-detection launch use it."""
-    monkeypatch.setenv("SSFFT_STAGED", "1")
+    monkeypatch.setenv("SSFFT_DEBUG", "staged=1")
     assert "batch_staged" in F.schedule_name(n, dt, kind, 64)
     assert F.jit_check(n, dt, kind, 64, "sm_103a") > 0
-    monkeypatch.delenv("SSFFT_STAGED")
+    monkeypatch.delenv("SSFFT_DEBUG")
     assert "batch_staged" not in F.schedule_name(n, dt, kind, 64)
 
 
@@ -115,7 +171,7 @@ def test_planner_policies_for_long_and_mid_transforms(monkeypatch):
     assert F.schedule_info(3840, "f32", "real", 16384)["radices"] == [16, 15, 8]
     assert F.schedule_info(480, "f32", "real", 16384)["radices"] == [16, 15]
     assert not F.schedule_name(16384, "f32", "complex", 64).startswith("ssfft_cl::pair<")
-    monkeypatch.setenv("SSFFT_PAIR_MIN", "8193")
+    monkeypatch.setenv("SSFFT_DEBUG", "pair_min=8193")
     assert F.schedule_name(16384, "f32", "complex", 64).startswith("ssfft_cl::pair<")
     assert not F.schedule_name(8192, "f32", "complex", 64).startswith("ssfft_cl::pair<")
 
