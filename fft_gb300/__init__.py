@@ -711,7 +711,8 @@ def fast_sizes(lo: int, hi: int) -> list:
 
 
 class Multi:
-    """ssfft_multi_*: one submission of complex transforms of uneven sizes stored back to back."""
+    """ssfft_multi_*: one submission of complex transforms of uneven sizes stored back to back
+    (a CUDA graph of work-item queue kernels, one per class of CTA shapes)."""
 
     def __init__(self, sizes, dtype="f32", autotune: int = 0, precision="fp32"):
         l = lib()
@@ -722,6 +723,8 @@ class Multi:
             l.ssfft_multi_exec.argtypes = [_vp, _int, _vp, _vp, _vp]
             l.ssfft_multi_exec_plain.argtypes = [_vp, _int, _vp, _vp, _vp]
             l.ssfft_multi_info.argtypes = [_vp, ctypes.POINTER(_sz), ctypes.POINTER(_sz)]
+            l.ssfft_multi_launches.argtypes = [_vp]
+            l.ssfft_multi_launches.restype = _sz
             l.ssfft_multi_destroy.argtypes = [_vp]
             for name in ("ssfft_multi_create", "ssfft_multi_create_ex", "ssfft_multi_exec", "ssfft_multi_exec_plain", "ssfft_multi_info",
                          "ssfft_multi_destroy"):
@@ -745,7 +748,8 @@ class Multi:
     def info(self) -> dict:
         a, b = _sz(), _sz()
         check(lib().ssfft_multi_info(self._h, ctypes.byref(a), ctypes.byref(b)), "multi_info")
-        return {"distinct_sizes": a.value, "total_elements": b.value}
+        return {"distinct_sizes": a.value, "total_elements": b.value,
+                "launches": int(lib().ssfft_multi_launches(self._h))}
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:

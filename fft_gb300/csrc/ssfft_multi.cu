@@ -2,19 +2,29 @@
 //
 // The reference transforms one size per FFT object, so a caller with transforms of many sizes
 // loops over objects (signalsmith-fft.h:374-386 per call).  ssfft_multi_* takes the whole list
-// once: transforms are grouped by size, each size gets its size-specialised kernel (compiled
-// concurrently at creation) and a device table of its transforms' offsets, so the caller's
-// layout (transform i at the prefix sum of the sizes before it) needs no reordering.  Execution
-// is one CUDA graph whose launches (one per size) sit on up to 8 parallel branches, balanced by
-// work, so small sizes fill the GPU together instead of one after another; the graph is
-// captured once per (input, output, direction) and replayed.  ssfft_multi_exec_plain issues the
-// same launches one after another on the caller's stream, for comparison.
+// once and runs it as a queue of work items:
+//   * every distinct size gets its size-specialised schedule (the planner's) and a device table
+//     of its transforms' offsets, so the caller's layout (transform i at the prefix sum of the
+//     sizes before it) needs no reordering;
+//   * sizes whose schedules share a CTA shape (threads per CTA rounded up to a multiple of 128,
+//     values per thread, register cap) form a class; one kernel per class (ssfft_cl::queue,
+//     compiled concurrently at creation; classes of more than 16 sizes are cut into several)
+//     holds its sizes' passes as compile-time members;
+//   * a class's transforms are cut into work items of as many transforms as one CTA runs, and
+//     the items are queued longest transforms first: CTA b of the class's single launch takes
+//     item b, so the long work starts first and the short work fills the last wave;
+//   * the class launches are one CUDA graph (parallel branches, largest class first, so CTAs of
+//     different classes share the SMs), captured once per (input, output, direction).
+// ssfft_multi_exec_plain issues one plain launch per size, one after another on the caller's
+// stream, for comparison; the debug switch multi_mode=1 runs the earlier design instead (one
+// CUDA graph of per-size launches on parallel branches).
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdlib>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <thread>
@@ -32,6 +42,8 @@ ssfft_status plan_prepare_launch(const Plan *p);
 namespace {
 
 constexpr int kMaxBranches = 32;
+constexpr int kQueueBucket = 128;     // queue CTAs: threads rounded up to a multiple of this
+constexpr size_t kQueueMembers = 16;  // sizes per queue kernel at most
 
 struct Group {
 	size_t n = 0, count = 0;
@@ -48,6 +60,36 @@ struct GraphKey {
 	bool operator<(const GraphKey &o) const { return std::tie(in, out, inverse) < std::tie(o.in, o.out, o.inverse); }
 };
 
+// One queue class: the sizes whose queue schedules share (CTA threads, values per thread,
+// register cap), run by one ssfft_cl::queue launch.
+struct QClass {
+	ssfft_dtype dtype = SSFFT_F32;
+	int cta = 0, emax = 16, minb = 1;
+	size_t smem = 0;
+	std::vector<size_t> members;   // indices into MultiPlan::groups
+	std::vector<Schedule> sch;     // member schedules (per_cta = transforms per work item)
+	CUfunction fwd = nullptr, inv = nullptr;
+	ssfft_cl::QItem *d_items = nullptr;
+	ssfft_cl::QSched *d_sch = nullptr;
+	long long nitems = 0;
+	long long pf_dist = 0;
+	double work = 0;
+	int branch = 0;
+
+	std::string name(bool inverse) const {
+		std::string r = "ssfft_cl::queue<";
+		r += dtype == SSFFT_F32 ? "float" : "double";
+		r += std::string(", ") + (inverse ? "true" : "false") + ", " + std::to_string(cta) + ", " + std::to_string(minb);
+		for (const Schedule &q : sch) {
+			r += ", ssfft_cl::QS<" + std::to_string(q.n) + ", " + std::to_string(q.threads) + ", " +
+			     std::to_string(q.smem_stride) + ", " + std::to_string(q.emax);
+			for (int x : q.radices) r += ", " + std::to_string(x);
+			r += ">";
+		}
+		return r + ">";
+	}
+};
+
 }  // namespace
 
 struct MultiPlan {
@@ -61,9 +103,13 @@ struct MultiPlan {
 	cudaEvent_t fork = nullptr, join[kMaxBranches] = {};
 	std::mutex mu;
 	std::map<GraphKey, cudaGraphExec_t> graphs;
+	bool queue_mode = true;        // work-item queue kernels (false: one launch per size)
+	std::vector<QClass> classes;   // queue mode
+	void *d_queue = nullptr;       // queue mode: items, per-schedule records and twiddle tables
 
 	~MultiPlan() {
 		for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+		if (d_queue) cudaFree(d_queue);
 		for (auto &g : groups) {
 			if (g.d_offs) cudaFree(g.d_offs);
 			if (g.plan) ssfft_plan_destroy(g.plan);
@@ -76,7 +122,25 @@ struct MultiPlan {
 		if (cap) cudaStreamDestroy(cap);
 	}
 
+	ssfft_status launch_queue(int inverse, const void *in, void *out, cudaStream_t *streams) {
+		for (const QClass &c : classes) {
+			ssfft_cl::QueueArgs a;
+			std::memset(&a, 0, sizeof a);
+			a.in = in;
+			a.out = out;
+			a.items = c.d_items;
+			a.nitems = c.nitems;
+			a.sch = c.d_sch;
+			a.pf_dist = c.pf_dist;
+			ssfft_status st = jit_launch(inverse ? c.inv : c.fwd, (unsigned)c.nitems, (unsigned)c.cta, c.smem,
+			                             streams[c.branch], &a);
+			if (st != SSFFT_SUCCESS) return st;
+		}
+		return SSFFT_SUCCESS;
+	}
+
 	ssfft_status launch_all(int inverse, const void *in, void *out, cudaStream_t *streams) {
+		if (queue_mode) return launch_queue(inverse, in, out, streams);
 		for (auto &g : groups) {
 			ssfft_status st = launch_batch_offs(reinterpret_cast<const Plan *>(g.plan), inverse, in, out, g.count,
 			                                    g.d_offs, streams[g.branch]);
@@ -109,7 +173,200 @@ struct MultiPlan {
 		if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
 		return SSFFT_SUCCESS;
 	}
+
+	ssfft_status build_queue();
 };
+
+// Queue schedule of one size: the planner's schedule (no staged or tensor-core variant), its
+// transforms per work item filling a CTA of threads rounded up to kQueueBucket.
+static bool queue_schedule(ssfft_dtype dtype, size_t n, size_t count, Schedule &s, int &cta) {
+	if (!make_schedule(dtype, (int)n, ssfft_cl::kComplex, false, count, s, 0, nullptr, 0)) return false;
+	if (s.staged || s.tc || s.pair) return false;
+	cta = (s.threads + kQueueBucket - 1) / kQueueBucket * kQueueBucket;
+	const size_t eb = dtype == SSFFT_F32 ? 8 : 16;
+	const size_t per = (size_t)s.smem_stride * eb;
+	int g = std::max(1, cta / s.threads);
+	// at most 48 KiB of shared memory per CTA unless one transform needs more (as the planner)
+	while (g > 1 && (size_t)g * per > std::max<size_t>(per, 48 * 1024)) --g;
+	if ((size_t)g > count) g = (int)std::max<size_t>(1, count);
+	s.per_cta = g;
+	s.smem_bytes = (size_t)g * per;
+	return true;
+}
+
+static size_t qalign(size_t v) { return (v + 255) / 256 * 256; }
+
+// The queue classes of distinct sizes (n, transform count, work), largest class first; members
+// index into `sizes`.  No GPU needed.
+static ssfft_status form_classes(ssfft_dtype dtype, const std::vector<std::tuple<size_t, size_t, double>> &sizes,
+                                 std::vector<QClass> &classes) {
+	// classes by (CTA threads, values per thread, register cap of the member's own schedule)
+	std::map<std::tuple<int, int, int>, QClass> cls;
+	for (size_t gi = 0; gi < sizes.size(); ++gi) {
+		Schedule s;
+		int cta = 0;
+		if (!queue_schedule(dtype, std::get<0>(sizes[gi]), std::get<1>(sizes[gi]), s, cta))
+			return SSFFT_ERR_UNSUPPORTED;
+		QClass &c = cls[std::make_tuple(cta, s.emax, s.minb)];
+		c.dtype = dtype;
+		c.cta = cta;
+		c.emax = s.emax;
+		c.minb = std::max(c.minb, s.minb);
+		c.smem = std::max(c.smem, s.smem_bytes);
+		c.members.push_back(gi);
+		c.sch.push_back(s);
+		c.work += std::get<2>(sizes[gi]);
+	}
+	classes.clear();
+	for (auto &kv : cls) {
+		// members longest first (the queue's order)
+		QClass &c = kv.second;
+		std::vector<size_t> ord(c.members.size());
+		for (size_t i = 0; i < ord.size(); ++i) ord[i] = i;
+		std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return c.sch[a].n > c.sch[b].n; });
+		std::vector<size_t> mem;
+		std::vector<Schedule> sch;
+		for (size_t i : ord) {
+			mem.push_back(c.members[i]);
+			sch.push_back(c.sch[i]);
+		}
+		// at most kQueueMembers sizes per kernel: NVRTC's time grows faster than the member count
+		// (71 members 48 s, 24 members 7.6 s), and chunks compile concurrently
+		for (size_t b = 0; b < mem.size(); b += kQueueMembers) {
+			QClass part = c;
+			part.members.assign(mem.begin() + b, mem.begin() + std::min(mem.size(), b + kQueueMembers));
+			part.sch.assign(sch.begin() + b, sch.begin() + std::min(sch.size(), b + kQueueMembers));
+			part.smem = 0;
+			part.work = 0;
+			for (size_t k = 0; k < part.sch.size(); ++k) {
+				part.smem = std::max(part.smem, part.sch[k].smem_bytes);
+				part.work += std::get<2>(sizes[part.members[k]]);
+			}
+			classes.push_back(part);
+		}
+	}
+	std::stable_sort(classes.begin(), classes.end(), [](const QClass &a, const QClass &b) { return a.work > b.work; });
+	return SSFFT_SUCCESS;
+}
+
+// The work items of one class, in queue order: member by member (longest first), each member's
+// transforms in groups of its transforms per CTA.
+static void class_items(const QClass &c, const std::vector<size_t> &counts, std::vector<ssfft_cl::QItem> &items) {
+	items.clear();
+	for (size_t k = 0; k < c.sch.size(); ++k) {
+		const size_t cnt = counts[c.members[k]];
+		const int per = c.sch[k].per_cta;
+		for (size_t f = 0; f < cnt; f += (size_t)per) {
+			ssfft_cl::QItem it;
+			it.k = (int)k;
+			it.count = (int)std::min<size_t>((size_t)per, cnt - f);
+			it.first = (long long)f;
+			items.push_back(it);
+		}
+	}
+}
+
+ssfft_status MultiPlan::build_queue() {
+	std::vector<std::tuple<size_t, size_t, double>> sizes;
+	std::vector<size_t> counts;
+	for (const Group &g : groups) {
+		sizes.emplace_back(g.n, g.count, g.work);
+		counts.push_back(g.count);
+	}
+	ssfft_status fst = form_classes(dtype, sizes, classes);
+	if (fst != SSFFT_SUCCESS) return fst;
+	const size_t smem_limit = device_smem_limit(device);
+	for (const QClass &c : classes)
+		if (c.smem > smem_limit) return SSFFT_ERR_UNSUPPORTED;
+	// one class kernel per compile, concurrently
+	std::atomic<size_t> next{0};
+	std::atomic<int> bad{0};
+	std::vector<std::thread> th;
+	const int nt = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+	const int dev = device;
+	for (int t = 0; t < nt; ++t)
+		th.emplace_back([&, dev] {
+			cudaSetDevice(dev);
+			for (size_t i = next++; i < classes.size(); i = next++) {
+				QClass &c = classes[i];
+				std::vector<CUfunction> fns;
+				if (jit_kernels({c.name(false), c.name(true)}, c.smem, fns) != SSFFT_SUCCESS) {
+					bad = 1;
+					continue;
+				}
+				c.fwd = fns[0];
+				c.inv = fns[1];
+			}
+		});
+	for (auto &x : th) x.join();
+	if (bad) return SSFFT_ERR_CUDA;
+	// device layout: per class its items and member records; then every member's tables
+	std::vector<std::vector<ssfft_cl::QItem>> items(classes.size());
+	std::vector<std::vector<double>> tw_all, roots_all;
+	size_t off = 0;
+	std::vector<size_t> off_items(classes.size()), off_sch(classes.size());
+	for (size_t ci = 0; ci < classes.size(); ++ci) {
+		QClass &c = classes[ci];
+		class_items(c, counts, items[ci]);
+		for (size_t k = 0; k < c.sch.size(); ++k) {
+			std::vector<double> tw, roots;
+			schedule_twiddles(c.sch[k], tw, roots);
+			tw_all.push_back(tw);
+			roots_all.push_back(roots);
+		}
+		c.nitems = (long long)items[ci].size();
+		if (c.nitems > 0x7fffffffLL) return SSFFT_ERR_INVALID_SIZE;
+		off_items[ci] = off;
+		off = qalign(off + items[ci].size() * sizeof(ssfft_cl::QItem));
+		off_sch[ci] = off;
+		off = qalign(off + c.sch.size() * sizeof(ssfft_cl::QSched));
+	}
+	const size_t sb = dtype == SSFFT_F32 ? 4 : 8;
+	std::vector<size_t> off_tw(tw_all.size()), off_roots(tw_all.size());
+	for (size_t i = 0; i < tw_all.size(); ++i) {
+		off_tw[i] = off;
+		off = qalign(off + tw_all[i].size() * sb);
+		off_roots[i] = off;
+		off = qalign(off + roots_all[i].size() * sb);
+	}
+	const size_t total = std::max<size_t>(off, 256);
+	cudaError_t e = cudaMalloc(&d_queue, total);
+	if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(multi queue)");
+	unsigned char *base = static_cast<unsigned char *>(d_queue);
+	std::vector<unsigned char> blob(total, 0);
+	size_t mi = 0;
+	for (size_t ci = 0; ci < classes.size(); ++ci) {
+		QClass &c = classes[ci];
+		std::memcpy(blob.data() + off_items[ci], items[ci].data(), items[ci].size() * sizeof(ssfft_cl::QItem));
+		std::vector<ssfft_cl::QSched> recs(c.sch.size());
+		for (size_t k = 0; k < c.sch.size(); ++k, ++mi) {
+			recs[k].tw = base + off_tw[mi];
+			recs[k].roots = base + off_roots[mi];
+			recs[k].offs = groups[c.members[k]].d_offs;
+			recs[k].n = (long long)c.sch[k].n;
+			for (size_t i = 0; i < tw_all[mi].size(); ++i) {
+				if (sb == 4) reinterpret_cast<float *>(blob.data() + off_tw[mi])[i] = (float)tw_all[mi][i];
+				else reinterpret_cast<double *>(blob.data() + off_tw[mi])[i] = tw_all[mi][i];
+			}
+			for (size_t i = 0; i < roots_all[mi].size(); ++i) {
+				if (sb == 4) reinterpret_cast<float *>(blob.data() + off_roots[mi])[i] = (float)roots_all[mi][i];
+				else reinterpret_cast<double *>(blob.data() + off_roots[mi])[i] = roots_all[mi][i];
+			}
+		}
+		std::memcpy(blob.data() + off_sch[ci], recs.data(), recs.size() * sizeof(ssfft_cl::QSched));
+		c.d_items = reinterpret_cast<ssfft_cl::QItem *>(base + off_items[ci]);
+		c.d_sch = reinterpret_cast<ssfft_cl::QSched *>(base + off_sch[ci]);
+		// L2 prefetch one wave of resident CTAs ahead, as the batch kernel does
+		int sms = 0;
+		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+		const long long resident = (long long)std::min(jit_occupancy(c.fwd, c.cta, c.smem),
+		                                                jit_occupancy(c.inv, c.cta, c.smem)) * std::max(1, sms);
+		c.pf_dist = debug_knob("prefetch", 1) == 0 ? 0 : resident;
+	}
+	e = cudaMemcpy(d_queue, blob.data(), total, cudaMemcpyHostToDevice);
+	if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(multi queue)");
+	return SSFFT_SUCCESS;
+}
 
 }  // namespace ssfft
 
@@ -199,9 +456,20 @@ ssfft_status ssfft_multi_create_ex(ssfft_multi_t *out, const size_t *sizes, size
 	std::vector<Group> sorted;
 	for (size_t i : order) sorted.push_back(m->groups[i]);
 	m->groups.swap(sorted);
+	// the work-item queue (default), except for the tensor-core precision option (per-size
+	// tcgen05 kernels) and the debug switch multi_mode=1 (per-size launches)
+	m->queue_mode = debug_knob("multi_mode", 0) != 1 && !(opt && opt->precision == SSFFT_PRECISION_SPLIT_BF16);
+	if (m->queue_mode) {
+		ssfft_status st = m->build_queue();
+		if (st != SSFFT_SUCCESS) return st;
+		// one graph branch per class, largest class first
+		m->branches = (int)std::min<size_t>(kMaxBranches, std::max<size_t>(1, m->classes.size()));
+		for (size_t i = 0; i < m->classes.size(); ++i) m->classes[i].branch = (int)(i % (size_t)m->branches);
+	}
+	const int nbr = m->branches;
 	e = cudaStreamCreateWithFlags(&m->cap, cudaStreamNonBlocking);
 	if (e == cudaSuccess) e = cudaEventCreateWithFlags(&m->fork, cudaEventDisableTiming);
-	for (int b = 0; b < nb && e == cudaSuccess; ++b) {
+	for (int b = 0; b < nbr && e == cudaSuccess; ++b) {
 		e = cudaStreamCreateWithFlags(&m->branch[b], cudaStreamNonBlocking);
 		if (e == cudaSuccess) e = cudaEventCreateWithFlags(&m->join[b], cudaEventDisableTiming);
 	}
@@ -249,6 +517,12 @@ ssfft_status ssfft_multi_info(ssfft_multi_t multi, size_t *distinct_sizes, size_
 	return SSFFT_SUCCESS;
 }
 
+size_t ssfft_multi_launches(ssfft_multi_t multi) {
+	if (!multi) return 0;
+	const MultiPlan *m = reinterpret_cast<const MultiPlan *>(multi);
+	return m->queue_mode ? m->classes.size() : m->groups.size();
+}
+
 ssfft_status ssfft_multi_destroy(ssfft_multi_t multi) {
 	if (!multi) return SSFFT_ERR_INVALID_VALUE;
 	delete reinterpret_cast<MultiPlan *>(multi);
@@ -256,3 +530,96 @@ ssfft_status ssfft_multi_destroy(ssfft_multi_t multi) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- diagnostics (no GPU)
+
+namespace {
+
+// Distinct sizes of an uneven list as ssfft_multi_create groups them: (n, count, work), sorted by
+// work, largest first (the order the library keeps its groups in).
+ssfft_status multi_groups(const size_t *sizes, size_t count, ssfft_dtype dtype,
+                          std::vector<std::tuple<size_t, size_t, double>> &out) {
+	if (!sizes || count == 0 || (dtype != SSFFT_F32 && dtype != SSFFT_F64)) return SSFFT_ERR_INVALID_VALUE;
+	const size_t max_n = dtype == SSFFT_F32 ? (size_t)kMaxSubTransform : (size_t)kMaxSubTransform / 2;
+	std::map<size_t, size_t> cnt;
+	for (size_t i = 0; i < count; ++i) {
+		if (sizes[i] == 0 || sizes[i] > max_n) return SSFFT_ERR_UNSUPPORTED;
+		++cnt[sizes[i]];
+	}
+	out.clear();
+	for (auto &kv : cnt)
+		out.emplace_back(kv.first, kv.second,
+		                 (double)kv.second * (double)kv.first * std::log2((double)std::max<size_t>(kv.first, 2)));
+	std::stable_sort(out.begin(), out.end(), [](const auto &a, const auto &b) { return std::get<2>(a) > std::get<2>(b); });
+	return SSFFT_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" ssfft_status ssfft_diag_multi_spec(const size_t *sizes, size_t count, ssfft_dtype dtype, char *json,
+                                              size_t json_len, void *blob, size_t *blob_bytes) {
+	std::vector<std::tuple<size_t, size_t, double>> g;
+	ssfft_status st = multi_groups(sizes, count, dtype, g);
+	if (st != SSFFT_SUCCESS) return st;
+	std::vector<QClass> classes;
+	st = form_classes(dtype, g, classes);
+	if (st != SSFFT_SUCCESS) return st;
+	std::vector<size_t> counts;
+	for (auto &x : g) counts.push_back(std::get<1>(x));
+	std::string js = "{\"classes\": [";
+	std::vector<double> tab;
+	for (size_t ci = 0; ci < classes.size(); ++ci) {
+		const QClass &c = classes[ci];
+		std::vector<ssfft_cl::QItem> items;
+		class_items(c, counts, items);
+		js += ci ? ", " : "";
+		js += "{\"fwd\": \"" + c.name(false) + "\", \"inv\": \"" + c.name(true) + "\", \"cta\": " + std::to_string(c.cta) +
+		      ", \"smem\": " + std::to_string(c.smem) + ", \"minb\": " + std::to_string(c.minb) +
+		      ", \"emax\": " + std::to_string(c.emax) + ", \"members\": [";
+		for (size_t k = 0; k < c.sch.size(); ++k) {
+			std::vector<double> tw, roots;
+			schedule_twiddles(c.sch[k], tw, roots);
+			js += k ? ", " : "";
+			js += "{\"n\": " + std::to_string(c.sch[k].n) + ", \"per_cta\": " + std::to_string(c.sch[k].per_cta) +
+			      ", \"threads\": " + std::to_string(c.sch[k].threads) + ", \"tw\": [" + std::to_string(tab.size()) +
+			      ", " + std::to_string(tw.size()) + "]";
+			tab.insert(tab.end(), tw.begin(), tw.end());
+			js += ", \"roots\": [" + std::to_string(tab.size()) + ", " + std::to_string(roots.size()) + "]}";
+			tab.insert(tab.end(), roots.begin(), roots.end());
+		}
+		js += "], \"items\": [";
+		for (size_t i = 0; i < items.size(); ++i)
+			js += (i ? ", [" : "[") + std::to_string(items[i].k) + ", " + std::to_string(items[i].count) + ", " +
+			      std::to_string(items[i].first) + "]";
+		js += "]}";
+	}
+	js += "]}";
+	if (blob_bytes) {
+		if (blob) std::memcpy(blob, tab.data(), std::min(*blob_bytes, tab.size() * sizeof(double)));
+		*blob_bytes = tab.size() * sizeof(double);
+	}
+	if (json && json_len) {
+		if (js.size() + 1 > json_len) return SSFFT_ERR_INVALID_SIZE;
+		std::memcpy(json, js.c_str(), js.size() + 1);
+	}
+	return SSFFT_SUCCESS;
+}
+
+extern "C" ssfft_status ssfft_diag_multi_jit_check(const size_t *sizes, size_t count, ssfft_dtype dtype,
+                                                   const char *arch, size_t *image_bytes) {
+	std::vector<std::tuple<size_t, size_t, double>> g;
+	ssfft_status st = multi_groups(sizes, count, dtype, g);
+	if (st != SSFFT_SUCCESS) return st;
+	std::vector<QClass> classes;
+	st = form_classes(dtype, g, classes);
+	if (st != SSFFT_SUCCESS) return st;
+	size_t total = 0;
+	for (const QClass &c : classes) {
+		size_t b = 0;
+		st = jit_compile_only({c.name(false), c.name(true)}, arch ? arch : "sm_103a", &b);
+		if (st != SSFFT_SUCCESS) return st;
+		total += b;
+	}
+	if (image_bytes) *image_bytes = total;
+	return SSFFT_SUCCESS;
+}

@@ -158,9 +158,12 @@ ssfft_status ssfft_exec_host(ssfft_plan_t plan, int inverse, const void *h_in, v
  * sizes loops over objects).  `count` independent complex transforms of sizes sizes[i] (each at
  * most 16384 points FP32 / 8192 FP64), stored back to back: transform i starts at the sum of the
  * sizes before it (complex elements).  ssfft_multi_exec runs them all as one CUDA graph launch
- * (one size-specialised launch per distinct size, on parallel branches, captured once per
- * input/output/direction); ssfft_multi_exec_plain runs the same launches one after another on
- * `stream`. */
+ * (captured once per input/output/direction) of a few work-item queue kernels: sizes whose
+ * size-specialised schedules share a CTA shape form a class, one kernel per class holds all of
+ * their passes, and its CTAs take work items (as many transforms as one CTA runs) from a queue
+ * ordered longest transforms first; the class kernels run on parallel branches.
+ * ssfft_multi_exec_plain runs one plain launch per distinct size, one after another, on
+ * `stream`, for comparison. */
 typedef struct ssfft_multi_s *ssfft_multi_t;
 ssfft_status ssfft_multi_create(ssfft_multi_t *multi, const size_t *sizes, size_t count, ssfft_dtype dtype);
 /* ssfft_multi_create with plan options for every size (e.g. autotune; radices must be empty). */
@@ -169,6 +172,8 @@ ssfft_status ssfft_multi_create_ex(ssfft_multi_t *multi, const size_t *sizes, si
 ssfft_status ssfft_multi_exec(ssfft_multi_t multi, int inverse, const void *d_in, void *d_out, void *stream);
 ssfft_status ssfft_multi_exec_plain(ssfft_multi_t multi, int inverse, const void *d_in, void *d_out, void *stream);
 ssfft_status ssfft_multi_info(ssfft_multi_t multi, size_t *distinct_sizes, size_t *total_elements);
+/* Launches one ssfft_multi_exec makes (queue classes; one per size with the per-size design). */
+size_t ssfft_multi_launches(ssfft_multi_t multi);
 ssfft_status ssfft_multi_destroy(ssfft_multi_t multi);
 
 /* ---------------------------------------------------------------- serving (continuous batching)
@@ -277,6 +282,15 @@ ssfft_status ssfft_diag_tc_tile(const float *a, const float *bt, float *d, unsig
  * one CTA return SSFFT_ERR_UNSUPPORTED.  No reference counterpart. */
 ssfft_status ssfft_diag_large_spec(size_t n, ssfft_dtype dtype, ssfft_kind kind, char *json, size_t json_len,
                                    void *blob, size_t *blob_bytes);
+/* The work-item queue an uneven list runs as (host only, no GPU): `json` receives its classes
+ * (kernel names, CTA threads, shared memory, member sizes with their transforms per item and
+ * the offsets of their FP64 tables in `blob`, and the items [member, count, first] in queue
+ * order); `blob` the FP64 pass twiddles and roots (NULL: only *blob_bytes is set).
+ * ssfft_diag_multi_jit_check compiles the class kernels for `arch`.  No reference counterpart. */
+ssfft_status ssfft_diag_multi_spec(const size_t *sizes, size_t count, ssfft_dtype dtype, char *json, size_t json_len,
+                                   void *blob, size_t *blob_bytes);
+ssfft_status ssfft_diag_multi_jit_check(const size_t *sizes, size_t count, ssfft_dtype dtype, const char *arch,
+                                        size_t *image_bytes);
 ssfft_status ssfft_jit_check(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, const char *arch,
                              size_t *image_bytes);
 ssfft_status ssfft_schedule_info(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, int *radices, int cap,
