@@ -726,9 +726,12 @@ def uneven_block(args, steps: int | None = None) -> dict:
             worst = max(worst, float(np.linalg.norm(got - refs[i]) / np.linalg.norm(refs[i])))
         return {"graph": {"ms": tg * 1e3, "GFLOP_s": flops / tg / 1e9, "alg_GB_s": alg / tg / 1e9,
                           "frac_of_hbm": alg / tg / 1e9 / peak},
-                "plain_per_size": {"ms": tp * 1e3, "GFLOP_s": flops / tp / 1e9, "alg_GB_s": alg / tp / 1e9},
+                "plain_per_size": {"ms": tp * 1e3, "GFLOP_s": flops / tp / 1e9, "alg_GB_s": alg / tp / 1e9,
+                                   "frac_of_hbm": alg / tp / 1e9 / peak},
                 "speedup_vs_plain": tp / tg, "plan_build_s": build_s, "worst_relL2_sampled": worst,
-                "distinct_sizes": m.info()["distinct_sizes"]}
+                "distinct_sizes": m.info()["distinct_sizes"], "launches_per_submission": m.info()["launches"],
+                "design": ("work-item queue kernels (one per class of CTA shapes) in one CUDA graph"
+                           if precision == "fp32" else "per-size tensor-core kernels in one CUDA graph")}
 
     t_all = time.perf_counter()
     fp32 = variant("fp32")
