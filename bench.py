@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the host-buffer leg (default: steps/10)")
     ap.add_argument("--workload", default="realfft",
-                    choices=["realfft", "fp64", "large", "serve", "uneven", "precision", "sizes"],
+                    choices=["realfft", "fp64", "large", "serve", "uneven", "precision", "sizes", "dropin"],
                     help="realfft: the batched RealFFT<float> line (default); fp64: FFT<double> N=1024 x256; "
                          "large: single FP32 transforms of 2^24, 3^15, 2^12 3^4 5^2; serve: request serving sweep; "
                          "sizes: per-size batched FP32 kernel sweep (--sizes, --kinds, --sweep-mb, --plan-options)")
@@ -749,6 +749,101 @@ def uneven_block(args, steps: int | None = None) -> dict:
     return out
 
 
+# Per-call timing of the drop-in header: the reference's usage pattern (one object, host
+# containers, one transform per call).  Compiled by run_dropin against include/signalsmith-fft.h.
+DROPIN_CPP = r"""
+#include <chrono>
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include "signalsmith-fft.h"
+
+template <class F>
+static void timed(const char *name, int calls, F &&call) {
+	for (int i = 0; i < 50; ++i) call();
+	std::vector<double> us(calls);
+	for (int i = 0; i < calls; ++i) {
+		auto t0 = std::chrono::steady_clock::now();
+		call();
+		us[i] = std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - t0).count();
+	}
+	double sum = 0;
+	for (double u : us) sum += u;
+	std::sort(us.begin(), us.end());
+	std::printf("{\"case\": \"%s\", \"calls\": %d, \"mean_us\": %.3f, \"p50_us\": %.3f, \"p99_us\": %.3f}\n", name,
+	            calls, sum / calls, us[calls / 2], us[(size_t)(calls * 0.99)]);
+}
+
+int main(int argc, char **argv) {
+	const int calls = argc > 1 ? std::atoi(argv[1]) : 2000;
+	std::mt19937_64 rng(7);
+	std::uniform_real_distribution<double> u(-1, 1);
+	{
+		signalsmith::FFT<double> fft(1024);
+		std::vector<std::complex<double>> in(1024), out(1024);
+		for (auto &v : in) v = {u(rng), u(rng)};
+		timed("FFT<double>(1024).fft(vector, vector)", calls, [&] { fft.fft(in, out); });
+	}
+	{
+		signalsmith::RealFFT<float> real(3840);
+		std::vector<float> in(3840);
+		std::vector<std::complex<float>> out(1920);
+		for (auto &v : in) v = (float)u(rng);
+		timed("RealFFT<float>(3840).fft(vector, vector)", calls, [&] { real.fft(in, out); });
+	}
+	{
+		signalsmith::RealFFT<float> real(65536);
+		std::vector<float> in(65536);
+		std::vector<std::complex<float>> out(32768);
+		for (auto &v : in) v = (float)u(rng);
+		timed("RealFFT<float>(65536).fft(vector, vector)", calls / 4, [&] { real.fft(in, out); });
+	}
+	return 0;
+}
+"""
+
+
+def run_dropin(args):
+    """Per-call latency of the drop-in header (host containers in and out, one transform per call,
+    synchronous, as the reference is used: benchmark/main.cpp of the reference times the same
+    pattern) against the reference algorithm per call on one host core (the oracle's C
+    restatement, one plan reused across calls)."""
+    import shutil
+    import tempfile
+    import oracle
+    cuda = os.path.dirname(os.path.dirname(os.path.realpath(shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")))
+    lib_dir = os.path.join(ROOT, "fft_gb300")
+    d = tempfile.mkdtemp(prefix="ssfft_dropin_")
+    src, exe = os.path.join(d, "dropin_bench.cpp"), os.path.join(d, "dropin_bench")
+    with open(src, "w") as f:
+        f.write(DROPIN_CPP)
+    subprocess.run(["g++", "-std=c++14", "-O2", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(cuda, "include"),
+                    src, "-L", lib_dir, "-lssfft", "-L", os.path.join(cuda, "lib64"), "-lcudart",
+                    f"-Wl,-rpath,{lib_dir}", f"-Wl,-rpath,{os.path.join(cuda, 'lib64')}", "-o", exe], check=True)
+    r = subprocess.run([exe, str(max(200, args.steps * 10))], capture_output=True, text=True, check=True)
+    gpu = [json.loads(line) for line in r.stdout.splitlines() if line.startswith("{")]
+    rng = np.random.default_rng(7)
+    cpu = []
+    for name, n, real, dt, reps in (("FFT<double>(1024)", 1024, False, np.complex128, 4000),
+                                    ("RealFFT<float>(3840)", 3840, True, np.float32, 2000),
+                                    ("RealFFT<float>(65536)", 65536, True, np.float32, 100)):
+        if real:
+            x = rng.standard_normal((1, n)).astype(dt)
+        else:
+            x = (rng.uniform(-1, 1, (1, n)) + 1j * rng.uniform(-1, 1, (1, n))).astype(dt)
+        oracle.batch(x, n, real=real, inverse=False, threads=1, repeats=10, kind=CPU_KIND)
+        t0 = time.perf_counter()
+        oracle.batch(x, n, real=real, inverse=False, threads=1, repeats=reps, kind=CPU_KIND)
+        cpu.append({"case": name, "us_per_call": (time.perf_counter() - t0) / reps * 1e6})
+    print(json.dumps({"workload": "drop-in header per call (host containers, synchronous)", "gpu": gpu,
+                      "cpu_reference_algorithm_1_core": cpu, "cpu_build": cpu_build_note()}), flush=True)
+
+
 def run_precision(args):
     """Complex FP32 N=1024, 32768 transforms: the FP32-FMA kernel against the split-BF16
     tensor-core first pass, forward + inverse, with relL2 against the FP64 oracle."""
@@ -832,7 +927,7 @@ def main():
         fb.build()
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         {"fp64": run_fp64, "large": run_large, "serve": run_serve, "uneven": run_uneven,
-         "precision": run_precision, "sizes": run_sizes}[args.workload](args)
+         "precision": run_precision, "sizes": run_sizes, "dropin": run_dropin}[args.workload](args)
     else:
         run_gpu(args, rank, world if "WORLD_SIZE" in os.environ else 1)
 

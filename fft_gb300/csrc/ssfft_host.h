@@ -89,6 +89,9 @@ struct HostStage {
 	void *d_out[kStreams] = {};
 	size_t chunk = 0;   // transforms per chunk
 	int streams = kStreams;
+	// small calls: pinned host bounce buffers (in and out, bounce_bytes each), allocated on first use
+	void *bounce_in = nullptr, *bounce_out = nullptr;
+	size_t bounce_bytes = 0;
 };
 
 struct Plan {

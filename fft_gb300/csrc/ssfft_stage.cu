@@ -28,6 +28,8 @@ void plan_release(Plan *p) {
 			if (st->d_out[i]) cudaFree(st->d_out[i]);
 			if (st->stream[i]) cudaStreamDestroy(st->stream[i]);
 		}
+		if (st->bounce_in) cudaFreeHost(st->bounce_in);
+		if (st->bounce_out) cudaFreeHost(st->bounce_out);
 		delete st;
 		p->stage = nullptr;
 	}
@@ -94,6 +96,60 @@ static void *mapped_host(const void *p, size_t bytes) {
 	return a.devicePointer;
 }
 
+// Whether [p, p + bytes) is page-locked host memory the runtime knows (a DMA from it needs no
+// staging by the driver).
+static bool pinned_host(const void *p, size_t bytes) {
+	if (!bytes) return false;
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+		cudaGetLastError();
+		return false;
+	}
+	if (a.type != cudaMemoryTypeHost) return false;
+	cudaPointerAttributes b;
+	const unsigned char *last = static_cast<const unsigned char *>(p) + bytes - 1;
+	if (cudaPointerGetAttributes(&b, last) != cudaSuccess) {
+		cudaGetLastError();
+		return false;
+	}
+	return b.type == cudaMemoryTypeHost;
+}
+
+// Small calls (the whole batch in one chunk, at most kBounceMax bytes each way; e.g. one
+// transform per call, the reference's usage pattern): one stream, and pageable buffers go through
+// the plan's pinned bounce buffers (a host memcpy, then true asynchronous DMA) instead of the
+// driver's synchronous staging of pageable copies.  Debug switch small_host=0 turns it off.
+static constexpr size_t kBounceMax = size_t(4) << 20;
+
+static ssfft_status exec_host_small(Plan *p, int inverse, const void *h_in, void *h_out, size_t in_b, size_t out_b) {
+	HostStage *sg = p->stage;
+	if (!sg->bounce_in) {
+		cudaError_t e = cudaHostAlloc(&sg->bounce_in, kBounceMax, cudaHostAllocDefault);
+		if (e == cudaSuccess) e = cudaHostAlloc(&sg->bounce_out, kBounceMax, cudaHostAllocDefault);
+		if (e != cudaSuccess) return cuda_fail(e, "exec_host bounce buffers");
+		sg->bounce_bytes = kBounceMax;
+	}
+	const bool pin_in = pinned_host(h_in, in_b), pin_out = pinned_host(h_out, out_b);
+	const void *src = h_in;
+	if (!pin_in) {
+		std::memcpy(sg->bounce_in, h_in, in_b);
+		src = sg->bounce_in;
+	}
+	void *dst = pin_out ? h_out : sg->bounce_out;
+	cudaStream_t s = sg->stream[0];
+	cudaError_t e = cudaMemcpyAsync(sg->d_in[0], src, in_b, cudaMemcpyHostToDevice, s);
+	if (e != cudaSuccess) return cuda_fail(e, "exec_host H2D");
+	ssfft_status st = p->large ? launch_large(p, inverse, sg->d_in[0], sg->d_out[0], p->batch, s)
+	                           : launch_batch(p, inverse, sg->d_in[0], sg->d_out[0], p->batch, s);
+	if (st != SSFFT_SUCCESS) return st;
+	e = cudaMemcpyAsync(dst, sg->d_out[0], out_b, cudaMemcpyDeviceToHost, s);
+	if (e != cudaSuccess) return cuda_fail(e, "exec_host D2H");
+	e = cudaStreamSynchronize(s);
+	if (e != cudaSuccess) return cuda_fail(e, "exec_host sync");
+	if (!pin_out) std::memcpy(h_out, sg->bounce_out, out_b);
+	return SSFFT_SUCCESS;
+}
+
 extern "C" ssfft_status ssfft_exec_host(ssfft_plan_t plan, int inverse, const void *h_in, void *h_out) {
 	Plan *p = reinterpret_cast<Plan *>(plan);
 	if (!p || !h_in || !h_out) return SSFFT_ERR_INVALID_VALUE;
@@ -121,6 +177,12 @@ extern "C" ssfft_status ssfft_exec_host(ssfft_plan_t plan, int inverse, const vo
 	if (st != SSFFT_SUCCESS) return st;
 	HostStage *sg = p->stage;
 	const size_t per_in = plan_in_bytes(p, inverse, 1), per_out = plan_out_bytes(p, inverse, 1);
+	if (p->batch <= sg->chunk && p->batch * std::max(per_in, per_out) <= kBounceMax &&
+	    debug_knob("small_host", 1) != 0) {
+		st = exec_host_small(p, inverse, h_in, h_out, p->batch * per_in, p->batch * per_out);
+		if (prev >= 0 && prev != p->device) cudaSetDevice(prev);
+		return st;
+	}
 	const unsigned char *src = static_cast<const unsigned char *>(h_in);
 	unsigned char *dst = static_cast<unsigned char *>(h_out);
 	size_t done = 0;

@@ -208,6 +208,38 @@ def test_config_realfft_f32_frames(F, n, kind):
     assert rel_l2(back.cpu().numpy(), n * x32.astype(np.float64)) <= 2e-6
 
 
+@pytest.mark.parametrize("n", [480, 960, 1920, 3840])
+def test_config_realfft_f32_full_16384_frames(F, n):
+    """The headline configuration at its full size: 16384 frames of N(0,1) noise + 3 sinusoids
+    (the bench's own generator), forward and inverse.  Every 64th frame (256 frames) against the
+    FP64 oracle at the FP32 bar; every frame through size-independent properties: the round trip
+    ifft(fft(x)) = N x and Parseval's identity for the packed spectrum."""
+    import os
+    import bench
+    frames = 16384
+    x32 = bench.frames_for(n, frames, 1000 + n)
+    p = F.Plan(n, "f32", "real", frames)
+    xi = dev(x32)
+    spec = torch.empty((frames, n // 2), dtype=torch.complex64, device="cuda")
+    back = torch.empty_like(xi)
+    p.exec(False, xi.data_ptr(), spec.data_ptr(), 0)
+    p.exec(True, spec.data_ptr(), back.data_ptr(), 0)
+    torch.cuda.synchronize()
+    s = spec.cpu().numpy()
+    b = back.cpu().numpy()
+    pick = np.arange(0, frames, 64)
+    threads = os.cpu_count() or 1
+    ref = oracle.batch(x32[pick].astype(np.float64), n, real=True, inverse=False, threads=threads)
+    assert rel_l2(s[pick], ref) <= F32_TOL, rel_l2(s[pick], ref)
+    refb = oracle.batch(s[pick].astype(np.complex128), n, real=True, inverse=True, threads=threads)
+    assert rel_l2(b[pick], refb) <= F32_TOL, rel_l2(b[pick], refb)
+    assert rel_l2(b, n * x32.astype(np.float64)) <= 2e-6
+    s64 = s.astype(np.complex128)
+    energy_bins = (s64[:, 0].real ** 2 + s64[:, 0].imag ** 2 + 2 * np.sum(np.abs(s64[:, 1:]) ** 2, axis=1)) / n
+    energy_time = np.sum(x32.astype(np.float64) ** 2, axis=1)
+    assert np.max(np.abs(energy_bins - energy_time) / energy_time) <= 1e-5
+
+
 def test_partial_batch_and_host_path(F):
     rng = np.random.default_rng(9)
     n, b = 240, 37
