@@ -604,7 +604,7 @@ class ServerStats(ctypes.Structure):
                 ("waves", ctypes.c_uint64), ("launches", ctypes.c_uint64), ("p50_latency_us", ctypes.c_double),
                 ("p99_latency_us", ctypes.c_double), ("mean_latency_us", ctypes.c_double),
                 ("max_latency_us", ctypes.c_double), ("span_seconds", ctypes.c_double), ("frames", ctypes.c_double),
-                ("flops", ctypes.c_double)]
+                ("flops", ctypes.c_double), ("in_place", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

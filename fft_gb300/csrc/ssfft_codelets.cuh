@@ -43,6 +43,8 @@ struct Args {
 	                          // [output column][input column] (FP32 values of FP64-built roots)
 	long long pf_dist;        // batch kernel: CTA b prefetches into L2 the input of CTA b + pf_dist
 	                          // (about one wave of resident CTAs ahead; 0 = off)
+	const long long *offs_out;  // batch kernel with offs: if set, transform g's output starts
+	                            // offs_out[g] scalars into out (else offs[g])
 };
 
 enum : int { kComplex = 0, kReal = 1, kRealHalfShift = 2 };
@@ -988,8 +990,12 @@ __global__ void __launch_bounds__(THREADS *PER_CTA, MINB) batch(const Args a) {
 	c.sm = reinterpret_cast<C *>(smem_raw) + g * SMEM_STRIDE;
 	long long oin = 0, oout = 0;
 	if (c.valid) {
-		if (a.offs) oin = oout = a.offs[gi];
-		else oin = gi * a.in_dist, oout = gi * a.out_dist;
+		if (a.offs) {
+			oin = a.offs[gi];
+			oout = a.offs_out ? a.offs_out[gi] : oin;
+		} else {
+			oin = gi * a.in_dist, oout = gi * a.out_dist;
+		}
 	}
 	c.gin = reinterpret_cast<const T *>(a.in) + oin;
 	c.gout = reinterpret_cast<T *>(a.out) + oout;
@@ -1532,7 +1538,8 @@ __global__ void __launch_bounds__(THREADS *PER_CTA, MINB) batch_tc(const Args a)
 			tc_ld32(taddr + ((unsigned)(warp * 32) << 16), v);
 			if (live) {
 				if constexpr (LAST) {
-					C *dst = reinterpret_cast<C *>(a.out) + (a.offs ? a.offs[gi] : gi * a.out_dist) / 2;
+					C *dst = reinterpret_cast<C *>(a.out) +
+					         (a.offs ? (a.offs_out ? a.offs_out[gi] : a.offs[gi]) : gi * a.out_dist) / 2;
 #pragma unroll
 					for (int k = 0; k < R0; ++k) __stcs(dst + j * R0 + k, make_float2(v[k], INV ? -v[16 + k] : v[16 + k]));
 				} else {
@@ -1558,7 +1565,7 @@ __global__ void __launch_bounds__(THREADS *PER_CTA, MINB) batch_tc(const Args a)
 		c.valid = gi < a.batch;
 		c.sm = reinterpret_cast<C *>(smem_raw) + g * SMEM_STRIDE;
 		long long oout = 0;
-		if (c.valid) oout = a.offs ? a.offs[gi] : gi * a.out_dist;
+		if (c.valid) oout = a.offs ? (a.offs_out ? a.offs_out[gi] : a.offs[gi]) : gi * a.out_dist;
 		c.gin = nullptr;
 		c.gout = reinterpret_cast<T *>(a.out) + oout;
 		c.rot = nullptr;
@@ -2040,7 +2047,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, MINB) pair(
 	c.valid = g < a.batch;
 	long long oin = 0, oout = 0;
 	if (c.valid) {
-		if (a.offs) oin = oout = a.offs[g];
+		if (a.offs) oin = a.offs[g], oout = a.offs_out ? a.offs_out[g] : oin;
 		else oin = g * a.in_dist, oout = g * a.out_dist;
 	}
 	c.gin = reinterpret_cast<const C *>(reinterpret_cast<const T *>(a.in) + oin) + c.rank * (N2 / 2);
@@ -2082,6 +2089,10 @@ struct BlueArgs {
 	const void *chirp;  // w_k, k < N
 	const void *bhat;   // M-point spectrum of b (b_m = conj(w_|m|), |m| < N, zero elsewhere)
 	long long n, m, batch, dist;
+	// half-shift RealFFT (ModifiedRealFFT): the packed input is multiplied by rot_k before the
+	// transform (forward, rot_in), or the output by conj(rot_k) after it (inverse, rot_out)
+	const void *rot_in;
+	const void *rot_out;
 };
 
 template <typename T, bool CONJ>
@@ -2093,6 +2104,7 @@ __global__ void __launch_bounds__(256) blue_pre(const BlueArgs a) {
 	if (k < a.n) {
 		C x = __ldcs(reinterpret_cast<const C *>(a.in) + b * a.dist + k);
 		if (CONJ) x = conj(x);
+		if (a.rot_in) x = mul(x, __ldg(reinterpret_cast<const C *>(a.rot_in) + k));
 		v = mul(x, __ldg(reinterpret_cast<const C *>(a.chirp) + k));
 	}
 	reinterpret_cast<C *>(a.work)[b * a.m + k] = v;
@@ -2114,7 +2126,35 @@ __global__ void __launch_bounds__(256) blue_post(const BlueArgs a) {
 	if (k >= a.n || b >= a.batch) return;
 	C y = mul(reinterpret_cast<const C *>(a.work)[b * a.m + k], __ldg(reinterpret_cast<const C *>(a.chirp) + k));
 	y = scale(y, T(1) / T(a.m));
-	__stcs(reinterpret_cast<C *>(a.out) + b * a.dist + k, CONJ ? conj(y) : y);
+	if (CONJ) y = conj(y);
+	if (a.rot_out) y = mulc(y, __ldg(reinterpret_cast<const C *>(a.rot_out) + k));
+	__stcs(reinterpret_cast<C *>(a.out) + b * a.dist + k, y);
+}
+
+// Odd real lengths beyond one CTA: the transform runs on h = floor(n/2) complex points
+// z_i = {x_2i, x_2i+1} (the last real is neither read nor written, as the reference's RealFFT
+// reads and writes pairs only, signalsmith-fft.h:446-502).  Rows of n reals do not keep the
+// pairs aligned, so they are packed into (unpacked from) rows of h complex around the passes.
+struct PackArgs {
+	const void *src;
+	void *dst;
+	long long batch, n, h;
+};
+
+template <typename T, bool UNPACK>
+__global__ void __launch_bounds__(256) real_pack(const PackArgs a) {
+	using C = typename Cx<T>::C;
+	const long long i = (long long)blockIdx.x * 256 + threadIdx.x, b = blockIdx.y;
+	if (i >= a.h || b >= a.batch) return;
+	if constexpr (!UNPACK) {
+		const T *x = reinterpret_cast<const T *>(a.src) + b * a.n;
+		reinterpret_cast<C *>(a.dst)[b * a.h + i] = mkc(__ldcs(x + 2 * i), __ldcs(x + 2 * i + 1));
+	} else {
+		const C v = __ldcs(reinterpret_cast<const C *>(a.src) + b * a.h + i);
+		T *x = reinterpret_cast<T *>(a.dst) + b * a.n;
+		__stcs(x + 2 * i, v.x);
+		__stcs(x + 2 * i + 1, v.y);
+	}
 }
 
 // Real split / merge over global memory for real transforms longer than one CTA holds

@@ -173,6 +173,8 @@ ssfft_status plan_build_large(Plan *p);
 bool plan_single_cta(size_t n, ssfft_dtype dtype, ssfft_kind kind);
 void plan_release(Plan *p);
 ssfft_status launch_batch(const Plan *p, int inverse, const void *in, void *out, size_t batch, cudaStream_t s);
+ssfft_status launch_batch_offs(const Plan *p, int inverse, const void *in, void *out, size_t batch,
+                               const long long *d_offs, cudaStream_t s, const long long *d_offs_out = nullptr);
 ssfft_status launch_large(Plan *p, int inverse, const void *in, void *out, size_t batch, cudaStream_t s);
 void large_release(LargePlan *lp);
 ssfft_status large_jit_check(size_t n, ssfft_dtype dtype, ssfft_kind kind, const char *arch, size_t *image_bytes);

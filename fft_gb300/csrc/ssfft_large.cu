@@ -60,8 +60,12 @@ struct LargePlan {
 	// Bluestein (M > 0): inner M-point plan, chirp w_k and spectrum of conj(w) in d_tables
 	long long M = 0;
 	ssfft_plan_t inner = nullptr;
-	size_t off_chirp = 0, off_bhat = 0;
+	size_t off_chirp = 0, off_bhat = 0, off_brot = 0;
 	CUfunction blue_pre[2] = {}, blue_mul = nullptr, blue_post[2] = {};
+	// odd real lengths: rows of n reals packed into (unpacked from) rows of N complex in d_pack
+	bool odd = false;
+	CUfunction pack = nullptr, unpack = nullptr;
+	void *d_pack = nullptr;
 };
 
 // Smallest 2^a 3^b 5^c >= v.
@@ -98,6 +102,11 @@ std::string LargePass::name(bool inverse, bool first, bool last, int rot) const 
 static std::string split_name(ssfft_dtype dt, long long h, bool mod, bool inverse) {
 	return std::string("ssfft_cl::real_split<") + (dt == SSFFT_F32 ? "float" : "double") + ", " + std::to_string(h) +
 	       "LL, " + (mod ? "true" : "false") + ", " + (inverse ? "true" : "false") + ">";
+}
+
+static std::string pack_name(ssfft_dtype dt, bool unpack) {
+	return std::string("ssfft_cl::real_pack<") + (dt == SSFFT_F32 ? "float" : "double") + ", " +
+	       (unpack ? "true" : "false") + ">";
 }
 
 // Split N into 2 (N <= kMaxFactor^2) or 3 balanced factors, each <= kMaxFactor.
@@ -140,6 +149,7 @@ static void put(std::vector<unsigned char> &blob, size_t off, const std::vector<
 void large_release(LargePlan *lp) {
 	if (!lp) return;
 	if (lp->inner) ssfft_plan_destroy(lp->inner);
+	if (lp->d_pack) cudaFree(lp->d_pack);
 	if (lp->d_scratch) cudaFree(lp->d_scratch);
 	if (lp->d_tables) cudaFree(lp->d_tables);
 	delete lp;
@@ -153,16 +163,16 @@ struct LargeTables {
 static ssfft_status large_schedule(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t smem_limit, LargePlan *lp,
                                    LargeTables &t) {
 	const bool real = kind != SSFFT_COMPLEX;
-	if (real && (n & 1)) return SSFFT_ERR_UNSUPPORTED;  // long odd real lengths
 	const long long N = (long long)(real ? n / 2 : n);
+	lp->odd = real && (n & 1);  // packed around the passes (the pairs of odd rows are misaligned)
 	std::vector<long long> F;
 	if (!large_factors(N, F)) {
-		// Bluestein: complex and RealFFT kinds (the half-shift rotation lives in the passes)
-		if (kind == SSFFT_REAL_HALFSHIFT || N > (1ll << 29)) return SSFFT_ERR_UNSUPPORTED;
+		// Bluestein (every kind; the half-shift rotations ride on its chirp kernels)
+		if (N > (1ll << 29)) return SSFFT_ERR_UNSUPPORTED;
 		lp->N = N;
 		lp->F.clear();
 		lp->real = real;
-		lp->modified = false;
+		lp->modified = kind == SSFFT_REAL_HALFSHIFT;
 		lp->pass.clear();
 		lp->M = smooth_at_least(2 * N - 1);
 		return SSFFT_SUCCESS;
@@ -254,8 +264,12 @@ static std::vector<std::string> large_kernel_names(const LargePlan *lp, ssfft_dt
 		names = {blue_name("blue_pre", dtype, 0), blue_name("blue_pre", dtype, 1), blue_name("blue_mul", dtype, -1),
 		         blue_name("blue_post", dtype, 0), blue_name("blue_post", dtype, 1)};
 		if (lp->real) {
-			names.push_back(split_name(dtype, lp->N, false, false));
-			names.push_back(split_name(dtype, lp->N, false, true));
+			names.push_back(split_name(dtype, lp->N, lp->modified, false));
+			names.push_back(split_name(dtype, lp->N, lp->modified, true));
+		}
+		if (lp->odd) {
+			names.push_back(pack_name(dtype, false));
+			names.push_back(pack_name(dtype, true));
 		}
 		return names;
 	}
@@ -271,6 +285,10 @@ static std::vector<std::string> large_kernel_names(const LargePlan *lp, ssfft_dt
 	if (lp->real) {
 		names.push_back(split_name(dtype, lp->N, lp->modified, false));
 		names.push_back(split_name(dtype, lp->N, lp->modified, true));
+	}
+	if (lp->odd) {
+		names.push_back(pack_name(dtype, false));
+		names.push_back(pack_name(dtype, true));
 	}
 	return names;
 }
@@ -316,23 +334,36 @@ static size_t blue_tables(LargePlan *lp, size_t n, ssfft_dtype dtype, std::vecto
 			b[2 * (M - k) + 1] = -im;
 		}
 	}
+	std::vector<double> rot;
 	if (lp->real)
 		for (long long i = 0; i <= N / 2; ++i) {
 			double re, im;
-			unit_root(i, n, &re, &im);
+			// -i e^{-2 pi i (k or k + 1/2) / n} (signalsmith-fft.h:420-425)
+			if (lp->modified) unit_root(2 * (unsigned long long)i + 1, 2 * (unsigned long long)n, &re, &im);
+			else unit_root((unsigned long long)i, n, &re, &im);
 			rtw.push_back(im);
 			rtw.push_back(-re);
 		}
+	if (lp->modified)
+		for (long long i = 0; i < N; ++i) {  // e^{-2 pi i k / n} (:426-432)
+			double re, im;
+			unit_root((unsigned long long)i, n, &re, &im);
+			rot.push_back(re);
+			rot.push_back(im);
+		}
 	lp->off_rtw = 0;
-	lp->off_chirp = align_up(rtw.size() * sb, 256);
+	lp->off_brot = align_up(rtw.size() * sb, 256);
+	lp->off_chirp = align_up(lp->off_brot + rot.size() * sb, 256);
 	lp->off_bhat = align_up(lp->off_chirp + chirp.size() * sb, 256);
 	const size_t total = align_up(lp->off_bhat + (size_t)M * eb, 256);
 	blob.assign(lp->off_bhat, 0);
 	if (sb == 4) {
 		put<float>(blob, lp->off_rtw, rtw);
+		put<float>(blob, lp->off_brot, rot);
 		put<float>(blob, lp->off_chirp, chirp);
 	} else {
 		put<double>(blob, lp->off_rtw, rtw);
+		put<double>(blob, lp->off_brot, rot);
 		put<double>(blob, lp->off_chirp, chirp);
 	}
 	bb.assign((size_t)M * eb, 0);
@@ -379,14 +410,23 @@ static ssfft_status plan_build_bluestein(Plan *p, LargePlan *lp) {
 		lp->split_fwd = fns[5];
 		lp->split_inv = fns[6];
 	}
-	p->launches_per_exec = 3 + 2 * reinterpret_cast<const Plan *>(lp->inner)->launches_per_exec + (lp->real ? 1 : 0);
+	if (lp->odd) {
+		lp->pack = fns[7];
+		lp->unpack = fns[8];
+		e = cudaMalloc(&lp->d_pack, (size_t)lp->N * eb * lp->scratch_batch);
+		if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(odd-length pack buffer)");
+		p->scratch_bytes += (size_t)lp->N * eb * lp->scratch_batch;
+	}
+	p->launches_per_exec = 3 + 2 * reinterpret_cast<const Plan *>(lp->inner)->launches_per_exec + (lp->real ? 1 : 0) +
+	                       (lp->odd ? 1 : 0);
 	return SSFFT_SUCCESS;
 }
 
 // The complex N-point transform of nb transforms (dist N) through Bluestein, src -> dst; cin /
 // cout conjugate the input / output.
 static ssfft_status launch_bluestein(LargePlan *lp, ssfft_dtype dtype, const void *src, void *dst, long long nb,
-                                     bool cin, bool cout, cudaStream_t s) {
+                                     bool cin, bool cout, cudaStream_t s, const void *rot_in = nullptr,
+                                     const void *rot_out = nullptr) {
 	const unsigned char *tab = static_cast<const unsigned char *>(lp->d_tables);
 	ssfft_cl::BlueArgs a;
 	a.in = src;
@@ -398,6 +438,8 @@ static ssfft_status launch_bluestein(LargePlan *lp, ssfft_dtype dtype, const voi
 	a.m = lp->M;
 	a.batch = nb;
 	a.dist = lp->N;
+	a.rot_in = rot_in;
+	a.rot_out = rot_out;
 	const unsigned gm = (unsigned)((lp->M + 255) / 256), gn = (unsigned)((lp->N + 255) / 256);
 	ssfft_status st = jit_launch_grid(lp->blue_pre[cin ? 1 : 0], gm, (unsigned)nb, 256, 0, s, &a);
 	if (st == SSFFT_SUCCESS) st = ssfft_exec_batch(lp->inner, 0, lp->d_scratch, lp->d_scratch, (size_t)nb, s);
@@ -520,25 +562,53 @@ ssfft_status plan_build_large(Plan *p) {
 		lp->split_fwd = fns[2 * P];
 		lp->split_inv = fns[2 * P + 1];
 	}
-	p->launches_per_exec = P + (real ? 1 : 0);
+	if (lp->odd) {
+		lp->pack = fns[2 * P + 2];
+		lp->unpack = fns[2 * P + 3];
+		e = cudaMalloc(&lp->d_pack, per * lp->scratch_batch);
+		if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(odd-length pack buffer)");
+		p->scratch_bytes += per * lp->scratch_batch;
+	}
+	p->launches_per_exec = P + (real ? 1 : 0) + (lp->odd ? 1 : 0);
 	return SSFFT_SUCCESS;
 }
 
 ssfft_status launch_large(Plan *p, int inverse, const void *in, void *out, size_t batch, cudaStream_t s) {
 	LargePlan *lp = p->large;
-	const size_t eb = p->dtype == SSFFT_F32 ? 8 : 16;
+	const size_t eb = p->dtype == SSFFT_F32 ? 8 : 16, sb = eb / 2;
 	const unsigned char *tab = static_cast<const unsigned char *>(lp->d_tables);
 	const long long N = lp->N;
 	const int P = (int)lp->pass.size();
+	long long in_dist, out_dist;  // scalars between consecutive transforms of the caller's buffers
+	plan_dists(p, inverse, in_dist, out_dist);
+	// odd real rows: the pass input (forward) or output (inverse) is the packed buffer
+	auto pack_launch = [&](CUfunction f, const void *src, void *dst, long long nb) {
+		ssfft_cl::PackArgs a;
+		a.src = src;
+		a.dst = dst;
+		a.batch = nb;
+		a.n = (long long)p->n;
+		a.h = N;
+		return jit_launch_grid(f, (unsigned)((N + 255) / 256), (unsigned)nb, 256, 0, s, &a);
+	};
 	for (size_t b0 = 0; b0 < batch; b0 += lp->scratch_batch) {
 		const long long nb = (long long)std::min(lp->scratch_batch, batch - b0);
-		const unsigned char *src = static_cast<const unsigned char *>(in) + b0 * N * eb;
-		unsigned char *dst = static_cast<unsigned char *>(out) + b0 * N * eb;
+		const unsigned char *src = static_cast<const unsigned char *>(in) + b0 * (size_t)in_dist * sb;
+		unsigned char *dst = static_cast<unsigned char *>(out) + b0 * (size_t)out_dist * sb;
 		const void *first_in = src;
+		// where the complex result of the passes goes: the caller's output, or (odd real
+		// inverse) the packed buffer that is unpacked into it at the end
+		void *pass_out = lp->odd && inverse ? lp->d_pack : static_cast<void *>(dst);
+		if (lp->odd && !inverse) {
+			// rows of n reals -> rows of N complex, into the caller's output (N complex a row)
+			ssfft_status st = pack_launch(lp->pack, src, dst, nb);
+			if (st != SSFFT_SUCCESS) return st;
+			first_in = dst;
+		}
 		if (lp->real && inverse) {
-			// pre-twiddle the bins into the output buffer (the caller's input is left alone)
+			// pre-twiddle the bins into the pass buffer (the caller's input is left alone)
 			ssfft_cl::SplitArgs a;
-			a.buf = dst;
+			a.buf = pass_out;
 			a.src = src;
 			a.batch = nb;
 			a.dist = N;
@@ -546,19 +616,21 @@ ssfft_status launch_large(Plan *p, int inverse, const void *in, void *out, size_
 			const long long pairs = N / 2 + 1;
 			ssfft_status st = jit_launch_grid(lp->split_inv, (unsigned)((pairs + 255) / 256), (unsigned)nb, 256, 0, s, &a);
 			if (st != SSFFT_SUCCESS) return st;
-			first_in = dst;
+			first_in = pass_out;
 		}
 		if (lp->M) {
 			// complex engine: Bluestein (a RealFFT inverse arrives pre-twiddled and conjugated)
 			const bool cin = inverse && !lp->real, cout = inverse;
-			ssfft_status st = launch_bluestein(lp, p->dtype, first_in, dst, nb, cin, cout, s);
+			const void *rot_in = lp->modified && !inverse ? tab + lp->off_brot : nullptr;
+			const void *rot_out = lp->modified && inverse ? tab + lp->off_brot : nullptr;
+			ssfft_status st = launch_bluestein(lp, p->dtype, first_in, pass_out, nb, cin, cout, s, rot_in, rot_out);
 			if (st != SSFFT_SUCCESS) return st;
 		}
 		for (int i = 0; i < P; ++i) {
 			const LargePass &ps = lp->pass[i];
 			ssfft_cl::StridedArgs a;
 			a.in = i == 0 ? first_in : lp->d_scratch;
-			a.out = i == P - 1 ? (void *)dst : lp->d_scratch;
+			a.out = i == P - 1 ? pass_out : lp->d_scratch;
 			a.U0 = ps.U0;
 			a.U1 = ps.U1;
 			a.U2 = nb;
@@ -596,6 +668,11 @@ ssfft_status launch_large(Plan *p, int inverse, const void *in, void *out, size_
 			ssfft_status st = jit_launch_grid(lp->split_fwd, (unsigned)((pairs + 255) / 256), (unsigned)nb, 256, 0, s, &a);
 			if (st != SSFFT_SUCCESS) return st;
 		}
+		if (lp->odd && inverse) {
+			// rows of N complex -> rows of n reals (2N of them; the last real is not written)
+			ssfft_status st = pack_launch(lp->unpack, lp->d_pack, dst, nb);
+			if (st != SSFFT_SUCCESS) return st;
+		}
 	}
 	return SSFFT_SUCCESS;
 }
@@ -621,18 +698,20 @@ ssfft_status large_spec(size_t n, ssfft_dtype dtype, ssfft_kind kind, std::strin
 		blob.resize(total, 0);
 		std::memcpy(blob.data() + lp.off_bhat, bb.data(), bb.size());
 		json = "{\"N\": " + num(lp.N) + ", \"M\": " + num(lp.M) + ", \"real\": " + num(lp.real) +
-		       ", \"modified\": 0, \"off_rtw\": " + num((long long)lp.off_rtw) + ", \"off_chirp\": " +
+		       ", \"modified\": " + num(lp.modified) + ", \"odd\": " + num(lp.odd) + ", \"off_rtw\": " +
+		       num((long long)lp.off_rtw) + ", \"off_brot\": " + num((long long)lp.off_brot) + ", \"off_chirp\": " +
 		       num((long long)lp.off_chirp) + ", \"off_bhat\": " + num((long long)lp.off_bhat) + ", \"blue\": [";
 		for (int i = 0; i < 5; ++i) json += std::string(i ? ", " : "") + "\"" + names[i] + "\"";
 		json += "], \"passes\": []";
 		if (lp.real) json += ", \"split_fwd\": \"" + names[5] + "\", \"split_inv\": \"" + names[6] + "\"";
+		if (lp.odd) json += ", \"pack\": \"" + names[7] + "\", \"unpack\": \"" + names[8] + "\"";
 		json += "}";
 		return SSFFT_SUCCESS;
 	}
 	large_blob(&lp, t, n, dtype, blob);
 	json = "{\"N\": " + num(lp.N) + ", \"real\": " + num(lp.real) + ", \"modified\": " + num(lp.modified) +
-	       ", \"off_rtw\": " + num((long long)lp.off_rtw) + ", \"off_rot\": " + num((long long)lp.off_rot) +
-	       ", \"passes\": [";
+	       ", \"odd\": " + num(lp.odd) + ", \"off_rtw\": " + num((long long)lp.off_rtw) + ", \"off_rot\": " +
+	       num((long long)lp.off_rot) + ", \"passes\": [";
 	for (size_t i = 0; i < lp.pass.size(); ++i) {
 		const LargePass &ps = lp.pass[i];
 		json += std::string(i ? ", " : "") + "{\"fwd\": \"" + names[2 * i] + "\", \"inv\": \"" + names[2 * i + 1] +
@@ -647,6 +726,8 @@ ssfft_status large_spec(size_t n, ssfft_dtype dtype, ssfft_kind kind, std::strin
 	json += "]";
 	if (lp.real) json += ", \"split_fwd\": \"" + names[2 * lp.pass.size()] + "\", \"split_inv\": \"" +
 		                  names[2 * lp.pass.size() + 1] + "\"";
+	if (lp.odd) json += ", \"pack\": \"" + names[2 * lp.pass.size() + 2] + "\", \"unpack\": \"" +
+		                 names[2 * lp.pass.size() + 3] + "\"";
 	json += "}";
 	return SSFFT_SUCCESS;
 }

@@ -35,8 +35,6 @@
 
 namespace ssfft {
 
-ssfft_status launch_batch_offs(const Plan *p, int inverse, const void *in, void *out, size_t batch,
-                               const long long *d_offs, cudaStream_t s);
 ssfft_status plan_prepare_launch(const Plan *p);
 
 namespace {
@@ -182,7 +180,18 @@ struct MultiPlan {
 static bool queue_schedule(ssfft_dtype dtype, size_t n, size_t count, Schedule &s, int &cta) {
 	if (!make_schedule(dtype, (int)n, ssfft_cl::kComplex, false, count, s, 0, nullptr, 0)) return false;
 	if (s.staged || s.tc || s.pair) return false;
-	cta = (s.threads + kQueueBucket - 1) / kQueueBucket * kQueueBucket;
+	// the debug switch queue_bucket overrides the rounding (a multiple of 32; with 32 a class is
+	// the planner's own CTA shape rounded to whole warps)
+	const long long qb = debug_knob("queue_bucket", kQueueBucket);
+	const int bucket = qb >= 32 && qb <= 1024 && qb % 32 == 0 ? (int)qb : kQueueBucket;
+	if (bucket < kQueueBucket) {
+		cta = (s.threads * s.per_cta + bucket - 1) / bucket * bucket;
+		const size_t eb0 = dtype == SSFFT_F32 ? 8 : 16;
+		if ((size_t)s.per_cta > count) s.per_cta = (int)std::max<size_t>(1, count);
+		s.smem_bytes = (size_t)s.per_cta * (size_t)s.smem_stride * eb0;
+		return true;
+	}
+	cta = (s.threads + bucket - 1) / bucket * bucket;
 	const size_t eb = dtype == SSFFT_F32 ? 8 : 16;
 	const size_t per = (size_t)s.smem_stride * eb;
 	int g = std::max(1, cta / s.threads);

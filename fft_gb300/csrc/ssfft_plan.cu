@@ -982,7 +982,8 @@ ssfft_status plan_prepare_launch(const Plan *p) {
 }
 
 static ssfft_status launch_unstaged(const Plan *p, int inverse, const void *in, void *out, size_t batch,
-                                    cudaStream_t s, const long long *offs = nullptr) {
+                                    cudaStream_t s, const long long *offs = nullptr,
+                                    const long long *offs_out = nullptr) {
 	Schedule u, ui;
 	std::vector<CUfunction> fns;
 	ssfft_status rc = unstaged_kernels(p, u, ui, fns);
@@ -1000,17 +1001,20 @@ static ssfft_status launch_unstaged(const Plan *p, int inverse, const void *in, 
 	a.rot = tab.rot;
 	a.roots = tab.roots;
 	a.offs = offs;
+	a.offs_out = offs_out;
 	const long long grid = sch.grid((long long)batch);
 	if (grid > 0x7fffffffLL) return SSFFT_ERR_INVALID_SIZE;
 	return jit_launch(inverse ? fns[1] : fns[0], (unsigned)grid, (unsigned)sch.cta_threads(), sch.smem_bytes, s, &a);
 }
 
-// Transforms at scattered offsets (d_offs[g] scalars into in and out), for uneven-size batches.
+// Transforms at scattered offsets: transform g reads d_offs[g] scalars into `in` and writes
+// d_offs_out[g] (d_offs[g] when d_offs_out is null) scalars into `out` (uneven-size batches;
+// requests served straight from their host buffers).
 ssfft_status launch_batch_offs(const Plan *p, int inverse, const void *in, void *out, size_t batch,
-                               const long long *d_offs, cudaStream_t s) {
+                               const long long *d_offs, cudaStream_t s, const long long *d_offs_out) {
 	if (batch == 0) return SSFFT_SUCCESS;
 	if (p->large) return SSFFT_ERR_UNSUPPORTED;
-	if (p->main.sch.staged) return launch_unstaged(p, inverse, in, out, batch, s, d_offs);
+	if (p->main.sch.staged) return launch_unstaged(p, inverse, in, out, batch, s, d_offs, d_offs_out);
 	const Schedule &sch = inverse ? p->main.sch_inv : p->main.sch;
 	const Tables &tab = inverse ? p->main.tab_inv : p->main.tab;
 	ssfft_cl::Args a;
@@ -1027,6 +1031,7 @@ ssfft_status launch_batch_offs(const Plan *p, int inverse, const void *in, void 
 	a.err = p->main.err;
 	a.spin_limit = 1u << 22;
 	a.offs = d_offs;
+	a.offs_out = d_offs_out;
 	a.pf_dist = inverse ? p->main.pf_dist_inv : p->main.pf_dist;
 	const long long grid = sch.grid((long long)batch);
 	if (grid > 0x7fffffffLL) return SSFFT_ERR_INVALID_SIZE;

@@ -11,6 +11,11 @@
 //     the GPU are admitted as soon as buffers and a wave slot free up;
 //   * a host callback at the end of each wave's stream work marks its requests complete (the
 //     latency of a request is completion time minus submit time) and releases its buffers.
+// Requests whose host buffers are page-locked and mapped (cudaHostAlloc / cudaHostRegister; the
+// GPU reaches them over the host link) and whose shape runs in one CTA are served in place: the
+// wave uploads one table of every transform's input and output offsets, and one launch per
+// group reads the inputs from and writes the outputs to the callers' buffers directly, so a
+// request costs no copy call and no arena space.  Other requests take the copy path above.
 // With coalesce = 0 the server runs the plain baseline instead: each request alone, one
 // synchronous copy-in / launch / copy-out at a time, which is what a caller looping over
 // ssfft_exec_host does.
@@ -85,7 +90,22 @@ struct Req {
 	Clock::time_point submitted;
 	int state = 0;  // 0 queued, 1 running, 2 done, 3 failed
 	size_t in_bytes = 0, out_bytes = 0;
+	bool zc = false;  // served in place from mapped host buffers (no copies, no arena)
 };
+
+// Whether [p, p + bytes) is page-locked host memory mapped into the device's address space at the
+// same address (the GPU can load and store it directly).
+bool host_mapped(const void *p, size_t bytes) {
+	if (!p || !bytes) return false;
+	cudaPointerAttributes a, b;
+	const unsigned char *last = static_cast<const unsigned char *>(p) + bytes - 1;
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess || cudaPointerGetAttributes(&b, last) != cudaSuccess) {
+		cudaGetLastError();
+		return false;
+	}
+	return a.type == cudaMemoryTypeHost && b.type == cudaMemoryTypeHost && a.devicePointer == p &&
+	       b.devicePointer == static_cast<const void *>(last);
+}
 
 struct ShapeKey {
 	size_t n;
@@ -129,11 +149,23 @@ double req_flops(const ssfft_request &r) {
 
 struct ServerImpl;
 
+// Requests of one wave with the same (n, dtype, kind, direction, in place): one batched launch.
+using GroupKey = std::tuple<size_t, int, int, int, int>;
+GroupKey group_key(const Req *q) {
+	return GroupKey(q->r.n, (int)q->r.dtype, (int)q->r.kind, q->r.inverse, q->zc ? 1 : 0);
+}
+
+struct WaveGroup {
+	std::vector<Req *> reqs;
+	bool zc = false;
+	size_t in_off = 0, out_off = 0, in_bytes = 0, out_bytes = 0;  // copy groups: arena blocks
+	size_t frames = 0;
+};
+
 struct Wave {
 	ServerImpl *srv = nullptr;
 	int slot = 0;
-	std::vector<Req *> reqs;
-	std::vector<std::pair<size_t, size_t>> blocks;  // arena (offset, bytes) to release
+	std::vector<WaveGroup> groups;
 	bool failed = false;
 };
 
@@ -144,6 +176,9 @@ struct ServerImpl {
 	Arena arena;
 	std::vector<cudaStream_t> streams;
 	std::vector<bool> slot_busy;
+	// per wave slot: pinned host and device tables of the in-place transforms' offsets
+	static constexpr size_t kTableBytes = size_t(1) << 20;
+	std::vector<long long *> h_tab, d_tab;
 	std::mutex mu;
 	std::condition_variable cv;       // scheduler: new work / resources freed
 	std::condition_variable done_cv;  // waiters: completions
@@ -151,7 +186,7 @@ struct ServerImpl {
 	std::deque<std::unique_ptr<Req>> all;  // owns requests; ids are indices + base
 	uint64_t id_base = 0;
 	std::vector<double> lat_us;
-	uint64_t n_submitted = 0, n_completed = 0, n_failed = 0, n_waves = 0, n_launches = 0;
+	uint64_t n_submitted = 0, n_completed = 0, n_failed = 0, n_waves = 0, n_launches = 0, n_in_place = 0;
 	double frames_done = 0, flops_done = 0;
 	Clock::time_point first_submit, last_done;
 	bool have_first = false;
@@ -201,6 +236,7 @@ struct ServerImpl {
 		q->state = ok ? 2 : 3;
 		if (ok) {
 			++n_completed;
+			if (q->zc) ++n_in_place;
 			lat_us.push_back(std::chrono::duration<double, std::micro>(now - q->submitted).count());
 			frames_done += (double)q->r.frames;
 			flops_done += req_flops(q->r);
@@ -216,8 +252,13 @@ struct ServerImpl {
 		const auto now = Clock::now();
 		{
 			std::lock_guard<std::mutex> lock(s->mu);
-			for (Req *q : w->reqs) s->finish_request(q, !w->failed, now);
-			for (auto &b : w->blocks) s->arena.release(b.first, b.second);
+			for (WaveGroup &g : w->groups) {
+				for (Req *q : g.reqs) s->finish_request(q, !w->failed, now);
+				if (!g.zc) {
+					s->arena.release(g.in_off, g.in_bytes);
+					s->arena.release(g.out_off, g.out_bytes);
+				}
+			}
 			s->slot_busy[w->slot] = false;
 			--s->running_waves;
 		}
@@ -229,44 +270,73 @@ struct ServerImpl {
 	// Run one wave on stream slot `slot`.  Called by the scheduler without the lock held.
 	void launch_wave(Wave *w) {
 		cudaStream_t s = streams[w->slot];
-		std::map<std::tuple<size_t, int, int, int>, std::vector<size_t>> groups;  // shape+dir -> req idx
-		for (size_t i = 0; i < w->reqs.size(); ++i) {
-			const ssfft_request &r = w->reqs[i]->r;
-			groups[std::make_tuple(r.n, (int)r.dtype, (int)r.kind, r.inverse)].push_back(i);
-		}
-		size_t bi = 0;
-		for (auto &g : groups) {
-			const auto &idx = g.second;
-			const size_t in_off = w->blocks[bi].first, out_off = w->blocks[bi + 1].first;
-			bi += 2;
-			size_t pos_in = 0, pos_out = 0, frames = 0;
-			for (size_t i : idx) {
-				Req *q = w->reqs[i];
-				if (cudaMemcpyAsync(arena_base + in_off + pos_in, q->r.h_in, q->in_bytes, cudaMemcpyHostToDevice, s) !=
-				    cudaSuccess)
-					w->failed = true;
-				pos_in += q->in_bytes;
-				frames += q->r.frames;
+		// in-place groups: every transform's input and output offset (scalars from the group's first
+		// request buffer) in one table, uploaded with one copy
+		long long *ht = h_tab[w->slot];
+		std::vector<size_t> tab_at(w->groups.size(), 0);
+		size_t tpos = 0;
+		for (size_t gi = 0; gi < w->groups.size(); ++gi) {
+			WaveGroup &g = w->groups[gi];
+			if (!g.zc) continue;
+			const ssfft_request &r0 = g.reqs[0]->r;
+			const size_t sb = scalar_bytes(r0.dtype);
+			const long long fin = (long long)(g.reqs[0]->in_bytes / r0.frames / sb);
+			const long long fout = (long long)(g.reqs[0]->out_bytes / r0.frames / sb);
+			const unsigned char *in0 = static_cast<const unsigned char *>(r0.h_in);
+			const unsigned char *out0 = static_cast<const unsigned char *>(r0.h_out);
+			tab_at[gi] = tpos;
+			size_t k = 0;
+			for (Req *q : g.reqs) {
+				const long long di = (static_cast<const unsigned char *>(q->r.h_in) - in0) / (long long)sb;
+				for (size_t f = 0; f < q->r.frames; ++f) ht[tpos + k++] = di + (long long)f * fin;
 			}
-			const ssfft_request &r0 = w->reqs[idx[0]]->r;
+			k = 0;
+			for (Req *q : g.reqs) {
+				const long long dout = (static_cast<unsigned char *>(q->r.h_out) - out0) / (long long)sb;
+				for (size_t f = 0; f < q->r.frames; ++f) ht[tpos + g.frames + k++] = dout + (long long)f * fout;
+			}
+			tpos += 2 * g.frames;
+		}
+		if (tpos && cudaMemcpyAsync(d_tab[w->slot], ht, tpos * sizeof(long long), cudaMemcpyHostToDevice, s) !=
+		                cudaSuccess)
+			w->failed = true;
+		for (size_t gi = 0; gi < w->groups.size(); ++gi) {
+			WaveGroup &g = w->groups[gi];
+			const ssfft_request &r0 = g.reqs[0]->r;
 			ssfft_plan_t plan = nullptr;
-			if (get_plan(r0, w->slot, plan) != SSFFT_SUCCESS) {
-				w->failed = true;
-			} else {
-				const size_t cap = ssfft_plan_batch(plan);
-				const size_t fin = w->reqs[idx[0]]->in_bytes / r0.frames, fout = w->reqs[idx[0]]->out_bytes / r0.frames;
-				for (size_t f0 = 0; f0 < frames; f0 += cap) {
-					const size_t nb = std::min(cap, frames - f0);
-					if (ssfft_exec_batch(plan, r0.inverse, arena_base + in_off + f0 * fin, arena_base + out_off + f0 * fout,
-					                     nb, s) != SSFFT_SUCCESS)
+			const bool have_plan = get_plan(r0, w->slot, plan) == SSFFT_SUCCESS;
+			if (!have_plan) w->failed = true;
+			const size_t cap = have_plan ? ssfft_plan_batch(plan) : 1;
+			if (g.zc) {
+				const long long *d_in_offs = d_tab[w->slot] + tab_at[gi];
+				for (size_t f0 = 0; have_plan && f0 < g.frames; f0 += cap) {
+					const size_t nb = std::min(cap, g.frames - f0);
+					if (launch_batch_offs(reinterpret_cast<const Plan *>(plan), r0.inverse, r0.h_in, r0.h_out, nb,
+					                      d_in_offs + f0, s, d_in_offs + g.frames + f0) != SSFFT_SUCCESS)
 						w->failed = true;
 					std::lock_guard<std::mutex> lock(mu);
 					++n_launches;
 				}
+				continue;
 			}
-			for (size_t i : idx) {
-				Req *q = w->reqs[i];
-				if (cudaMemcpyAsync(q->r.h_out, arena_base + out_off + pos_out, q->out_bytes, cudaMemcpyDeviceToHost, s) !=
+			size_t pos_in = 0, pos_out = 0;
+			for (Req *q : g.reqs) {
+				if (cudaMemcpyAsync(arena_base + g.in_off + pos_in, q->r.h_in, q->in_bytes, cudaMemcpyHostToDevice, s) !=
+				    cudaSuccess)
+					w->failed = true;
+				pos_in += q->in_bytes;
+			}
+			const size_t fin = g.reqs[0]->in_bytes / r0.frames, fout = g.reqs[0]->out_bytes / r0.frames;
+			for (size_t f0 = 0; have_plan && f0 < g.frames; f0 += cap) {
+				const size_t nb = std::min(cap, g.frames - f0);
+				if (ssfft_exec_batch(plan, r0.inverse, arena_base + g.in_off + f0 * fin, arena_base + g.out_off + f0 * fout,
+				                     nb, s) != SSFFT_SUCCESS)
+					w->failed = true;
+				std::lock_guard<std::mutex> lock(mu);
+				++n_launches;
+			}
+			for (Req *q : g.reqs) {
+				if (cudaMemcpyAsync(q->r.h_out, arena_base + g.out_off + pos_out, q->out_bytes, cudaMemcpyDeviceToHost, s) !=
 				    cudaSuccess)
 					w->failed = true;
 				pos_out += q->out_bytes;
@@ -282,69 +352,59 @@ struct ServerImpl {
 
 	// Take admitted requests for one wave (lock held); returns nullptr if nothing fits now.
 	Wave *form_wave(int slot) {
+		const size_t maxr = cfg.coalesce ? (size_t)cfg.max_requests_per_wave : 1;
+		// group in arrival order
+		std::map<GroupKey, size_t> index;
+		std::vector<WaveGroup> groups;
+		std::vector<Req *> back;
+		size_t taken = 0, table = 0;
+		const size_t table_cap = kTableBytes / sizeof(long long);
+		while (!pending.empty() && taken < maxr) {
+			Req *q = pending.front();
+			pending.pop_front();
+			++taken;
+			if (q->zc && table + 2 * q->r.frames > table_cap) {
+				back.push_back(q);  // the offset table is full: next wave
+				continue;
+			}
+			if (q->zc) table += 2 * q->r.frames;
+			auto it = index.find(group_key(q));
+			if (it == index.end()) {
+				it = index.emplace(group_key(q), groups.size()).first;
+				groups.emplace_back();
+				groups.back().zc = q->zc;
+			}
+			WaveGroup &g = groups[it->second];
+			g.reqs.push_back(q);
+			g.frames += q->r.frames;
+			g.in_bytes += q->in_bytes;
+			g.out_bytes += q->out_bytes;
+		}
+		// arena blocks for the copy groups; groups that do not fit go back to the queue
 		Wave *w = new Wave();
 		w->srv = this;
 		w->slot = slot;
-		const size_t maxr = cfg.coalesce ? (size_t)cfg.max_requests_per_wave : 1;
-		// group in arrival order; each group needs one contiguous in and out block
-		std::map<std::tuple<size_t, int, int, int>, std::vector<Req *>> groups;
-		std::vector<std::tuple<size_t, int, int, int>> order;
-		size_t taken = 0;
-		while (!pending.empty() && taken < maxr) {
-			Req *q = pending.front();
-			auto key = std::make_tuple(q->r.n, (int)q->r.dtype, (int)q->r.kind, q->r.inverse);
-			if (!groups.count(key)) order.push_back(key);
-			groups[key].push_back(q);
-			pending.pop_front();
-			++taken;
-		}
-		// allocate per group; groups that do not fit go back to the front, in order
-		std::vector<Req *> back;
-		for (auto &key : order) {
-			auto &v = groups[key];
-			size_t bin = 0, bout = 0;
-			for (Req *q : v) bin += q->in_bytes, bout += q->out_bytes;
-			size_t oi = 0, oo = 0;
-			bool ok = arena.alloc(bin, oi);
-			if (ok && !arena.alloc(bout, oo)) {
-				arena.release(oi, bin);
-				ok = false;
+		for (WaveGroup &g : groups) {
+			if (!g.zc) {
+				bool ok = arena.alloc(g.in_bytes, g.in_off);
+				if (ok && !arena.alloc(g.out_bytes, g.out_off)) {
+					arena.release(g.in_off, g.in_bytes);
+					ok = false;
+				}
+				if (!ok) {
+					back.insert(back.end(), g.reqs.begin(), g.reqs.end());
+					continue;
+				}
 			}
-			if (!ok) {
-				back.insert(back.end(), v.begin(), v.end());
-				continue;
-			}
-			w->blocks.push_back({oi, bin});
-			w->blocks.push_back({oo, bout});
-			for (Req *q : v) {
-				q->state = 1;
-				w->reqs.push_back(q);
-			}
+			for (Req *q : g.reqs) q->state = 1;
+			w->groups.push_back(std::move(g));
 		}
 		// keep FIFO order for the ones sent back
 		std::sort(back.begin(), back.end(), [](Req *a, Req *b) { return a->id < b->id; });
 		for (auto it = back.rbegin(); it != back.rend(); ++it) pending.push_front(*it);
-		if (w->reqs.empty()) {
+		if (w->groups.empty()) {
 			delete w;
 			return nullptr;
-		}
-		// launch_wave walks groups in key order; lay blocks out to match
-		std::map<std::tuple<size_t, int, int, int>, std::pair<std::pair<size_t, size_t>, std::pair<size_t, size_t>>> blk;
-		std::vector<Req *> ordered;
-		size_t bi = 0;
-		std::map<std::tuple<size_t, int, int, int>, std::vector<Req *>> placed;
-		for (Req *q : w->reqs) placed[std::make_tuple(q->r.n, (int)q->r.dtype, (int)q->r.kind, q->r.inverse)].push_back(q);
-		for (auto &key : order) {
-			if (!placed.count(key)) continue;
-			blk[key] = {w->blocks[bi], w->blocks[bi + 1]};
-			bi += 2;
-		}
-		w->blocks.clear();
-		w->reqs.clear();
-		for (auto &kv : placed) {
-			w->blocks.push_back(blk[kv.first].first);
-			w->blocks.push_back(blk[kv.first].second);
-			for (Req *q : kv.second) w->reqs.push_back(q);
 		}
 		return w;
 	}
@@ -455,6 +515,26 @@ ssfft_status ssfft_server_create(ssfft_server_t *out, const ssfft_server_config 
 		s->streams.push_back(st);
 	}
 	s->slot_busy.assign(nstreams, false);
+	// per-slot offset tables of the in-place groups (batched servers only)
+	if (s->cfg.coalesce) {
+		for (int i = 0; i < nstreams; ++i) {
+			void *h = nullptr, *d = nullptr;
+			e = cudaHostAlloc(&h, ServerImpl::kTableBytes, cudaHostAllocDefault);
+			if (e == cudaSuccess) e = cudaMalloc(&d, ServerImpl::kTableBytes);
+			if (e != cudaSuccess) {
+				if (h) cudaFreeHost(h);
+				for (size_t k = 0; k < s->h_tab.size(); ++k) {
+					cudaFreeHost(s->h_tab[k]);
+					cudaFree(s->d_tab[k]);
+				}
+				for (auto x : s->streams) cudaStreamDestroy(x);
+				cudaFree(base);
+				return cuda_fail(e, "server offset tables");
+			}
+			s->h_tab.push_back(static_cast<long long *>(h));
+			s->d_tab.push_back(static_cast<long long *>(d));
+		}
+	}
 	ServerImpl *raw = s.get();
 	s->worker = std::thread([raw] { raw->loop(); });
 	*out = reinterpret_cast<ssfft_server_t>(s.release());
@@ -485,7 +565,14 @@ ssfft_status ssfft_server_submit(ssfft_server_t srv, const ssfft_request *req, u
 	std::unique_ptr<Req> q(new Req());
 	q->r = *req;
 	req_bytes(q->r, q->in_bytes, q->out_bytes);
-	if (q->in_bytes + q->out_bytes + 512 > s->cfg.hbm_budget_bytes) return SSFFT_ERR_BUDGET;
+	// in place: batched server, a shape that runs in one CTA, mapped host buffers aligned for the
+	// kernel's paired loads and stores, and a table share that fits one wave
+	const size_t align = 2 * scalar_bytes(q->r.dtype);
+	q->zc = s->cfg.coalesce && debug_knob("serve_inplace", 1) != 0 && !multi_pass(q->r) &&
+	        2 * q->r.frames <= ServerImpl::kTableBytes / sizeof(long long) &&
+	        (uintptr_t)q->r.h_in % align == 0 && (uintptr_t)q->r.h_out % align == 0 &&
+	        host_mapped(q->r.h_in, q->in_bytes) && host_mapped(q->r.h_out, q->out_bytes);
+	if (!q->zc && q->in_bytes + q->out_bytes + 512 > s->cfg.hbm_budget_bytes) return SSFFT_ERR_BUDGET;
 	q->submitted = Clock::now();
 	{
 		std::lock_guard<std::mutex> lock(s->mu);
@@ -541,6 +628,7 @@ ssfft_status ssfft_server_get_stats(ssfft_server_t srv, ssfft_server_stats *st, 
 	st->failed = s->n_failed;
 	st->waves = s->n_waves;
 	st->launches = s->n_launches;
+	st->in_place = s->n_in_place;
 	st->frames = s->frames_done;
 	st->flops = s->flops_done;
 	if (s->have_first && s->n_completed)
@@ -563,7 +651,7 @@ ssfft_status ssfft_server_get_stats(ssfft_server_t srv, ssfft_server_stats *st, 
 		// keep request records of anything still in flight; forget the statistics
 		s->lat_us.clear();
 		s->n_submitted -= s->n_completed + s->n_failed;
-		s->n_completed = s->n_failed = s->n_waves = s->n_launches = 0;
+		s->n_completed = s->n_failed = s->n_waves = s->n_launches = s->n_in_place = 0;
 		s->frames_done = s->flops_done = 0;
 		s->have_first = false;
 	}
@@ -592,6 +680,10 @@ ssfft_status ssfft_server_destroy(ssfft_server_t srv) {
 		cudaStreamDestroy(st);
 	}
 	for (auto &kv : s->plans) ssfft_plan_destroy(kv.second);
+	for (size_t k = 0; k < s->h_tab.size(); ++k) {
+		cudaFreeHost(s->h_tab[k]);
+		cudaFree(s->d_tab[k]);
+	}
 	if (s->arena_base) cudaFree(s->arena_base);
 	delete s;
 	return SSFFT_SUCCESS;

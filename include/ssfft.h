@@ -200,9 +200,13 @@ typedef struct {
 	int inverse;
 	size_t n;          /* transform size (real length for real kinds) */
 	size_t frames;     /* transforms in this request, stored back to back */
-	const void *h_in;  /* host input (pinned memory overlaps best); valid until completion */
+	const void *h_in;  /* host input; valid until completion */
 	void *h_out;       /* host output; valid until completion */
 } ssfft_request;
+/* Requests whose h_in and h_out are page-locked and mapped (cudaHostAlloc, cudaHostRegister),
+ * aligned to two scalars, and whose shape runs in one CTA are served in place by a batched server:
+ * its kernels read the input from and write the output to those buffers over the host link, and
+ * the request takes no arena space.  Other requests are copied through the HBM arena. */
 
 typedef struct {
 	uint64_t submitted, completed, failed, waves, launches;
@@ -210,6 +214,7 @@ typedef struct {
 	double span_seconds;   /* first submit to last completion */
 	double frames;         /* transforms completed */
 	double flops;          /* 5 n log2 n per complex, 2.5 n log2 n per real transform completed */
+	uint64_t in_place;     /* requests served in place from mapped host buffers (no copies) */
 } ssfft_server_stats;
 
 ssfft_status ssfft_server_create(ssfft_server_t *srv, const ssfft_server_config *cfg);

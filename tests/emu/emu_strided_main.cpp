@@ -12,7 +12,11 @@
 // Bluestein element-wise kernels (emu_blue_cases.inc): argv = "b<case>", blocks per transform,
 //       transforms, raw input file, raw output file, raw work file (both written back), table
 //       file, n, m, distance between transforms, table byte offsets of the chirp and of the
-//       spectrum of b.
+//       spectrum of b [, table byte offsets of the half-shift rotations applied to the input and
+//       to the output, -1 for none].
+// Odd-length pack / unpack (emu_pack_cases.inc): argv = "k<case>", blocks per transform, raw
+//       source file, raw destination file (pre-filled; written back), transforms, real length n,
+//       complex points per transform h.
 #include "cuda_emu.h"
 #include "ssfft_codelets.cuh"
 
@@ -71,10 +75,19 @@ static const BlueCase kBlueCases[] = {
 #include "emu_blue_cases.inc"
 	{nullptr, nullptr}};
 
+struct PackCase {
+	const char *name;
+	void (*fn)(const ssfft_cl::PackArgs);
+};
+static const PackCase kPackCases[] = {
+#include "emu_pack_cases.inc"
+	{nullptr, nullptr}};
+
 // real_split and the Bluestein kernels: 256 threads per block (no barriers), blockIdx.y =
 // transform
 static int run_split(int argc, char **argv);
 static int run_blue(int argc, char **argv);
+static int run_pack(int argc, char **argv);
 
 static std::vector<char> slurp(const char *path) {
 	std::ifstream f(path, std::ios::binary);
@@ -84,6 +97,7 @@ static std::vector<char> slurp(const char *path) {
 int main(int argc, char **argv) {
 	if (argc > 1 && argv[1][0] == 's') return run_split(argc, argv);
 	if (argc > 1 && argv[1][0] == 'b') return run_blue(argc, argv);
+	if (argc > 1 && argv[1][0] == 'k') return run_pack(argc, argv);
 	if (argc != 21 || argv[1][0] != 'p') return 2;
 	const Case &c = kCases[std::atoi(argv[1] + 1)];
 	const int grid = std::atoi(argv[2]);
@@ -158,8 +172,33 @@ static int run_split(int argc, char **argv) {
 	return 0;
 }
 
+static int run_pack(int argc, char **argv) {
+	if (argc != 8) return 2;
+	const PackCase &c = kPackCases[std::atoi(argv[1] + 1)];
+	const int blocks = std::atoi(argv[2]);
+	std::vector<char> src = slurp(argv[3]), dst = slurp(argv[4]);
+	ssfft_cl::PackArgs a{};
+	a.src = src.data();
+	a.dst = dst.data();
+	a.batch = std::atoll(argv[5]);
+	a.n = std::atoll(argv[6]);
+	a.h = std::atoll(argv[7]);
+	for (long long y = 0; y < a.batch; ++y)
+		for (int b = 0; b < blocks; ++b)
+			for (int t = 0; t < 256; ++t) {
+				threadIdx.x = (unsigned)t;
+				blockIdx.x = (unsigned)b;
+				blockIdx.y = (unsigned)y;
+				gridDim.x = (unsigned)blocks;
+				c.fn(a);
+			}
+	std::ofstream f(argv[4], std::ios::binary);
+	f.write(dst.data(), (std::streamsize)dst.size());
+	return 0;
+}
+
 static int run_blue(int argc, char **argv) {
-	if (argc != 13) return 2;
+	if (argc != 13 && argc != 15) return 2;
 	const BlueCase &c = kBlueCases[std::atoi(argv[1] + 1)];
 	const int blocks = std::atoi(argv[2]);
 	std::vector<char> in = slurp(argv[4]), out = slurp(argv[5]), work = slurp(argv[6]), tab = slurp(argv[7]);
@@ -173,6 +212,11 @@ static int run_blue(int argc, char **argv) {
 	a.dist = std::atoll(argv[10]);
 	a.chirp = tab.data() + std::atoll(argv[11]);
 	a.bhat = tab.data() + std::atoll(argv[12]);
+	if (argc == 15) {
+		const long long ri = std::atoll(argv[13]), ro = std::atoll(argv[14]);
+		a.rot_in = ri >= 0 ? tab.data() + ri : nullptr;
+		a.rot_out = ro >= 0 ? tab.data() + ro : nullptr;
+	}
 	for (long long y = 0; y < a.batch; ++y)
 		for (int b = 0; b < blocks; ++b)
 			for (int t = 0; t < 256; ++t) {

@@ -24,14 +24,18 @@ CASES = [(20000, "f32", "complex", 2), (32768, "f32", "complex", 1), (10000, "f6
          (1 << 21, "f32", "complex", 1), (2 * 3 ** 9, "f32", "complex", 1), (40000, "f32", "real", 2),
          (40000, "f32", "real_halfshift", 1), (20000, "f64", "real", 1), (20000, "f64", "real_halfshift", 1),
          (17527, "f32", "complex", 1), (10007, "f64", "complex", 1), (35054, "f32", "real", 1),
-         (20014, "f64", "real", 1)]
+         (20014, "f64", "real", 1),
+         # the reference accepts every length: odd real lengths beyond one CTA (packed rows, the
+         # last real neither read nor written) and half-shift lengths that need Bluestein
+         (40001, "f32", "real", 3), (40001, "f32", "real_halfshift", 2), (20003, "f64", "real", 2),
+         (35054, "f32", "real_halfshift", 1), (35055, "f32", "real", 2), (20014, "f64", "real_halfshift", 1)]
 
 
 class Emu:
     """The emulator binary, its case tables and the planner's records of every case."""
 
     def __init__(self, d):
-        self.d, self.passes, self.splits, self.blues, self.specs = d, [], [], [], {}
+        self.d, self.passes, self.splits, self.blues, self.packs, self.specs = d, [], [], [], [], {}
 
     def add_plan(self, n, dt, kind):
         key = (n, dt, kind)
@@ -39,7 +43,7 @@ class Emu:
             return self.specs[key]
         spec, blob = F.large_spec(n, dt, kind)
         rec = {"spec": spec, "blob": blob, "pass0": len(self.passes), "split0": len(self.splits),
-               "blue0": len(self.blues)}
+               "blue0": len(self.blues), "pack0": len(self.packs)}
         for p in spec["passes"]:
             for k in ("fwd", "inv"):
                 self.passes.append(f'{{"{n}-{dt}-{k}", &{p[k]}, {p["cta"]}, {p["smem"]}}},')
@@ -48,6 +52,8 @@ class Emu:
                             f'{{"{n}-{dt}-{kind}-inv", &{spec["split_inv"]}}},']
         if "M" in spec:
             self.blues += [f'{{"{n}-{dt}-blue{i}", &{name}}},' for i, name in enumerate(spec["blue"])]
+        if spec.get("odd"):
+            self.packs += [f'{{"{n}-{dt}-pack", &{spec["pack"]}}},', f'{{"{n}-{dt}-unpack", &{spec["unpack"]}}},']
         self.specs[key] = rec
         if "M" in spec:
             rec["inner"] = self.add_plan(spec["M"], dt, "complex")
@@ -55,7 +61,7 @@ class Emu:
 
     def build(self):
         for name, lines in (("emu_strided_cases.inc", self.passes), ("emu_split_cases.inc", self.splits),
-                            ("emu_blue_cases.inc", self.blues)):
+                            ("emu_blue_cases.inc", self.blues), ("emu_pack_cases.inc", self.packs)):
             (self.d / name).write_text("\n".join(lines) + "\n")
         self.exe = self.d / "emu_strided"
         cmd = ["g++", "-std=c++20", "-O2", "-pthread", "-w", "-I", str(self.d), "-I",
@@ -108,9 +114,18 @@ def _split(e, rec, inverse, src, buf, nb, table):
     return np.frombuffer(fo.read_bytes(), dtype=buf.dtype).copy()
 
 
-def _bluestein(e, rec, cur, nb, cin, cout, dt):
+def _pack(e, rec, src, dst, nb, n, unpack):
+    """Odd real lengths: rows of n reals to rows of N complex (or back)."""
+    N = rec["spec"]["N"]
+    fi, fo = e.file("kin", src), e.file("kout", dst)
+    e.run([f"k{rec['pack0'] + int(unpack)}", -(-N // 256), fi, fo, nb, n, N])
+    return np.frombuffer(fo.read_bytes(), dtype=dst.dtype).copy()
+
+
+def _bluestein(e, rec, cur, nb, cin, cout, dt, rot_in=-1, rot_out=-1):
     """Bluestein's launches in the library's order: chirp product, M-point forward, product with
-    the spectrum of b, M-point inverse, final chirp product scaled by 1/M."""
+    the spectrum of b, M-point inverse, final chirp product scaled by 1/M (with the half-shift
+    rotation on the input of a forward, on the output of an inverse)."""
     spec, inner = rec["spec"], rec["inner"]
     N, M = spec["N"], spec["M"]
     sdt = _sdt(dt)
@@ -128,7 +143,8 @@ def _bluestein(e, rec, cur, nb, cin, cout, dt):
 
     def blue(i, grid, o, w):
         fi, fo, fw = e.file("bin", cur), e.file("bout", o), e.file("bwork", w)
-        e.run([f"b{rec['blue0'] + i}", grid, nb, fi, fo, fw, table, N, M, N, spec["off_chirp"], spec["off_bhat"]])
+        e.run([f"b{rec['blue0'] + i}", grid, nb, fi, fo, fw, table, N, M, N, spec["off_chirp"], spec["off_bhat"],
+               rot_in if i in (0, 1) else -1, rot_out if i in (3, 4) else -1])
         return (np.frombuffer(fo.read_bytes(), dtype=sdt).copy(), np.frombuffer(fw.read_bytes(), dtype=sdt).copy())
 
     _, work = blue(1 if cin else 0, gm, out, work)
@@ -140,25 +156,37 @@ def _bluestein(e, rec, cur, nb, cin, cout, dt):
 
 
 def _transform(e, n, dt, kind, x, inverse):
-    """x: [transforms, complex points] (the reals viewed as pairs for a RealFFT forward, the
-    bins for its inverse); returns the same shape, launched as the library launches it."""
+    """x: [transforms, n] reals for a RealFFT forward, [transforms, N] bins for its inverse,
+    [transforms, n] complex points otherwise; returns [transforms, N] complex (forward), [transforms,
+    n] reals (RealFFT inverse; for odd n the last real of a row is the prefilled NaN, unwritten) or
+    complex points, launched as the library launches it."""
     rec = e.specs[(n, dt, kind)]
     spec = rec["spec"]
     sdt = _sdt(dt)
-    nb, N = x.shape
-    cur = np.ascontiguousarray(x).view(sdt).reshape(-1)
     real = bool(spec["real"])
+    odd = bool(spec.get("odd"))
+    N = spec["N"]
+    nb = x.shape[0]
+    cur = np.ascontiguousarray(x).view(sdt).reshape(-1)
     table = e.file("tab", rec["blob"])
+    if real and not inverse and odd:
+        cur = _pack(e, rec, cur, np.full(nb * 2 * N, np.nan, dtype=sdt), nb, n, False)
     if real and inverse:
         cur = _split(e, rec, True, cur, np.full_like(cur, np.nan), nb, table)
     if "M" in spec:
-        cur = _bluestein(e, rec, cur, nb, inverse and not real, inverse, dt)
+        mod = bool(spec.get("modified"))
+        cur = _bluestein(e, rec, cur, nb, inverse and not real, inverse, dt,
+                         spec["off_brot"] if mod and not inverse else -1, spec["off_brot"] if mod and inverse else -1)
     else:
         cur = _passes(e, rec, cur, nb, inverse, table)
     if real and not inverse:
         cur = _split(e, rec, False, cur, cur, nb, table)
     cdt = np.complex64 if dt == "f32" else np.complex128
-    return cur.view(cdt).reshape(nb, N)
+    if real and inverse:
+        if odd:
+            return _pack(e, rec, cur, np.full(nb * n, np.nan, dtype=sdt), nb, n, True).reshape(nb, n)
+        return cur.reshape(nb, n)
+    return cur.view(cdt).reshape(nb, -1)
 
 
 @pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}-{c[1]}-{c[2]}")
@@ -181,10 +209,13 @@ def test_emulated_path_beyond_one_cta_matches_oracle(emu, case):
     else:
         mod = kind == "real_halfshift"
         x = rng.standard_normal((nb, n)).astype(rdt)
-        got = _transform(emu, n, dt, kind, x.view(cdt), False)
+        got = _transform(emu, n, dt, kind, x, False)
+        assert np.all(np.isfinite(got)), "every bin written"
         ref = np.stack([oracle.rfft(r.astype(np.float64), mod) for r in x])
         assert rel_l2(got, ref) <= tol, rel_l2(got, ref)
         s = (rng.standard_normal((nb, n // 2)) + 1j * rng.standard_normal((nb, n // 2))).astype(cdt)
-        back = _transform(emu, n, dt, kind, s, True).view(rdt)
+        back = _transform(emu, n, dt, kind, s, True)
+        h2 = 2 * (n // 2)
+        assert np.all(np.isfinite(back[:, :h2])) and np.all(np.isnan(back[:, h2:])), "2*(n//2) reals written"
         ref = np.stack([oracle.irfft(r.astype(np.complex128), n, mod) for r in s])
-        assert rel_l2(back, ref) <= tol, rel_l2(back, ref)
+        assert rel_l2(back[:, :h2], ref) <= tol, rel_l2(back[:, :h2], ref)

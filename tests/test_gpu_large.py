@@ -167,3 +167,37 @@ def test_bluestein_real_vs_oracle(F, n):
     ref = oracle.rfft(x[0].astype(np.float64))
     assert rel_l2(s.cpu().numpy()[0], ref) <= 2e-6, rel_l2(s.cpu().numpy()[0], ref)
     assert rel_l2(b.cpu().numpy() / n, x) <= 4e-6
+
+
+# Lengths the reference accepts that need the path beyond one CTA in a special form: odd real
+# lengths (packed rows: the last real is neither read nor written, signalsmith-fft.h:446-502) and
+# half-shift lengths with a prime factor above 1024 (Bluestein with the rotations on its chirp
+# kernels).  Batches of several transforms, so odd rows start at odd offsets.
+@pytest.mark.parametrize("n,dt,kind,b,tol", [
+    (40001, "f32", "real", 3, 1e-6), (40001, "f32", "real_halfshift", 2, 1e-6), (35055, "f32", "real", 3, 2e-6),
+    (20003, "f64", "real", 2, 1e-13), (35054, "f32", "real_halfshift", 2, 2e-6), (2 * 20011 * 2, "f32", "real_halfshift", 1, 2e-6),
+    (20014, "f64", "real_halfshift", 1, 5e-11)])
+def test_reference_lengths_beyond_one_cta(F, n, dt, kind, b, tol):
+    rng = np.random.default_rng(n + b)
+    mod = kind == "real_halfshift"
+    rdt = np.float32 if dt == "f32" else np.float64
+    cdt = np.complex64 if dt == "f32" else np.complex128
+    h = n // 2
+    x = rng.standard_normal((b, n)).astype(rdt)
+    p = F.Plan(n, dt, kind, b)
+    xi = torch.from_numpy(x).cuda()
+    spec = torch.full((b, h), complex(5, 5), dtype=torch.complex64 if dt == "f32" else torch.complex128,
+                      device="cuda")
+    p.exec(False, xi.data_ptr(), spec.data_ptr(), 0)
+    back = torch.full_like(xi, 7.0)
+    p.exec(True, spec.data_ptr(), back.data_ptr(), 0)
+    torch.cuda.synchronize()
+    s = spec.cpu().numpy()
+    ref = np.stack([oracle.rfft(r.astype(np.float64), mod) for r in x])
+    assert rel_l2(s, ref) <= tol, rel_l2(s, ref)
+    bk = back.cpu().numpy()
+    refb = np.stack([oracle.irfft(r.astype(np.complex128), n, mod) for r in s.astype(cdt)])
+    assert rel_l2(bk[:, :2 * h], refb) <= tol, rel_l2(bk[:, :2 * h], refb)
+    if n & 1:
+        assert np.all(bk[:, 2 * h:] == 7.0), "the last real of an odd row is not written"
+    assert np.array_equal(xi.cpu().numpy(), x)

@@ -107,3 +107,52 @@ def test_loadgen_reports_latency_and_throughput(F):
     assert 0 < st["p50_latency_us"] <= st["p99_latency_us"]
     assert st["frames"] > 0 and st["flops"] > 0
     srv.close()
+
+
+def _pinned_like(a):
+    """A page-locked (and, under unified addressing, device-mapped) copy of a numpy array."""
+    t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    return t, t.numpy()
+
+
+def test_in_place_requests_match_copy_path_and_oracle(F):
+    """Requests in pinned host buffers are served in place (the kernels read and write the host
+    buffers, no copies): mixed single-CTA shapes, both directions, in place and copied requests in
+    the same waves; every result equals the oracle and, bit for bit, the copied result."""
+    rng = np.random.default_rng(17)
+    shapes = [(256, "complex"), (480, "real"), (1920, "real"), (3840, "real"), (1000, "complex"),
+              (4096, "real_halfshift"), (98, "real"), (7, "complex"), (16384, "complex"), (32768, "real")]
+    srv = F.Server(hbm_budget_bytes=256 << 20, waves=3, max_requests_per_wave=24)
+    keep, jobs = [], []
+    for i in range(48):
+        n, kind = shapes[i % len(shapes)]
+        inverse = bool(i % 3 == 1)
+        x, out = make_request(rng, n, kind, inverse, 1 + (i * 5) % 7)
+        tx, px = _pinned_like(x)
+        to, po = _pinned_like(out)
+        keep += [tx, to]
+        t1 = srv.submit(n, kind, inverse, px, po, frames=x.shape[0])
+        o2 = np.empty_like(out)
+        t2 = srv.submit(n, kind, inverse, x, o2, frames=x.shape[0])   # pageable: copy path
+        jobs.append((t1, t2, n, kind, inverse, x, po, o2))
+    srv.drain()
+    st = srv.stats()
+    assert st["failed"] == 0 and st["completed"] == 96
+    assert st["in_place"] == 48, st["in_place"]
+    for t1, t2, n, kind, inverse, x, po, o2 in jobs:
+        assert np.array_equal(po, o2), (n, kind, inverse)
+        ref = expected(x, n, kind, inverse)
+        assert rel_l2(po, ref) <= 1e-6, (n, kind, inverse, rel_l2(po, ref))
+    srv.close()
+
+
+def test_plain_server_never_in_place(F):
+    rng = np.random.default_rng(18)
+    plain = F.Server(hbm_budget_bytes=64 << 20, coalesce=False)
+    x, out = make_request(rng, 480, "real", False, 2)
+    tx, px = _pinned_like(x)
+    to, po = _pinned_like(out)
+    plain.wait(plain.submit(480, "real", False, px, po, frames=2))
+    assert plain.stats()["in_place"] == 0
+    assert rel_l2(po, expected(x, 480, "real", False)) <= 1e-6
+    plain.close()
