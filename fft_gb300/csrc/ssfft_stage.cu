@@ -124,10 +124,28 @@ static constexpr size_t kBounceMax = size_t(4) << 20;
 static ssfft_status exec_host_small(Plan *p, int inverse, const void *h_in, void *h_out, size_t in_b, size_t out_b) {
 	HostStage *sg = p->stage;
 	if (!sg->bounce_in) {
-		cudaError_t e = cudaHostAlloc(&sg->bounce_in, kBounceMax, cudaHostAllocDefault);
-		if (e == cudaSuccess) e = cudaHostAlloc(&sg->bounce_out, kBounceMax, cudaHostAllocDefault);
+		cudaError_t e = cudaHostAlloc(&sg->bounce_in, kBounceMax, cudaHostAllocMapped);
+		if (e == cudaSuccess) e = cudaHostAlloc(&sg->bounce_out, kBounceMax, cudaHostAllocMapped);
 		if (e != cudaSuccess) return cuda_fail(e, "exec_host bounce buffers");
 		sg->bounce_bytes = kBounceMax;
+	}
+	// one-CTA plans with plain loads and stores (not the bulk-copy staged, tensor-core or cluster
+	// kernels) run the kernel on the mapped bounce buffers themselves, over the host link: no copy
+	// calls, one launch (debug switch small_zc=0 copies through device buffers instead)
+	const Schedule &sch = p->main.sch;
+	if (!p->large && !sch.staged && !sch.tc && !sch.pair && debug_knob("small_zc", 1) != 0) {
+		void *d_bin = nullptr, *d_bout = nullptr;
+		cudaError_t e = cudaHostGetDevicePointer(&d_bin, sg->bounce_in, 0);
+		if (e == cudaSuccess) e = cudaHostGetDevicePointer(&d_bout, sg->bounce_out, 0);
+		if (e != cudaSuccess) return cuda_fail(e, "exec_host mapped bounce buffers");
+		std::memcpy(sg->bounce_in, h_in, in_b);
+		cudaStream_t s = sg->stream[0];
+		ssfft_status st = launch_batch(p, inverse, d_bin, d_bout, p->batch, s);
+		if (st != SSFFT_SUCCESS) return st;
+		e = cudaStreamSynchronize(s);
+		if (e != cudaSuccess) return cuda_fail(e, "exec_host sync");
+		std::memcpy(h_out, sg->bounce_out, out_b);
+		return SSFFT_SUCCESS;
 	}
 	const bool pin_in = pinned_host(h_in, in_b), pin_out = pinned_host(h_out, out_b);
 	const void *src = h_in;
