@@ -336,12 +336,16 @@ def run_gpu(args, rank: int, world: int):
     elapsed = max_over_ranks(t0.elapsed_time(t1) / 1e3, dist, "cuda")
     value = flops_per_step(frames) * passes * args.steps * world / elapsed / 1e9
 
-    # per-kernel durations for the roofline: each kernel timed alone on the launching stream,
-    # CUDA events around `reps` back-to-back launches of it (idempotent: same input and output),
-    # mean per launch; each launch streams >= 63 MB, so no launch is served from L2
-    reps = max(10, args.steps // 20)
+    # per-kernel durations for the roofline: each kernel timed alone, CUDA events around `reps`
+    # back-to-back launches of it (idempotent: same input and output), mean per launch.  The
+    # launches are captured in a CUDA graph, so the gaps between them are the device's, not the
+    # host's launch rate (a 14 us kernel would otherwise carry ~1 us of launch overhead each);
+    # the mean over plain stream launches is reported beside it.
+    reps = max(20, args.steps)
     kt = np.zeros(nl)
+    kt_stream = np.zeros(nl)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    gstream = torch.cuda.Stream()
     for i, (p, x, s, b) in enumerate(zip(plans, xs, specs, backs)):
         for d, (src, dst) in enumerate(((x, s), (s, b))):
             p.exec(bool(d), src.data_ptr(), dst.data_ptr(), sh)
@@ -350,7 +354,20 @@ def run_gpu(args, rank: int, world: int):
                 p.exec(bool(d), src.data_ptr(), dst.data_ptr(), sh)
             ev1.record(stream)
             torch.cuda.synchronize()
+            kt_stream[2 * i + d] = ev0.elapsed_time(ev1) / 1e3 / reps
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=gstream):
+                gsh = int(torch.cuda.current_stream().cuda_stream)
+                for _ in range(reps):
+                    p.exec(bool(d), src.data_ptr(), dst.data_ptr(), gsh)
+            g.replay()
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            g.replay()
+            ev1.record(stream)
+            torch.cuda.synchronize()
             kt[2 * i + d] = ev0.elapsed_time(ev1) / 1e3 / reps
+            del g
     names, alg = [], []
     for n in SIZES:
         for d in ("r2c", "c2r"):
@@ -360,7 +377,8 @@ def run_gpu(args, rank: int, world: int):
     peak, peak_kind = measured_peak_hbm()
     achieved = alg[top] / kt[top] / 1e9
     kernels = {names[j]: {"ms": round(kt[j] * 1e3, 4), "GB_s": round(alg[j] / kt[j] / 1e9, 1),
-                          "frac": round(alg[j] / kt[j] / 1e9 / peak, 3)} for j in range(nl)}
+                          "frac": round(alg[j] / kt[j] / 1e9 / peak, 3),
+                          "ms_stream_launches": round(kt_stream[j] * 1e3, 4)} for j in range(nl)}
     agg_bytes = sum(alg)
     agg_gbs = agg_bytes / (elapsed / (args.steps * passes)) / 1e9
 
@@ -444,7 +462,7 @@ def run_gpu(args, rank: int, world: int):
             "roofline": {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": peak,
                          "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic_for(names[top]), "alg_bytes_per_launch": alg[top],
-                         "timing": "kernel alone: CUDA events around back-to-back launches of it, mean",
+                         "timing": "kernel alone: CUDA events around a CUDA graph of back-to-back launches of it, mean",
                          "aggregate_GB_s": agg_gbs, "aggregate_frac": agg_gbs / peak},
             "kernels": kernels,
             "e2e": e2e,
