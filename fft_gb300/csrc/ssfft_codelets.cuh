@@ -1020,27 +1020,27 @@ __global__ void __launch_bounds__(THREADS *PER_CTA, MINB) batch(const Args a) {
 
 // ------------------------------------------------------------------ uneven batches: a work-item queue
 
-// One work item: `count` (<= the schedule's transforms per CTA) complex transforms of schedule k,
-// whose element offsets are offs[first .. first + count) of that schedule's table.
-struct QItem {
-	int k;
-	int count;
-	long long first;
-};
-// Per-schedule device tables of a queue kernel.
+// Per-member device tables of a queue kernel.
 struct QSched {
 	const void *tw;          // pass twiddles
 	const void *roots;       // direct-pass roots
-	const long long *offs;   // element offset (in scalars) of every transform of this size
 	long long n;             // complex points per transform
+	long long threads;       // threads per transform
 };
+// The queue of one class launch: item b (CTA b) runs member kidx[b]; thread t of item b works on
+// the transform whose first complex element is toff[b * CTA + t] elements into in and out
+// (-1: none -- a partial item, or threads past the member's transforms per CTA).  Both loads
+// depend on blockIdx and threadIdx only, so a thread issues its first data load one load after
+// it starts.
 struct QueueArgs {
 	const void *in;
 	void *out;
-	const QItem *items;      // the queue, longest transforms first
+	const int *kidx;
+	const int *toff;
 	long long nitems;
 	const QSched *sch;
-	long long pf_dist;       // CTA b prefetches into L2 the inputs of item b + pf_dist (0 = off)
+	long long pf_dist;       // after its first pass, CTA b prefetches into L2 the inputs of item
+	                         // b + pf_dist (0 = off)
 };
 
 // A member schedule of a queue kernel: N points, THREADS threads a transform, SMEM_STRIDE padded
@@ -1048,52 +1048,53 @@ struct QueueArgs {
 template <int N, int THREADS, int SMEM_STRIDE, int EMAX, int... Rs>
 struct QS {};
 
-// Inputs of the item pf_dist ahead, one 128-byte line per thread per step (every address lies
-// inside a transform of that item).
+// Inputs of item pf_dist ahead: thread t takes the 128-byte lines r, r + THREADS, ... of the
+// transform it would work on (r = its index in that transform's threads), so every address lies
+// inside a transform of that item.
 template <typename T, int CTA>
 __device__ __forceinline__ void queue_prefetch(const QueueArgs &a) {
 	if (a.pf_dist <= 0) return;
 	const long long b = (long long)blockIdx.x + a.pf_dist;
 	if (b >= a.nitems) return;
-	const QItem it = a.items[b];
-	const QSched &s = a.sch[it.k];
-	const long long per = 2 * s.n * (long long)sizeof(T);
-	const long long lines = (per + 127) / 128;
-	const unsigned char *in = reinterpret_cast<const unsigned char *>(a.in);
-	for (long long q = threadIdx.x; q < it.count * lines; q += CTA) {
-		const long long g = q / lines;
-		prefetch_l2(in + s.offs[it.first + g] * (long long)sizeof(T) + (q - g * lines) * 128);
-	}
+	const int o = a.toff[b * CTA + threadIdx.x];
+	if (o < 0) return;
+	const QSched &s = a.sch[a.kidx[b]];
+	const long long th = s.threads;
+	const long long lines = (2 * s.n * (long long)sizeof(T) + 127) / 128;
+	const unsigned char *p = reinterpret_cast<const unsigned char *>(a.in) + 2ll * o * (long long)sizeof(T);
+	for (long long q = (long long)threadIdx.x % th; q < lines; q += th) prefetch_l2(p + q * 128);
 }
 
-template <typename T, bool INV, int I, class... Ss>
+template <typename T, bool INV, int CTA, int I, class... Ss>
 struct QDispatch {
-	static __device__ __forceinline__ void run(const QueueArgs &, const QItem &, unsigned char *) {}
+	static __device__ __forceinline__ void run(const QueueArgs &, int, int, unsigned char *) {}
 };
-template <typename T, bool INV, int I, int N, int THREADS, int SMEM_STRIDE, int EMAX, int... Rs, class... Rest>
-struct QDispatch<T, INV, I, QS<N, THREADS, SMEM_STRIDE, EMAX, Rs...>, Rest...> {
-	static __device__ __forceinline__ void run(const QueueArgs &a, const QItem &it, unsigned char *smem) {
-		if (it.k != I) {
-			QDispatch<T, INV, I + 1, Rest...>::run(a, it, smem);
+template <typename T, bool INV, int CTA, int I, int N, int THREADS, int SMEM_STRIDE, int EMAX, int... Rs,
+          class... Rest>
+struct QDispatch<T, INV, CTA, I, QS<N, THREADS, SMEM_STRIDE, EMAX, Rs...>, Rest...> {
+	static __device__ __forceinline__ void run(const QueueArgs &a, int k, int off, unsigned char *smem) {
+		if (k != I) {
+			QDispatch<T, INV, CTA, I + 1, Rest...>::run(a, k, off, smem);
 			return;
 		}
 		using C = typename Cx<T>::C;
-		// transform g of the item: threads [g THREADS, (g + 1) THREADS); threads past the item's
-		// transforms (a partial item, or a CTA wider than PER_CTA * THREADS) only join barriers
+		// transform g of the item: threads [g THREADS, (g + 1) THREADS); threads without one only
+		// join the barriers
 		const int g = threadIdx.x / THREADS;
 		Ctx<T, kComplex, INV, INV> c;
 		c.t = threadIdx.x - g * THREADS;
-		c.valid = g < it.count;
+		c.valid = off >= 0;
 		c.sm = reinterpret_cast<C *>(smem) + g * SMEM_STRIDE;
-		const QSched &s = a.sch[I];
-		const long long o = c.valid ? s.offs[it.first + g] : 0;
+		const long long o = c.valid ? 2ll * off : 0;
 		c.gin = reinterpret_cast<const T *>(a.in) + o;
 		c.gout = reinterpret_cast<T *>(a.out) + o;
 		c.rot = nullptr;
 		c.rtw = nullptr;
 		c.st = nullptr;
+		const QSched &s = a.sch[I];
+		auto pf = [&a] { queue_prefetch<T, CTA>(a); };
 		passes<T, N, THREADS, 1, 0, 0, kGlobal, kGlobal, kComplex, INV, INV, false, EMAX, Rs...>(
-		    c, reinterpret_cast<const C *>(s.tw), reinterpret_cast<const C *>(s.roots));
+		    c, reinterpret_cast<const C *>(s.tw), reinterpret_cast<const C *>(s.roots), pf);
 	}
 };
 
@@ -1104,9 +1105,10 @@ struct QDispatch<T, INV, I, QS<N, THREADS, SMEM_STRIDE, EMAX, Rs...>, Rest...> {
 template <typename T, bool INV, int CTA, int MINB, class... Ss>
 __global__ void __launch_bounds__(CTA, MINB) queue(const QueueArgs a) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	const QItem it = a.items[blockIdx.x];
-	queue_prefetch<T, CTA>(a);
-	QDispatch<T, INV, 0, Ss...>::run(a, it, smem_raw);
+	const long long b = blockIdx.x;
+	const int off = a.toff[b * CTA + threadIdx.x];
+	const int k = a.kidx[b];
+	QDispatch<T, INV, CTA, 0, Ss...>::run(a, k, off, smem_raw);
 }
 
 // ------------------------------------------------------------------ asynchronous staging

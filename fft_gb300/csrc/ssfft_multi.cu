@@ -67,7 +67,8 @@ struct QClass {
 	std::vector<size_t> members;   // indices into MultiPlan::groups
 	std::vector<Schedule> sch;     // member schedules (per_cta = transforms per work item)
 	CUfunction fwd = nullptr, inv = nullptr;
-	ssfft_cl::QItem *d_items = nullptr;
+	const int *d_kidx = nullptr;   // member of each item
+	const int *d_toff = nullptr;   // item x thread: transform offset in complex elements (-1: none)
 	ssfft_cl::QSched *d_sch = nullptr;
 	long long nitems = 0;
 	long long pf_dist = 0;
@@ -126,7 +127,8 @@ struct MultiPlan {
 			std::memset(&a, 0, sizeof a);
 			a.in = in;
 			a.out = out;
-			a.items = c.d_items;
+			a.kidx = c.d_kidx;
+			a.toff = c.d_toff;
 			a.nitems = c.nitems;
 			a.sch = c.d_sch;
 			a.pf_dist = c.pf_dist;
@@ -172,7 +174,7 @@ struct MultiPlan {
 		return SSFFT_SUCCESS;
 	}
 
-	ssfft_status build_queue();
+	ssfft_status build_queue(const std::vector<std::vector<long long>> &elem_offs);
 };
 
 // Queue schedule of one size: the planner's schedule (no staged or tensor-core variant), its
@@ -258,24 +260,45 @@ static ssfft_status form_classes(ssfft_dtype dtype, const std::vector<std::tuple
 	return SSFFT_SUCCESS;
 }
 
+// One work item of a class: `count` transforms of member k, its transforms first .. first+count-1.
+struct QueueItem {
+	int k, count;
+	size_t first;
+};
+
 // The work items of one class, in queue order: member by member (longest first), each member's
 // transforms in groups of its transforms per CTA.
-static void class_items(const QClass &c, const std::vector<size_t> &counts, std::vector<ssfft_cl::QItem> &items) {
+static void class_items(const QClass &c, const std::vector<size_t> &counts, std::vector<QueueItem> &items) {
 	items.clear();
 	for (size_t k = 0; k < c.sch.size(); ++k) {
 		const size_t cnt = counts[c.members[k]];
 		const int per = c.sch[k].per_cta;
-		for (size_t f = 0; f < cnt; f += (size_t)per) {
-			ssfft_cl::QItem it;
-			it.k = (int)k;
-			it.count = (int)std::min<size_t>((size_t)per, cnt - f);
-			it.first = (long long)f;
-			items.push_back(it);
+		for (size_t f = 0; f < cnt; f += (size_t)per)
+			items.push_back(QueueItem{(int)k, (int)std::min<size_t>((size_t)per, cnt - f), f});
+	}
+}
+
+// The device tables of a class queue: kidx[b] = member of item b; toff[b * cta + t] = offset, in
+// complex elements, of the transform thread t of item b works on (-1: none).  elem_offs[m] lists
+// the element offsets of member-size m's transforms (indexed like `counts`).
+static void class_tables(const QClass &c, const std::vector<QueueItem> &items,
+                         const std::vector<std::vector<long long>> &elem_offs, std::vector<int> &kidx,
+                         std::vector<int> &toff) {
+	kidx.resize(items.size());
+	toff.assign(items.size() * (size_t)c.cta, -1);
+	for (size_t b = 0; b < items.size(); ++b) {
+		const QueueItem &it = items[b];
+		kidx[b] = it.k;
+		const int th = c.sch[it.k].threads;
+		const std::vector<long long> &offs = elem_offs[c.members[it.k]];
+		for (int t = 0; t < c.cta; ++t) {
+			const int g = t / th;
+			if (g < it.count) toff[b * (size_t)c.cta + t] = (int)offs[it.first + (size_t)g];
 		}
 	}
 }
 
-ssfft_status MultiPlan::build_queue() {
+ssfft_status MultiPlan::build_queue(const std::vector<std::vector<long long>> &elem_offs) {
 	std::vector<std::tuple<size_t, size_t, double>> sizes;
 	std::vector<size_t> counts;
 	for (const Group &g : groups) {
@@ -309,24 +332,29 @@ ssfft_status MultiPlan::build_queue() {
 		});
 	for (auto &x : th) x.join();
 	if (bad) return SSFFT_ERR_CUDA;
-	// device layout: per class its items and member records; then every member's tables
-	std::vector<std::vector<ssfft_cl::QItem>> items(classes.size());
+	// device layout: per class its member indices, per-thread offsets and member records; then
+	// every member's tables
+	std::vector<std::vector<int>> kidx(classes.size()), toff(classes.size());
 	std::vector<std::vector<double>> tw_all, roots_all;
 	size_t off = 0;
-	std::vector<size_t> off_items(classes.size()), off_sch(classes.size());
+	std::vector<size_t> off_kidx(classes.size()), off_toff(classes.size()), off_sch(classes.size());
 	for (size_t ci = 0; ci < classes.size(); ++ci) {
 		QClass &c = classes[ci];
-		class_items(c, counts, items[ci]);
+		std::vector<QueueItem> items;
+		class_items(c, counts, items);
+		class_tables(c, items, elem_offs, kidx[ci], toff[ci]);
 		for (size_t k = 0; k < c.sch.size(); ++k) {
 			std::vector<double> tw, roots;
 			schedule_twiddles(c.sch[k], tw, roots);
 			tw_all.push_back(tw);
 			roots_all.push_back(roots);
 		}
-		c.nitems = (long long)items[ci].size();
+		c.nitems = (long long)items.size();
 		if (c.nitems > 0x7fffffffLL) return SSFFT_ERR_INVALID_SIZE;
-		off_items[ci] = off;
-		off = qalign(off + items[ci].size() * sizeof(ssfft_cl::QItem));
+		off_kidx[ci] = off;
+		off = qalign(off + kidx[ci].size() * sizeof(int));
+		off_toff[ci] = off;
+		off = qalign(off + toff[ci].size() * sizeof(int));
 		off_sch[ci] = off;
 		off = qalign(off + c.sch.size() * sizeof(ssfft_cl::QSched));
 	}
@@ -346,13 +374,14 @@ ssfft_status MultiPlan::build_queue() {
 	size_t mi = 0;
 	for (size_t ci = 0; ci < classes.size(); ++ci) {
 		QClass &c = classes[ci];
-		std::memcpy(blob.data() + off_items[ci], items[ci].data(), items[ci].size() * sizeof(ssfft_cl::QItem));
+		std::memcpy(blob.data() + off_kidx[ci], kidx[ci].data(), kidx[ci].size() * sizeof(int));
+		std::memcpy(blob.data() + off_toff[ci], toff[ci].data(), toff[ci].size() * sizeof(int));
 		std::vector<ssfft_cl::QSched> recs(c.sch.size());
 		for (size_t k = 0; k < c.sch.size(); ++k, ++mi) {
 			recs[k].tw = base + off_tw[mi];
 			recs[k].roots = base + off_roots[mi];
-			recs[k].offs = groups[c.members[k]].d_offs;
 			recs[k].n = (long long)c.sch[k].n;
+			recs[k].threads = (long long)c.sch[k].threads;
 			for (size_t i = 0; i < tw_all[mi].size(); ++i) {
 				if (sb == 4) reinterpret_cast<float *>(blob.data() + off_tw[mi])[i] = (float)tw_all[mi][i];
 				else reinterpret_cast<double *>(blob.data() + off_tw[mi])[i] = tw_all[mi][i];
@@ -363,7 +392,8 @@ ssfft_status MultiPlan::build_queue() {
 			}
 		}
 		std::memcpy(blob.data() + off_sch[ci], recs.data(), recs.size() * sizeof(ssfft_cl::QSched));
-		c.d_items = reinterpret_cast<ssfft_cl::QItem *>(base + off_items[ci]);
+		c.d_kidx = reinterpret_cast<const int *>(base + off_kidx[ci]);
+		c.d_toff = reinterpret_cast<const int *>(base + off_toff[ci]);
 		c.d_sch = reinterpret_cast<ssfft_cl::QSched *>(base + off_sch[ci]);
 		// L2 prefetch one wave of resident CTAs ahead, as the batch kernel does
 		int sms = 0;
@@ -466,10 +496,18 @@ ssfft_status ssfft_multi_create_ex(ssfft_multi_t *out, const size_t *sizes, size
 	for (size_t i : order) sorted.push_back(m->groups[i]);
 	m->groups.swap(sorted);
 	// the work-item queue (default), except for the tensor-core precision option (per-size
-	// tcgen05 kernels) and the debug switch multi_mode=1 (per-size launches)
-	m->queue_mode = debug_knob("multi_mode", 0) != 1 && !(opt && opt->precision == SSFFT_PRECISION_SPLIT_BF16);
+	// tcgen05 kernels), the debug switch multi_mode=1 (per-size launches) and batches of 2^31
+	// complex elements or more (the queue's offsets are 32-bit element counts)
+	m->queue_mode = debug_knob("multi_mode", 0) != 1 && !(opt && opt->precision == SSFFT_PRECISION_SPLIT_BF16) &&
+	                m->total < ((size_t)1 << 31);
 	if (m->queue_mode) {
-		ssfft_status st = m->build_queue();
+		std::vector<std::vector<long long>> elem_offs;
+		for (const Group &g : m->groups) {
+			std::vector<long long> v;
+			for (long long sc : by_size[g.n]) v.push_back(sc / 2);
+			elem_offs.push_back(std::move(v));
+		}
+		ssfft_status st = m->build_queue(elem_offs);
 		if (st != SSFFT_SUCCESS) return st;
 		// one graph branch per class, largest class first
 		m->branches = (int)std::min<size_t>(kMaxBranches, std::max<size_t>(1, m->classes.size()));
@@ -575,16 +613,33 @@ extern "C" ssfft_status ssfft_diag_multi_spec(const size_t *sizes, size_t count,
 	if (st != SSFFT_SUCCESS) return st;
 	std::vector<size_t> counts;
 	for (auto &x : g) counts.push_back(std::get<1>(x));
-	std::string js = "{\"classes\": [";
+	// element offsets of every size's transforms, in list order (the caller's layout)
+	std::vector<std::vector<long long>> elem_offs(g.size());
+	{
+		std::map<size_t, size_t> gi;
+		for (size_t i = 0; i < g.size(); ++i) gi[std::get<0>(g[i])] = i;
+		long long off = 0;
+		for (size_t i = 0; i < count; ++i) {
+			elem_offs[gi[sizes[i]]].push_back(off);
+			off += (long long)sizes[i];
+		}
+		if (off >= (1ll << 31)) return SSFFT_ERR_UNSUPPORTED;
+	}
+	// blob: FP64 tables of every member, then per class the int32 member indices and per-thread
+	// offsets (8-byte aligned)
 	std::vector<double> tab;
+	std::string js = "{\"classes\": [";
+	std::vector<std::vector<int>> kidx(classes.size()), toff(classes.size());
 	for (size_t ci = 0; ci < classes.size(); ++ci) {
 		const QClass &c = classes[ci];
-		std::vector<ssfft_cl::QItem> items;
+		std::vector<QueueItem> items;
 		class_items(c, counts, items);
+		class_tables(c, items, elem_offs, kidx[ci], toff[ci]);
 		js += ci ? ", " : "";
 		js += "{\"fwd\": \"" + c.name(false) + "\", \"inv\": \"" + c.name(true) + "\", \"cta\": " + std::to_string(c.cta) +
 		      ", \"smem\": " + std::to_string(c.smem) + ", \"minb\": " + std::to_string(c.minb) +
-		      ", \"emax\": " + std::to_string(c.emax) + ", \"members\": [";
+		      ", \"emax\": " + std::to_string(c.emax) + ", \"nitems\": " + std::to_string(items.size()) +
+		      ", \"members\": [";
 		for (size_t k = 0; k < c.sch.size(); ++k) {
 			std::vector<double> tw, roots;
 			schedule_twiddles(c.sch[k], tw, roots);
@@ -602,10 +657,31 @@ extern "C" ssfft_status ssfft_diag_multi_spec(const size_t *sizes, size_t count,
 			      std::to_string(items[i].first) + "]";
 		js += "]}";
 	}
-	js += "]}";
+	size_t pos = tab.size() * sizeof(double);
+	std::string tjs = ", \"tables\": [";
+	for (size_t ci = 0; ci < classes.size(); ++ci) {
+		tjs += (ci ? ", [" : "[") + std::to_string(pos) + ", ";
+		pos += kidx[ci].size() * sizeof(int);
+		pos = (pos + 7) / 8 * 8;
+		tjs += std::to_string(pos) + "]";
+		pos += toff[ci].size() * sizeof(int);
+		pos = (pos + 7) / 8 * 8;
+	}
+	js += "]" + tjs + "]}";
 	if (blob_bytes) {
-		if (blob) std::memcpy(blob, tab.data(), std::min(*blob_bytes, tab.size() * sizeof(double)));
-		*blob_bytes = tab.size() * sizeof(double);
+		if (blob && *blob_bytes >= pos) {
+			unsigned char *b = static_cast<unsigned char *>(blob);
+			std::memset(b, 0, pos);
+			std::memcpy(b, tab.data(), tab.size() * sizeof(double));
+			size_t q = tab.size() * sizeof(double);
+			for (size_t ci = 0; ci < classes.size(); ++ci) {
+				std::memcpy(b + q, kidx[ci].data(), kidx[ci].size() * sizeof(int));
+				q = (q + kidx[ci].size() * sizeof(int) + 7) / 8 * 8;
+				std::memcpy(b + q, toff[ci].data(), toff[ci].size() * sizeof(int));
+				q = (q + toff[ci].size() * sizeof(int) + 7) / 8 * 8;
+			}
+		}
+		*blob_bytes = pos;
 	}
 	if (json && json_len) {
 		if (js.size() + 1 > json_len) return SSFFT_ERR_INVALID_SIZE;

@@ -289,8 +289,10 @@ ssfft_status ssfft_diag_large_spec(size_t n, ssfft_dtype dtype, ssfft_kind kind,
                                    void *blob, size_t *blob_bytes);
 /* The work-item queue an uneven list runs as (host only, no GPU): `json` receives its classes
  * (kernel names, CTA threads, shared memory, member sizes with their transforms per item and
- * the offsets of their FP64 tables in `blob`, and the items [member, count, first] in queue
- * order); `blob` the FP64 pass twiddles and roots (NULL: only *blob_bytes is set).
+ * the offsets of their FP64 tables in `blob`, the items [member, count, first] in queue order,
+ * and per class the byte offsets in `blob` of its int32 tables: the member of each item and, per
+ * item and thread, the element offset of the transform that thread works on, -1 for none);
+ * `blob` the FP64 pass twiddles and roots, then those tables (NULL: only *blob_bytes is set).
  * ssfft_diag_multi_jit_check compiles the class kernels for `arch`.  No reference counterpart. */
 ssfft_status ssfft_diag_multi_spec(const size_t *sizes, size_t count, ssfft_dtype dtype, char *json, size_t json_len,
                                    void *blob, size_t *blob_bytes);

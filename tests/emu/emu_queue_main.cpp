@@ -1,10 +1,10 @@
 // tests/emu/emu_queue_main.cpp -- runs one emulated launch of an uneven-batch queue kernel
 // (ssfft_cl::queue).  Compiled together with a generated case table (emu_queue_cases.inc:
-// `{&ssfft_cl::queue<...>, cta_threads, smem_bytes},` lines).
-// argv: case index, items file (QItem records), members file (int64 per member: n, tw offset,
-//       roots offset, offset-table offset, in elements of the tables / offsets files), tables
-//       file (the kernel's dtype), offsets file (int64), input file, output file (pre-filled;
-//       rewritten), prefetch distance (items ahead).
+// `{&ssfft_cl::queue<...>, cta_threads, smem_bytes, scalar_bytes},` lines).
+// argv: case index, member-index file (int32 per item), thread-offset file (int32 per item and
+//       thread), members file (int64 per member: n, tw offset, roots offset, threads per
+//       transform; offsets in elements of the tables file), tables file (the kernel's dtype),
+//       input file, output file (pre-filled; rewritten), prefetch distance (items ahead).
 #include "cuda_emu.h"
 #include "ssfft_codelets.cuh"
 
@@ -40,7 +40,7 @@ static std::vector<char> slurp(const char *path) {
 int main(int argc, char **argv) {
 	if (argc != 9) return 2;
 	const QCase &c = kCases[std::atoi(argv[1])];
-	std::vector<char> items = slurp(argv[2]), members = slurp(argv[3]), tab = slurp(argv[4]), offs = slurp(argv[5]),
+	std::vector<char> kidx = slurp(argv[2]), toff = slurp(argv[3]), members = slurp(argv[4]), tab = slurp(argv[5]),
 	                  in = slurp(argv[6]), out = slurp(argv[7]);
 	const long long *mem = reinterpret_cast<const long long *>(members.data());
 	const size_t nm = members.size() / (4 * sizeof(long long));
@@ -49,13 +49,15 @@ int main(int argc, char **argv) {
 		sch[k].n = mem[4 * k];
 		sch[k].tw = tab.data() + mem[4 * k + 1] * c.scalar_bytes;
 		sch[k].roots = tab.data() + mem[4 * k + 2] * c.scalar_bytes;
-		sch[k].offs = reinterpret_cast<const long long *>(offs.data()) + mem[4 * k + 3];
+		sch[k].threads = mem[4 * k + 3];
 	}
 	ssfft_cl::QueueArgs a{};
 	a.in = in.data();
 	a.out = out.data();
-	a.items = reinterpret_cast<const ssfft_cl::QItem *>(items.data());
-	a.nitems = (long long)(items.size() / sizeof(ssfft_cl::QItem));
+	a.kidx = reinterpret_cast<const int *>(kidx.data());
+	a.toff = reinterpret_cast<const int *>(toff.data());
+	a.nitems = (long long)(kidx.size() / sizeof(int));
+	if (toff.size() != (size_t)a.nitems * (size_t)c.cta_threads * sizeof(int)) return 6;
 	a.sch = sch.data();
 	a.pf_dist = std::atoll(argv[8]);
 	if (c.smem > sizeof(ssfft_cl::smem_raw)) return 5;

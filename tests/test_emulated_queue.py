@@ -24,7 +24,6 @@ CASES = {
             (2048, 2), (3840, 1), (4096, 2), (3645, 1), (6561, 1), (8192, 1), (12288, 1), (15552, 1), (16384, 1)],
     "f64": [(64, 10), (96, 7), (243, 2), (1024, 3), (2187, 1), (4096, 1), (8192, 1)],
 }
-QITEM = np.dtype([("k", "<i4"), ("count", "<i4"), ("first", "<i8")])
 
 
 def spec_of(sizes, dt):
@@ -38,7 +37,7 @@ def spec_of(sizes, dt):
     nb = ctypes.c_size_t()
     code = 0 if dt == "f32" else 1
     assert l.ssfft_diag_multi_spec(arr, len(sizes), code, buf, 1 << 22, None, ctypes.byref(nb)) == 0
-    blob = np.zeros(nb.value // 8, dtype=np.float64)
+    blob = np.zeros(nb.value, dtype=np.uint8)
     assert l.ssfft_diag_multi_spec(arr, len(sizes), code, None, 0, blob.ctypes.data, ctypes.byref(nb)) == 0
     return json.loads(buf.value.decode()), blob
 
@@ -114,7 +113,8 @@ def test_emulated_queue_kernels_match_oracle(emulator, dt, inv):
     by_size = {}
     for i, n in enumerate(sizes):
         by_size.setdefault(n, []).append(2 * int(starts[i]))  # scalar offsets, in list order
-    tables = blob.astype(sdt)
+    ntab = spec["tables"][0][0] // 8 if spec["tables"] else 0
+    tables = blob[:ntab * 8].view(np.float64).astype(sdt)
     sentinel = np.array(complex(3.0, -7.0), dtype=cdt)
     (d / "tab.bin").write_bytes(tables.tobytes())
     (d / "in.bin").write_bytes(x.tobytes())
@@ -122,17 +122,28 @@ def test_emulated_queue_kernels_match_oracle(emulator, dt, inv):
     tol = 1e-6 if dt == "f32" else 1e-13
     worst = 0.0
     for ci, c in enumerate(spec["classes"]):
-        offs, mem = [], []
+        mem = []
         for m in c["members"]:
-            mem += [m["n"], m["tw"][0], m["roots"][0], len(offs)]
-            offs += by_size[m["n"]]
-        items = np.array([tuple(it) for it in c["items"]], dtype=QITEM)
-        (d / "items.bin").write_bytes(items.tobytes())
+            mem += [m["n"], m["tw"][0], m["roots"][0], m["threads"]]
+        ok, ot = spec["tables"][ci]
+        nit = c["nitems"]
+        kidx = blob[ok:ok + 4 * nit].view(np.int32)
+        toff = blob[ot:ot + 4 * nit * c["cta"]].view(np.int32).reshape(nit, c["cta"])
+        # the tables are the items: item b runs member k on its transforms first.., one thread group each
+        for b, (k, cnt, first) in enumerate(c["items"]):
+            assert kidx[b] == k
+            th = c["members"][k]["threads"]
+            n = c["members"][k]["n"]
+            for t in range(c["cta"]):
+                g = t // th
+                want = by_size[n][first + g] // 2 if g < cnt else -1
+                assert toff[b, t] == want, (ci, b, t)
+        (d / "kidx.bin").write_bytes(kidx.tobytes())
+        (d / "toff.bin").write_bytes(toff.tobytes())
         (d / "mem.bin").write_bytes(np.array(mem, dtype=np.int64).tobytes())
-        (d / "offs.bin").write_bytes(np.array(offs, dtype=np.int64).tobytes())
         (d / "out.bin").write_bytes(np.full(total, sentinel).tobytes())
-        r = subprocess.run([str(exe), str(index[(dt, ci, inv)]), str(d / "items.bin"), str(d / "mem.bin"),
-                            str(d / "tab.bin"), str(d / "offs.bin"), str(d / "in.bin"), str(d / "out.bin"), "3"],
+        r = subprocess.run([str(exe), str(index[(dt, ci, inv)]), str(d / "kidx.bin"), str(d / "toff.bin"),
+                            str(d / "mem.bin"), str(d / "tab.bin"), str(d / "in.bin"), str(d / "out.bin"), "3"],
                            capture_output=True, text=True, timeout=900)
         assert r.returncode == 0, r.stderr[-2000:]
         y = np.frombuffer((d / "out.bin").read_bytes(), dtype=cdt)
