@@ -9,8 +9,9 @@
 //     group's contiguous device block, runs one batched launch per group, and copies outputs back;
 //   * up to max_waves_in_flight waves run at once, so requests arriving while earlier ones are on
 //     the GPU are admitted as soon as buffers and a wave slot free up;
-//   * a host callback at the end of each wave's stream work marks its requests complete (the
-//     latency of a request is completion time minus submit time) and releases its buffers.
+//   * an event recorded after each wave's stream work is polled by a completion thread, which
+//     marks the wave's requests complete (the latency of a request is completion time minus
+//     submit time) and releases its buffers.
 // Requests whose host buffers are page-locked and mapped (cudaHostAlloc / cudaHostRegister; the
 // GPU reaches them over the host link) and whose shape runs in one CTA are served in place: the
 // wave uploads one table of every transform's input and output offsets, and one launch per
@@ -195,6 +196,15 @@ struct ServerImpl {
 	std::mutex plan_mu;
 	std::map<ShapeKey, ssfft_plan_t> plans;
 	std::thread worker;
+	// completion: an event per wave slot, polled by the completion thread while waves are in flight
+	// (lower latency than a host-function callback; debug switch serve_hostfunc=1 uses callbacks)
+	bool hostfunc = false;
+	std::vector<cudaEvent_t> slot_event;
+	std::mutex fly_mu;
+	std::condition_variable fly_cv;
+	std::deque<Wave *> in_flight;
+	bool fly_stop = false;
+	std::thread completer;
 
 	// Plan of a request shape; multi-pass shapes get one plan per wave slot so that concurrent
 	// waves never share scratch.  Compiles outside the lock so shapes build concurrently.
@@ -342,11 +352,58 @@ struct ServerImpl {
 				pos_out += q->out_bytes;
 			}
 		}
+		if (!hostfunc) {
+			if (cudaEventRecord(slot_event[w->slot], s) != cudaSuccess) {
+				cudaStreamSynchronize(s);
+				w->failed = true;
+				on_wave_done(w);
+				return;
+			}
+			{
+				std::lock_guard<std::mutex> lock(fly_mu);
+				in_flight.push_back(w);
+			}
+			fly_cv.notify_one();
+			return;
+		}
 		if (cudaLaunchHostFunc(s, on_wave_done, w) != cudaSuccess) {
 			// no callback will come: complete synchronously
 			cudaStreamSynchronize(s);
 			w->failed = true;
 			on_wave_done(w);
+		}
+	}
+
+	// Completion thread: polls the events of the waves in flight (in any order; a slot's event was
+	// recorded after its wave's last copy or launch) and completes each wave whose work is done;
+	// sleeps when nothing is in flight.
+	void complete_loop() {
+		cudaSetDevice(device);
+		std::vector<Wave *> mine;
+		for (;;) {
+			{
+				std::unique_lock<std::mutex> lock(fly_mu);
+				if (mine.empty()) fly_cv.wait(lock, [this] { return fly_stop || !in_flight.empty(); });
+				while (!in_flight.empty()) {
+					mine.push_back(in_flight.front());
+					in_flight.pop_front();
+				}
+				if (fly_stop && mine.empty()) return;
+			}
+			bool progress = false;
+			for (size_t i = 0; i < mine.size();) {
+				const cudaError_t e = cudaEventQuery(slot_event[mine[i]->slot]);
+				if (e == cudaErrorNotReady) {
+					++i;
+					continue;
+				}
+				Wave *w = mine[i];
+				if (e != cudaSuccess) w->failed = true;
+				mine.erase(mine.begin() + (long)i);
+				on_wave_done(w);
+				progress = true;
+			}
+			if (!progress) std::this_thread::yield();
 		}
 	}
 
@@ -535,7 +592,24 @@ ssfft_status ssfft_server_create(ssfft_server_t *out, const ssfft_server_config 
 			s->d_tab.push_back(static_cast<long long *>(d));
 		}
 	}
+	s->hostfunc = debug_knob("serve_hostfunc", 0) == 1;
+	for (int i = 0; i < nstreams; ++i) {
+		cudaEvent_t ev = nullptr;
+		e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+		if (e != cudaSuccess) {
+			for (auto x : s->slot_event) cudaEventDestroy(x);
+			for (size_t k = 0; k < s->h_tab.size(); ++k) {
+				cudaFreeHost(s->h_tab[k]);
+				cudaFree(s->d_tab[k]);
+			}
+			for (auto x : s->streams) cudaStreamDestroy(x);
+			cudaFree(base);
+			return cuda_fail(e, "server events");
+		}
+		s->slot_event.push_back(ev);
+	}
 	ServerImpl *raw = s.get();
+	s->completer = std::thread([raw] { raw->complete_loop(); });
 	s->worker = std::thread([raw] { raw->loop(); });
 	*out = reinterpret_cast<ssfft_server_t>(s.release());
 	return SSFFT_SUCCESS;
@@ -675,10 +749,17 @@ ssfft_status ssfft_server_destroy(ssfft_server_t srv) {
 		}
 		std::this_thread::sleep_for(std::chrono::milliseconds(10));
 	}
+	{
+		std::lock_guard<std::mutex> lock(s->fly_mu);
+		s->fly_stop = true;
+	}
+	s->fly_cv.notify_all();
+	if (s->completer.joinable()) s->completer.join();
 	for (auto st : s->streams) {
 		cudaStreamSynchronize(st);
 		cudaStreamDestroy(st);
 	}
+	for (auto ev : s->slot_event) cudaEventDestroy(ev);
 	for (auto &kv : s->plans) ssfft_plan_destroy(kv.second);
 	for (size_t k = 0; k < s->h_tab.size(); ++k) {
 		cudaFreeHost(s->h_tab[k]);

@@ -156,3 +156,25 @@ def test_plain_server_never_in_place(F):
     assert plain.stats()["in_place"] == 0
     assert rel_l2(po, expected(x, 480, "real", False)) <= 1e-6
     plain.close()
+
+
+def test_completion_by_callbacks_matches(F, monkeypatch):
+    """Waves complete through a polling completion thread; the callback form kept behind the
+    debug switch serve_hostfunc=1 gives the same results."""
+    rng = np.random.default_rng(19)
+    monkeypatch.setenv("SSFFT_DEBUG", "serve_hostfunc=1")
+    cb = F.Server(hbm_budget_bytes=128 << 20, waves=2)
+    monkeypatch.delenv("SSFFT_DEBUG")
+    poll = F.Server(hbm_budget_bytes=128 << 20, waves=2)
+    for i in range(8):
+        n, kind = SHAPES[i % len(SHAPES)]
+        x, o1 = make_request(rng, n, kind, bool(i % 2), 2)
+        o2 = np.empty_like(o1)
+        t1 = cb.submit(n, kind, bool(i % 2), x, o1, frames=2)
+        t2 = poll.submit(n, kind, bool(i % 2), x, o2, frames=2)
+        cb.wait(t1)
+        poll.wait(t2)
+        assert np.array_equal(o1, o2)
+    assert cb.stats()["failed"] == 0 and poll.stats()["failed"] == 0
+    cb.close()
+    poll.close()
