@@ -42,6 +42,7 @@ namespace {
 constexpr int kMaxBranches = 32;
 constexpr int kQueueBucket = 128;     // queue CTAs: threads rounded up to a multiple of this
 constexpr size_t kQueueMembers = 16;  // sizes per queue kernel at most
+constexpr size_t kQueueMaxN = 4096;   // longest size run by a queue class (longer: own launch)
 
 struct Group {
 	size_t n = 0, count = 0;
@@ -103,7 +104,9 @@ struct MultiPlan {
 	std::mutex mu;
 	std::map<GraphKey, cudaGraphExec_t> graphs;
 	bool queue_mode = true;        // work-item queue kernels (false: one launch per size)
-	std::vector<QClass> classes;   // queue mode
+	std::vector<QClass> classes;   // queue mode: sizes up to queue_max_n
+	std::vector<size_t> big;       // queue mode: groups above queue_max_n, one launch per size
+	size_t queue_max_n = 0;
 	void *d_queue = nullptr;       // queue mode: items, per-schedule records and twiddle tables
 
 	~MultiPlan() {
@@ -134,6 +137,12 @@ struct MultiPlan {
 			a.pf_dist = c.pf_dist;
 			ssfft_status st = jit_launch(inverse ? c.inv : c.fwd, (unsigned)c.nitems, (unsigned)c.cta, c.smem,
 			                             streams[c.branch], &a);
+			if (st != SSFFT_SUCCESS) return st;
+		}
+		for (size_t gi : big) {
+			const Group &g = groups[gi];
+			ssfft_status st = launch_batch_offs(reinterpret_cast<const Plan *>(g.plan), inverse, in, out, g.count,
+			                                    g.d_offs, streams[g.branch]);
 			if (st != SSFFT_SUCCESS) return st;
 		}
 		return SSFFT_SUCCESS;
@@ -298,12 +307,22 @@ static void class_tables(const QClass &c, const std::vector<QueueItem> &items,
 	}
 }
 
-ssfft_status MultiPlan::build_queue(const std::vector<std::vector<long long>> &elem_offs) {
+ssfft_status MultiPlan::build_queue(const std::vector<std::vector<long long>> &group_offs) {
+	// sizes up to queue_max_n go into queue classes; longer ones keep their own launch (a class
+	// kernel holding several long fully unrolled transforms thrashes the instruction cache)
 	std::vector<std::tuple<size_t, size_t, double>> sizes;
 	std::vector<size_t> counts;
-	for (const Group &g : groups) {
+	std::vector<std::vector<long long>> elem_offs;
+	big.clear();
+	for (size_t gi = 0; gi < groups.size(); ++gi) {
+		const Group &g = groups[gi];
+		if (g.n > queue_max_n) {
+			big.push_back(gi);
+			continue;
+		}
 		sizes.emplace_back(g.n, g.count, g.work);
 		counts.push_back(g.count);
+		elem_offs.push_back(group_offs[gi]);
 	}
 	ssfft_status fst = form_classes(dtype, sizes, classes);
 	if (fst != SSFFT_SUCCESS) return fst;
@@ -501,6 +520,7 @@ ssfft_status ssfft_multi_create_ex(ssfft_multi_t *out, const size_t *sizes, size
 	m->queue_mode = debug_knob("multi_mode", 0) != 1 && !(opt && opt->precision == SSFFT_PRECISION_SPLIT_BF16) &&
 	                m->total < ((size_t)1 << 31);
 	if (m->queue_mode) {
+		m->queue_max_n = (size_t)std::max(0ll, debug_knob("queue_max_n", (long long)kQueueMaxN));
 		std::vector<std::vector<long long>> elem_offs;
 		for (const Group &g : m->groups) {
 			std::vector<long long> v;
@@ -509,9 +529,22 @@ ssfft_status ssfft_multi_create_ex(ssfft_multi_t *out, const size_t *sizes, size
 		}
 		ssfft_status st = m->build_queue(elem_offs);
 		if (st != SSFFT_SUCCESS) return st;
-		// one graph branch per class, largest class first
-		m->branches = (int)std::min<size_t>(kMaxBranches, std::max<size_t>(1, m->classes.size()));
-		for (size_t i = 0; i < m->classes.size(); ++i) m->classes[i].branch = (int)(i % (size_t)m->branches);
+		// graph branches: the class launches and the long sizes' launches, largest work first, each on
+		// the least loaded of up to 32 branches
+		std::vector<std::pair<double, long long>> jobs;  // (work, class index or -1 - group index)
+		for (size_t i = 0; i < m->classes.size(); ++i) jobs.emplace_back(m->classes[i].work, (long long)i);
+		for (size_t gi : m->big) jobs.emplace_back(m->groups[gi].work, -1 - (long long)gi);
+		std::stable_sort(jobs.begin(), jobs.end(), [](const auto &a, const auto &b) { return a.first > b.first; });
+		m->branches = (int)std::min<size_t>(kMaxBranches, std::max<size_t>(1, jobs.size()));
+		double bload[kMaxBranches] = {};
+		for (const auto &j : jobs) {
+			int bb = 0;
+			for (int q = 1; q < m->branches; ++q)
+				if (bload[q] < bload[bb]) bb = q;
+			bload[bb] += j.first;
+			if (j.second >= 0) m->classes[(size_t)j.second].branch = bb;
+			else m->groups[(size_t)(-1 - j.second)].branch = bb;
+		}
 	}
 	const int nbr = m->branches;
 	e = cudaStreamCreateWithFlags(&m->cap, cudaStreamNonBlocking);
@@ -567,7 +600,7 @@ ssfft_status ssfft_multi_info(ssfft_multi_t multi, size_t *distinct_sizes, size_
 size_t ssfft_multi_launches(ssfft_multi_t multi) {
 	if (!multi) return 0;
 	const MultiPlan *m = reinterpret_cast<const MultiPlan *>(multi);
-	return m->queue_mode ? m->classes.size() : m->groups.size();
+	return m->queue_mode ? m->classes.size() + m->big.size() : m->groups.size();
 }
 
 ssfft_status ssfft_multi_destroy(ssfft_multi_t multi) {
@@ -605,9 +638,17 @@ ssfft_status multi_groups(const size_t *sizes, size_t count, ssfft_dtype dtype,
 
 extern "C" ssfft_status ssfft_diag_multi_spec(const size_t *sizes, size_t count, ssfft_dtype dtype, char *json,
                                               size_t json_len, void *blob, size_t *blob_bytes) {
-	std::vector<std::tuple<size_t, size_t, double>> g;
-	ssfft_status st = multi_groups(sizes, count, dtype, g);
+	std::vector<std::tuple<size_t, size_t, double>> g0, g;
+	ssfft_status st = multi_groups(sizes, count, dtype, g0);
 	if (st != SSFFT_SUCCESS) return st;
+	// sizes above queue_max_n run as their own launches (as ssfft_multi_create does)
+	const size_t qmax = (size_t)std::max(0ll, debug_knob("queue_max_n", (long long)kQueueMaxN));
+	std::string own = "[";
+	for (auto &x : g0) {
+		if (std::get<0>(x) <= qmax) g.push_back(x);
+		else own += (own.size() > 1 ? ", " : "") + std::to_string(std::get<0>(x));
+	}
+	own += "]";
 	std::vector<QClass> classes;
 	st = form_classes(dtype, g, classes);
 	if (st != SSFFT_SUCCESS) return st;
@@ -620,7 +661,8 @@ extern "C" ssfft_status ssfft_diag_multi_spec(const size_t *sizes, size_t count,
 		for (size_t i = 0; i < g.size(); ++i) gi[std::get<0>(g[i])] = i;
 		long long off = 0;
 		for (size_t i = 0; i < count; ++i) {
-			elem_offs[gi[sizes[i]]].push_back(off);
+			auto it = gi.find(sizes[i]);
+			if (it != gi.end()) elem_offs[it->second].push_back(off);
 			off += (long long)sizes[i];
 		}
 		if (off >= (1ll << 31)) return SSFFT_ERR_UNSUPPORTED;
@@ -667,7 +709,7 @@ extern "C" ssfft_status ssfft_diag_multi_spec(const size_t *sizes, size_t count,
 		pos += toff[ci].size() * sizeof(int);
 		pos = (pos + 7) / 8 * 8;
 	}
-	js += "]" + tjs + "]}";
+	js += "]" + tjs + "], \"own_launch\": " + own + "}";
 	if (blob_bytes) {
 		if (blob && *blob_bytes >= pos) {
 			unsigned char *b = static_cast<unsigned char *>(blob);
@@ -692,9 +734,12 @@ extern "C" ssfft_status ssfft_diag_multi_spec(const size_t *sizes, size_t count,
 
 extern "C" ssfft_status ssfft_diag_multi_jit_check(const size_t *sizes, size_t count, ssfft_dtype dtype,
                                                    const char *arch, size_t *image_bytes) {
-	std::vector<std::tuple<size_t, size_t, double>> g;
-	ssfft_status st = multi_groups(sizes, count, dtype, g);
+	std::vector<std::tuple<size_t, size_t, double>> g0, g;
+	ssfft_status st = multi_groups(sizes, count, dtype, g0);
 	if (st != SSFFT_SUCCESS) return st;
+	const size_t qmax = (size_t)std::max(0ll, debug_knob("queue_max_n", (long long)kQueueMaxN));
+	for (auto &x : g0)
+		if (std::get<0>(x) <= qmax) g.push_back(x);
 	std::vector<QClass> classes;
 	st = form_classes(dtype, g, classes);
 	if (st != SSFFT_SUCCESS) return st;

@@ -26,7 +26,21 @@ CASES = {
 }
 
 
-def spec_of(sizes, dt):
+def spec_of(sizes, dt, qmax=16384):
+    """The queue spec of an uneven list; every size up to qmax in a class (the library's default
+    keeps sizes above 4096 out of the classes; the kernel must be right for any class)."""
+    old = os.environ.get("SSFFT_DEBUG")
+    os.environ["SSFFT_DEBUG"] = f"queue_max_n={qmax}"
+    try:
+        return _spec(sizes, dt)
+    finally:
+        if old is None:
+            os.environ.pop("SSFFT_DEBUG", None)
+        else:
+            os.environ["SSFFT_DEBUG"] = old
+
+
+def _spec(sizes, dt):
     l = F.lib()
     l.ssfft_diag_multi_spec.argtypes = [ctypes.POINTER(ctypes.c_size_t), ctypes.c_size_t, ctypes.c_int,
                                         ctypes.c_char_p, ctypes.c_size_t, ctypes.c_void_p,
@@ -69,6 +83,14 @@ def emulator(tmp_path_factory):
            "-o", str(exe)]
     subprocess.run(cmd, check=True)
     return exe, index, d
+
+
+def test_default_queue_keeps_long_sizes_out_of_classes():
+    """By default sizes above 4096 points run as launches of their own."""
+    sizes = uneven_list("f32")
+    spec, _ = _spec(sizes, "f32")
+    assert sorted(spec["own_launch"]) == sorted({n for n in sizes if n > 4096})
+    assert all(m["n"] <= 4096 for c in spec["classes"] for m in c["members"])
 
 
 def test_queue_classes_cover_every_transform_once():
