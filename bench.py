@@ -49,7 +49,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the host-buffer leg (default: steps/10)")
     ap.add_argument("--workload", default="realfft",
-                    choices=["realfft", "fp64", "large", "serve", "uneven", "precision", "sizes", "dropin"],
+                    choices=["realfft", "fp64", "large", "serve", "uneven", "precision", "sizes", "dropin",
+                             "uneven_class"],
                     help="realfft: the batched RealFFT<float> line (default); fp64: FFT<double> N=1024 x256; "
                          "large: single FP32 transforms of 2^24, 3^15, 2^12 3^4 5^2; serve: request serving sweep; "
                          "sizes: per-size batched FP32 kernel sweep (--sizes, --kinds, --sweep-mb, --plan-options)")
@@ -67,6 +68,8 @@ def parse():
     ap.add_argument("--no-uneven", action="store_true", help="default line: skip the uneven-batch block")
     ap.add_argument("--served-duration", type=float, default=1.0,
                     help="default line: seconds of offered load per point of the served sweep")
+    ap.add_argument("--queue-mode", default="queue", choices=["queue", "pergraph"],
+                    help="uneven_class workload: one queue-class launch or one launch per size")
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
                     help="CPU baseline: seconds of CPU work in the bounded sample")
     ap.add_argument("--tune", type=int, default=2, choices=[0, 1, 2],
@@ -862,6 +865,36 @@ def run_dropin(args):
                       "cpu_reference_algorithm_1_core": cpu, "cpu_build": cpu_build_note()}), flush=True)
 
 
+def run_uneven_class(args):
+    """One queue class of long transforms on its own: 300 complex FP32 transforms each of the
+    eight sizes 8640-11520 (the 384-thread class), shuffled, U[-1,1); --queue-mode queue runs them
+    as one queue-class launch (every size in a class), pergraph as one launch per size in a CUDA
+    graph.  Mean time of --steps submissions after one warm-up."""
+    import torch
+    import fft_gb300 as F
+    sizes0 = [11520, 10800, 10240, 10125, 9375, 9216, 9000, 8640]
+    rng = np.random.default_rng(9)
+    sizes = [n for n in sizes0 for _ in range(300)]
+    rng.shuffle(sizes)
+    total = int(sum(sizes))
+    x = torch.empty(total, dtype=torch.complex64, device="cuda")
+    x.real.uniform_(-1, 1)
+    x.imag.uniform_(-1, 1)
+    y = torch.empty_like(x)
+    sh = int(torch.cuda.current_stream().cuda_stream)
+    old = os.environ.get("SSFFT_DEBUG")
+    os.environ["SSFFT_DEBUG"] = "multi_mode=1" if args.queue_mode == "pergraph" else "queue_max_n=16384"
+    m = F.Multi(sizes, "f32")
+    if old is None:
+        os.environ.pop("SSFFT_DEBUG")
+    else:
+        os.environ["SSFFT_DEBUG"] = old
+    t = _time_device(lambda: m.exec(False, x.data_ptr(), y.data_ptr(), sh), max(1, args.steps), 1)
+    peak, kind = measured_peak_hbm()
+    print(json.dumps({"workload": "uneven class 8640-11520 x300 each", "mode": args.queue_mode, "ms": t * 1e3,
+                      "frac_of_hbm": 16 * total / t / 1e9 / peak, "launches": m.info()["launches"]}), flush=True)
+
+
 def run_precision(args):
     """Complex FP32 N=1024, 32768 transforms: the FP32-FMA kernel against the split-BF16
     tensor-core first pass, forward + inverse, with relL2 against the FP64 oracle."""
@@ -945,7 +978,8 @@ def main():
         fb.build()
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         {"fp64": run_fp64, "large": run_large, "serve": run_serve, "uneven": run_uneven,
-         "precision": run_precision, "sizes": run_sizes, "dropin": run_dropin}[args.workload](args)
+         "precision": run_precision, "sizes": run_sizes, "dropin": run_dropin,
+         "uneven_class": run_uneven_class}[args.workload](args)
     else:
         run_gpu(args, rank, world if "WORLD_SIZE" in os.environ else 1)
 
