@@ -250,12 +250,17 @@ static ssfft_status form_classes(ssfft_dtype dtype, const std::vector<std::tuple
 			mem.push_back(c.members[i]);
 			sch.push_back(c.sch[i]);
 		}
-		// at most kQueueMembers sizes per kernel: NVRTC's time grows faster than the member count
-		// (71 members 48 s, 24 members 7.6 s), and chunks compile concurrently
-		for (size_t b = 0; b < mem.size(); b += kQueueMembers) {
+		// at most kQueueMembers sizes per kernel (debug switch queue_members): each member's passes
+		// are fully unrolled, and a kernel holding many of them thrashes the instruction cache
+		// (measured on GB300: 16 sizes of 900-2048 points, 0.82 of the copy bandwidth as one-size
+		// classes, 0.46 as one 16-size class, no_instruction stalls 5.9 per issue); NVRTC's time
+		// also grows faster than the member count
+		const long long qm = debug_knob("queue_members", (long long)kQueueMembers);
+		const size_t members = qm >= 1 && qm <= 64 ? (size_t)qm : kQueueMembers;
+		for (size_t b = 0; b < mem.size(); b += members) {
 			QClass part = c;
-			part.members.assign(mem.begin() + b, mem.begin() + std::min(mem.size(), b + kQueueMembers));
-			part.sch.assign(sch.begin() + b, sch.begin() + std::min(sch.size(), b + kQueueMembers));
+			part.members.assign(mem.begin() + b, mem.begin() + std::min(mem.size(), b + members));
+			part.sch.assign(sch.begin() + b, sch.begin() + std::min(sch.size(), b + members));
 			part.smem = 0;
 			part.work = 0;
 			for (size_t k = 0; k < part.sch.size(); ++k) {
