@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the host-buffer leg (default: steps/10)")
     ap.add_argument("--workload", default="realfft",
                     choices=["realfft", "fp64", "large", "serve", "uneven", "precision", "sizes", "dropin",
-                             "uneven_class"],
+                             "uneven_class", "uneven_members"],
                     help="realfft: the batched RealFFT<float> line (default); fp64: FFT<double> N=1024 x256; "
                          "large: single FP32 transforms of 2^24, 3^15, 2^12 3^4 5^2; serve: request serving sweep; "
                          "sizes: per-size batched FP32 kernel sweep (--sizes, --kinds, --sweep-mb, --plan-options)")
@@ -70,6 +70,8 @@ def parse():
                     help="default line: seconds of offered load per point of the served sweep")
     ap.add_argument("--queue-mode", default="queue", choices=["queue", "pergraph"],
                     help="uneven_class workload: one queue-class launch or one launch per size")
+    ap.add_argument("--members", type=int, default=16, help="uneven_members workload: sizes in the class")
+    ap.add_argument("--frames-total", type=int, default=4000, help="uneven_members workload: transforms in all")
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
                     help="CPU baseline: seconds of CPU work in the bounded sample")
     ap.add_argument("--tune", type=int, default=2, choices=[0, 1, 2],
@@ -895,6 +897,38 @@ def run_uneven_class(args):
                       "frac_of_hbm": 16 * total / t / 1e9 / peak, "launches": m.info()["launches"]}), flush=True)
 
 
+def run_uneven_members(args):
+    """The first --members of the 16 sizes 900-2048 (one CTA shape), 4000 // members complex FP32
+    transforms each (--frames-total overrides the 4000), shuffled, U[-1,1): as one queue class
+    (--queue-mode queue, every size in the class) or one launch per size (pergraph).  Mean time of
+    --steps submissions after two warm-ups; the instruction-cache pressure of a class grows with its
+    member count."""
+    import torch
+    import fft_gb300 as F
+    pool = [2048, 1920, 1800, 1536, 1440, 1350, 1280, 1200, 1152, 1125, 1080, 1024, 1000, 972, 960, 900]
+    k = max(1, min(16, args.members))
+    rng = np.random.default_rng(3)
+    sizes = [n for n in pool[:k] for _ in range(args.frames_total // k)]
+    rng.shuffle(sizes)
+    total = int(sum(sizes))
+    x = torch.empty(total, dtype=torch.complex64, device="cuda")
+    x.real.uniform_(-1, 1)
+    x.imag.uniform_(-1, 1)
+    y = torch.empty_like(x)
+    sh = int(torch.cuda.current_stream().cuda_stream)
+    old = os.environ.get("SSFFT_DEBUG")
+    os.environ["SSFFT_DEBUG"] = "multi_mode=1" if args.queue_mode == "pergraph" else "queue_max_n=16384,queue_members=16"
+    m = F.Multi(sizes, "f32")
+    if old is None:
+        os.environ.pop("SSFFT_DEBUG")
+    else:
+        os.environ["SSFFT_DEBUG"] = old
+    t = _time_device(lambda: m.exec(False, x.data_ptr(), y.data_ptr(), sh), max(1, args.steps), 2)
+    peak, kind = measured_peak_hbm()
+    print(json.dumps({"workload": f"uneven sizes 900-2048, {k} members", "mode": args.queue_mode, "ms": t * 1e3,
+                      "frac_of_hbm": 16 * total / t / 1e9 / peak, "launches": m.info()["launches"]}), flush=True)
+
+
 def run_precision(args):
     """Complex FP32 N=1024, 32768 transforms: the FP32-FMA kernel against the split-BF16
     tensor-core first pass, forward + inverse, with relL2 against the FP64 oracle."""
@@ -979,7 +1013,7 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         {"fp64": run_fp64, "large": run_large, "serve": run_serve, "uneven": run_uneven,
          "precision": run_precision, "sizes": run_sizes, "dropin": run_dropin,
-         "uneven_class": run_uneven_class}[args.workload](args)
+         "uneven_class": run_uneven_class, "uneven_members": run_uneven_members}[args.workload](args)
     else:
         run_gpu(args, rank, world if "WORLD_SIZE" in os.environ else 1)
 
