@@ -521,6 +521,47 @@ __device__ __forceinline__ void gstore(const Ctx<T, KIND, CIN, COUT> &c, int e, 
 	}
 }
 
+// Two adjacent elements e, e + 1 (e even) of the pass input / output in one 16-byte access
+// (FP32 with paired layout; the caller has checked that the transform starts on a 16-byte
+// boundary), with the same conjugation, packing and rotation as gload / gstore.
+template <typename T, int KIND, bool CIN, bool COUT, bool ODD>
+__device__ __forceinline__ void gload2(const Ctx<T, KIND, CIN, COUT> &c, int e, typename Cx<T>::C &a,
+                                       typename Cx<T>::C &b) {
+	static_assert(sizeof(T) == 4 && !ODD, "paired access is for FP32 data in complex pairs");
+	const float4 q = __ldcs(reinterpret_cast<const float4 *>(c.gin) + e / 2);
+	a = mkc(q.x, q.y);
+	b = mkc(q.z, q.w);
+	if constexpr (KIND == kComplex) {
+		if (CIN) {
+			a = conj(a);
+			b = conj(b);
+		}
+	} else if constexpr (KIND == kRealHalfShift) {
+		a = mul(a, __ldg(c.rot + e));
+		b = mul(b, __ldg(c.rot + e + 1));
+	}
+}
+
+template <typename T, int KIND, bool CIN, bool COUT, bool ODD>
+__device__ __forceinline__ void gstore2(const Ctx<T, KIND, CIN, COUT> &c, int e, typename Cx<T>::C a,
+                                        typename Cx<T>::C b) {
+	static_assert(sizeof(T) == 4 && !ODD, "paired access is for FP32 data in complex pairs");
+	if constexpr (KIND == kComplex) {
+		if (COUT) {
+			a = conj(a);
+			b = conj(b);
+		}
+	} else {
+		a = conj(a);
+		b = conj(b);
+		if constexpr (KIND == kRealHalfShift) {
+			a = mulc(a, __ldg(c.rot + e));
+			b = mulc(b, __ldg(c.rot + e + 1));
+		}
+	}
+	__stcs(reinterpret_cast<float4 *>(c.gout) + e / 2, make_float4(a.x, a.y, b.x, b.y));
+}
+
 // ------------------------------------------------------------------ one pass
 
 // Twiddle rows stored for a pass of radix R: FP32 register butterflies store exponents 1, 2, 4, 8,
@@ -567,37 +608,94 @@ __device__ __forceinline__ void pass(const Ctx<T, KIND, CIN, COUT> &c, const typ
 	if constexpr (Specialised<R>::value) {
 		constexpr int NBPT = (NB + THREADS - 1) / THREADS;  // butterflies per thread
 		constexpr bool GUARD = NB % THREADS != 0;
+		// 128-bit global access: when a thread holds two or more butterflies of a pass that reads
+		// or writes HBM (the first / last pass), it takes adjacent pairs (j, j + 1), whose
+		// elements j + r NB and j + 1 + r NB (and, in the last pass, outputs) are one 16-byte
+		// load or store; transforms that do not start on a 16-byte boundary use 8-byte accesses
+		constexpr int NPAIR = NB / 2;
+		constexpr bool PAIRED = sizeof(T) == 4 && !ODD && (SRC == kGlobal || DST == kGlobal) && NB % 2 == 0 &&
+		                        NBPT % 2 == 0 && 2 * ((NPAIR + THREADS - 1) / THREADS) == NBPT;
+		constexpr bool PGUARD = NPAIR % THREADS != 0;
+		auto jof = [&c](int i) { return PAIRED ? 2 * (c.t + (i >> 1) * THREADS) + (i & 1) : c.t + i * THREADS; };
+		auto okof = [&c](int i) {
+			return PAIRED ? (!PGUARD || c.t + (i >> 1) * THREADS < NPAIR) : (!GUARD || c.t + i * THREADS < NB);
+		};
 		C v[NBPT][R];
+		if constexpr (PAIRED && SRC == kGlobal) {
+			const bool al = (reinterpret_cast<unsigned long long>(c.gin) & 15ull) == 0;
 #pragma unroll
-		for (int i = 0; i < NBPT; ++i) {
-			const int j = c.t + i * THREADS;
-			if (c.valid && (!GUARD || j < NB)) {
+			for (int i = 0; i < NBPT; i += 2) {
+				const int j = jof(i);
+				if (c.valid && okof(i)) {
+					if (al) {
 #pragma unroll
-				for (int r = 0; r < R; ++r) {
-					if constexpr (SRC == kSmem) v[i][r] = c.sm[pidx<PS>(j + r * NB)];
-					else if constexpr (SRC == kStage) v[i][r] = sload(c, j + r * NB);
-					else v[i][r] = gload<T, KIND, CIN, COUT, ODD>(c, j + r * NB);
+						for (int r = 0; r < R; ++r)
+							gload2<T, KIND, CIN, COUT, ODD>(c, j + r * NB, v[i][r], v[i + 1][r]);
+					} else {
+#pragma unroll
+						for (int r = 0; r < R; ++r) {
+							v[i][r] = gload<T, KIND, CIN, COUT, ODD>(c, j + r * NB);
+							v[i + 1][r] = gload<T, KIND, CIN, COUT, ODD>(c, j + 1 + r * NB);
+						}
+					}
+				}
+			}
+		} else {
+#pragma unroll
+			for (int i = 0; i < NBPT; ++i) {
+				const int j = jof(i);
+				if (c.valid && okof(i)) {
+#pragma unroll
+					for (int r = 0; r < R; ++r) {
+						if constexpr (SRC == kSmem) v[i][r] = c.sm[pidx<PS>(j + r * NB)];
+						else if constexpr (SRC == kStage) v[i][r] = sload(c, j + r * NB);
+						else v[i][r] = gload<T, KIND, CIN, COUT, ODD>(c, j + r * NB);
+					}
 				}
 			}
 		}
 #pragma unroll
 		for (int i = 0; i < NBPT; ++i) {
-			const int j = c.t + i * THREADS;
-			if (c.valid && (!GUARD || j < NB)) {
+			const int j = jof(i);
+			if (c.valid && okof(i)) {
 				if constexpr (NS > 1) apply_twiddles<T, R, NS, TWO>(v[i], tw, j % NS);
 				dft<R>(v[i]);
 			}
 		}
 		if constexpr (SRC == kSmem && DST == kSmem) __syncthreads();
+		if constexpr (PAIRED && DST == kGlobal) {
+			// the last pass (NS = NB): butterfly j writes outputs j + r NS, so a pair's outputs sit
+			// side by side
+			static_assert(NS == NB, "paired stores are for the last pass");
+			const bool al = (reinterpret_cast<unsigned long long>(c.gout) & 15ull) == 0;
 #pragma unroll
-		for (int i = 0; i < NBPT; ++i) {
-			const int j = c.t + i * THREADS;
-			if (c.valid && (!GUARD || j < NB)) {
-				const int base = (j / NS) * NS * (R - 1) + j;  // (j - j mod NS) * R + j mod NS
+			for (int i = 0; i < NBPT; i += 2) {
+				const int j = jof(i);
+				if (c.valid && okof(i)) {
+					if (al) {
 #pragma unroll
-				for (int r = 0; r < R; ++r) {
-					if constexpr (DST == kSmem) c.sm[pidx<PS>(base + r * NS)] = v[i][r];
-					else gstore<T, KIND, CIN, COUT, ODD>(c, base + r * NS, v[i][r]);
+						for (int r = 0; r < R; ++r)
+							gstore2<T, KIND, CIN, COUT, ODD>(c, j + r * NS, v[i][r], v[i + 1][r]);
+					} else {
+#pragma unroll
+						for (int r = 0; r < R; ++r) {
+							gstore<T, KIND, CIN, COUT, ODD>(c, j + r * NS, v[i][r]);
+							gstore<T, KIND, CIN, COUT, ODD>(c, j + 1 + r * NS, v[i + 1][r]);
+						}
+					}
+				}
+			}
+		} else {
+#pragma unroll
+			for (int i = 0; i < NBPT; ++i) {
+				const int j = jof(i);
+				if (c.valid && okof(i)) {
+					const int base = (j / NS) * NS * (R - 1) + j;  // (j - j mod NS) * R + j mod NS
+#pragma unroll
+					for (int r = 0; r < R; ++r) {
+						if constexpr (DST == kSmem) c.sm[pidx<PS>(base + r * NS)] = v[i][r];
+						else gstore<T, KIND, CIN, COUT, ODD>(c, base + r * NS, v[i][r]);
+					}
 				}
 			}
 		}

@@ -25,6 +25,10 @@ struct float2 {
 struct double2 {
 	double x, y;
 };
+struct alignas(16) float4 {
+	float x, y, z, w;
+};
+inline float4 make_float4(float x, float y, float z, float w) { return float4{x, y, z, w}; }
 inline float2 make_float2(float x, float y) { return float2{x, y}; }
 inline double2 make_double2(double x, double y) { return double2{x, y}; }
 
