@@ -158,12 +158,12 @@ ssfft_status ssfft_exec_host(ssfft_plan_t plan, int inverse, const void *h_in, v
  * sizes loops over objects).  `count` independent complex transforms of sizes sizes[i] (each at
  * most 16384 points FP32 / 8192 FP64), stored back to back: transform i starts at the sum of the
  * sizes before it (complex elements).  ssfft_multi_exec runs them all as one CUDA graph launch
- * (captured once per input/output/direction) of a few work-item queue kernels: sizes up to 4096
- * points whose size-specialised schedules share a CTA shape form a class, one kernel per class
- * holds all of their passes, and its CTAs take work items (as many transforms as one CTA runs)
- * from a queue ordered longest transforms first; longer sizes keep one offset-table launch each
- * (their unrolled code is too large to share an instruction cache); all launches run on parallel
- * branches.
+ * (captured once per input/output/direction) of work-item queue kernels and per-size launches:
+ * sizes up to 1024 points whose size-specialised schedules share a CTA shape form classes of up
+ * to four, one kernel per class holds their passes, and its CTAs take work items (as many
+ * transforms as one CTA runs) from a queue ordered longest transforms first; longer sizes keep
+ * one offset-table launch each (fully unrolled passes of many sizes in one kernel thrash the
+ * instruction cache); all launches run on parallel branches.
  * ssfft_multi_exec_plain runs one plain launch per distinct size, one after another, on
  * `stream`, for comparison. */
 typedef struct ssfft_multi_s *ssfft_multi_t;
@@ -295,7 +295,7 @@ ssfft_status ssfft_diag_large_spec(size_t n, ssfft_dtype dtype, ssfft_kind kind,
  * and per class the byte offsets in `blob` of its int32 tables: the member of each item and, per
  * item and thread, the element offset of the transform that thread works on, -1 for none);
  * `blob` the FP64 pass twiddles and roots, then those tables (NULL: only *blob_bytes is set).
- * Sizes above 4096 points keep a launch of their own ("own_launch" in `json`).
+ * Sizes above 1024 points keep a launch of their own ("own_launch" in `json`).
  * ssfft_diag_multi_jit_check compiles the class kernels for `arch`.  No reference counterpart. */
 ssfft_status ssfft_diag_multi_spec(const size_t *sizes, size_t count, ssfft_dtype dtype, char *json, size_t json_len,
                                    void *blob, size_t *blob_bytes);

@@ -26,11 +26,11 @@ CASES = {
 }
 
 
-def spec_of(sizes, dt, qmax=16384):
+def spec_of(sizes, dt, qmax=16384, members=16):
     """The queue spec of an uneven list; every size up to qmax in a class (the library's default
     keeps sizes above 4096 out of the classes; the kernel must be right for any class)."""
     old = os.environ.get("SSFFT_DEBUG")
-    os.environ["SSFFT_DEBUG"] = f"queue_max_n={qmax}"
+    os.environ["SSFFT_DEBUG"] = f"queue_max_n={qmax},queue_members={members}"
     try:
         return _spec(sizes, dt)
     finally:
@@ -86,11 +86,13 @@ def emulator(tmp_path_factory):
 
 
 def test_default_queue_keeps_long_sizes_out_of_classes():
-    """By default sizes above 4096 points run as launches of their own."""
+    """By default sizes above 1024 points run as launches of their own, and a class holds at most
+    four sizes."""
     sizes = uneven_list("f32")
     spec, _ = _spec(sizes, "f32")
-    assert sorted(spec["own_launch"]) == sorted({n for n in sizes if n > 4096})
-    assert all(m["n"] <= 4096 for c in spec["classes"] for m in c["members"])
+    assert sorted(spec["own_launch"]) == sorted({n for n in sizes if n > 1024})
+    assert all(m["n"] <= 1024 for c in spec["classes"] for m in c["members"])
+    assert all(len(c["members"]) <= 4 for c in spec["classes"])
 
 
 def test_queue_classes_cover_every_transform_once():
