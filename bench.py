@@ -995,7 +995,7 @@ def run_sizes(args):
             d = p.describe()
             print(json.dumps({"n": n, "kind": kind, "batch": batch, **res, "peak_GB_s": peak, "peak_source": kind_src,
                               "radices": d["radices"], "threads": d["threads"], "per_cta": d["per_cta"],
-                              "schedule": p.tuning()["choice"]}), flush=True)
+                              "schedule": p.tuning()["choice"], "kernel": p.kernel(False)}), flush=True)
             del x, y, p
             torch.cuda.empty_cache()
 

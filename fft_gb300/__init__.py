@@ -125,6 +125,7 @@ def _declare(l):
     l.ssfft_plan_device_bytes.restype = _sz
     l.ssfft_plan_describe.argtypes = [_vp, ctypes.POINTER(_int), ctypes.POINTER(_int), _int, ctypes.POINTER(_int),
                                       ctypes.POINTER(_int), ctypes.POINTER(_int)]
+    l.ssfft_plan_kernel.argtypes = [_vp, _int, ctypes.c_char_p, _sz]
     l.ssfft_exec.argtypes = [_vp, _int, _vp, _vp, _vp]
     l.ssfft_exec_batch.argtypes = [_vp, _int, _vp, _vp, _sz, _vp]
     l.ssfft_exec_host.argtypes = [_vp, _int, _vp, _vp]
@@ -140,7 +141,8 @@ def _declare(l):
     l.ssfft_schedule_options.argtypes = [ctypes.POINTER(PlanOptions)]
     l.ssfft_schedule_direction.argtypes = [_int]
     l.ssfft_diag_tc_tile.argtypes = [_vp, _vp, _vp, ctypes.POINTER(ctypes.c_uint)]
-    for name in ("ssfft_plan_create", "ssfft_plan_create_ex", "ssfft_plan_tuning", "ssfft_plan_destroy", "ssfft_plan_describe", "ssfft_exec", "ssfft_exec_batch",
+    for name in ("ssfft_plan_create", "ssfft_plan_create_ex", "ssfft_plan_tuning", "ssfft_plan_destroy", "ssfft_plan_describe",
+                 "ssfft_plan_kernel", "ssfft_exec", "ssfft_exec_batch",
                  "ssfft_exec_host", "ssfft_plan_error", "ssfft_diag_staged_timeout", "ssfft_schedule_options", "ssfft_schedule_direction",
                  "ssfft_diag_tc_tile", "ssfft_jit_check", "ssfft_schedule_info", "ssfft_schedule_name",
                  "ssfft_schedule_tables"):
@@ -333,6 +335,12 @@ class Plan:
         b = ctypes.create_string_buffer(16384)
         check(lib().ssfft_plan_tuning(self._h, a, 256, b, 16384), "plan_tuning")
         return {"choice": a.value.decode(), "log": [x for x in b.value.decode().splitlines() if x]}
+
+    def kernel(self, inverse: bool = False) -> str:
+        """Kernel template the plan launches ("multi-pass" beyond one CTA)."""
+        b = ctypes.create_string_buffer(1024)
+        check(lib().ssfft_plan_kernel(self._h, int(bool(inverse)), b, 1024), "plan_kernel")
+        return b.value.decode()
 
     @property
     def handle(self):

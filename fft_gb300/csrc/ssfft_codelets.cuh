@@ -51,6 +51,11 @@ enum : int { kComplex = 0, kReal = 1, kRealHalfShift = 2 };
 // element sources / destinations of a pass: padded shared memory, HBM, or the unpadded staging
 // buffer a bulk copy filled
 enum : int { kSmem = 0, kGlobal = 1, kStage = 2 };
+// first pass of a split-staged kernel: rows r < K of the first pass (elements j + r NB) in the
+// staging buffer, rows r >= K in the work buffer (unpadded, from element K NB on); the source
+// code is kStageSplit + K
+enum : int { kStageSplit = 16 };
+__host__ __device__ constexpr bool is_stage(int src) { return src == kStage || src >= kStageSplit; }
 // fused real split: the last pass of a RealFFT forward writes the bins (kFusedR2C), the first pass
 // of its inverse reads the bins and pre-twiddles them (kFusedC2R)
 enum : int { kFusedR2C = 3, kFusedC2R = 4 };
@@ -423,6 +428,7 @@ struct Ctx {
 	T *gout;       // this transform's output, in scalars
 	const C *rot;  // half-shift rotations
 	const C *st;   // staged kernels: this transform's input in the unpadded staging buffer
+	const C *st2;  // split-staged kernels: the first pass's rows >= K (unpadded, in the work buffer)
 	const C *rtw;  // real split twiddles (fused split passes)
 	int t;         // thread index inside the transform
 	bool valid;    // the transform exists (the last CTA may be partial)
@@ -430,14 +436,29 @@ struct Ctx {
 
 // Element e of the staged input (same meaning as gload, but from shared memory).
 template <typename T, int KIND, bool CIN, bool COUT>
-__device__ __forceinline__ typename Cx<T>::C sload(const Ctx<T, KIND, CIN, COUT> &c, int e) {
-	using C = typename Cx<T>::C;
-	C v = c.st[e];
+__device__ __forceinline__ typename Cx<T>::C sfix(const Ctx<T, KIND, CIN, COUT> &c, int e, typename Cx<T>::C v) {
 	if constexpr (KIND == kComplex) {
 		return CIN ? conj(v) : v;
 	} else {
 		if constexpr (KIND == kRealHalfShift) v = mul(v, __ldg(c.rot + e));
 		return v;
+	}
+}
+template <typename T, int KIND, bool CIN, bool COUT>
+__device__ __forceinline__ typename Cx<T>::C sload(const Ctx<T, KIND, CIN, COUT> &c, int e) {
+	return sfix(c, e, c.st[e]);
+}
+// Element j + r NB of the first pass's input from a staging source SRC (kStage: all of it in the
+// staging buffer; kStageSplit + K: rows r < K there, the others in the work buffer).  With r a
+// compile-time constant (unrolled loops) the choice of buffer costs nothing.
+template <int SRC, int NB, typename T, int KIND, bool CIN, bool COUT>
+__device__ __forceinline__ typename Cx<T>::C sload_row(const Ctx<T, KIND, CIN, COUT> &c, int j, int r) {
+	const int e = j + r * NB;
+	if constexpr (SRC >= kStageSplit) {
+		constexpr int K = SRC - kStageSplit;
+		return sfix(c, e, r < K ? c.st[e] : c.st2[e - K * NB]);
+	} else {
+		return sload(c, e);
 	}
 }
 
@@ -564,6 +585,12 @@ __device__ __forceinline__ void gstore2(const Ctx<T, KIND, CIN, COUT> &c, int e,
 
 // ------------------------------------------------------------------ one pass
 
+// A hook that does nothing (passes / pass take hooks at fixed points of the pass list).
+struct NoHook {
+	__device__ __forceinline__ void operator()() const {}
+};
+
+
 // Twiddle rows stored for a pass of radix R: FP32 register butterflies store exponents 1, 2, 4, 8,
 // 16 (< R); FP64 passes (bound by FP64 arithmetic, not memory) and direct passes store every
 // exponent 1..R-1.
@@ -598,13 +625,17 @@ __device__ __forceinline__ void apply_twiddles(typename Cx<T>::C (&v)[R], const 
 	}
 }
 
+// `loaded` runs once every thread has its inputs of the pass in registers (the split-staged
+// kernel refills the work buffer there, during the last pass).  A first pass that reads part of
+// its input from the buffer it writes (split staging) waits for every thread's loads first.
 template <typename T, int N, int THREADS, int R, int NS, int TWO, int ROOTS, int SRC, int DST, int KIND, bool CIN,
-          bool COUT, bool ODD, int EMAX>
+          bool COUT, bool ODD, int EMAX, class Loaded = NoHook>
 __device__ __forceinline__ void pass(const Ctx<T, KIND, CIN, COUT> &c, const typename Cx<T>::C *tw,
-                                     const typename Cx<T>::C *roots) {
+                                     const typename Cx<T>::C *roots, const Loaded &loaded = Loaded()) {
 	using C = typename Cx<T>::C;
 	constexpr int PS = Cx<T>::kPadShift;
 	constexpr int NB = N / R;
+	constexpr bool IN_PLACE = (SRC == kSmem || SRC >= kStageSplit) && DST == kSmem;
 	if constexpr (Specialised<R>::value) {
 		constexpr int NBPT = (NB + THREADS - 1) / THREADS;  // butterflies per thread
 		constexpr bool GUARD = NB % THREADS != 0;
@@ -648,12 +679,13 @@ __device__ __forceinline__ void pass(const Ctx<T, KIND, CIN, COUT> &c, const typ
 #pragma unroll
 					for (int r = 0; r < R; ++r) {
 						if constexpr (SRC == kSmem) v[i][r] = c.sm[pidx<PS>(j + r * NB)];
-						else if constexpr (SRC == kStage) v[i][r] = sload(c, j + r * NB);
+						else if constexpr (is_stage(SRC)) v[i][r] = sload_row<SRC, NB>(c, j, r);
 						else v[i][r] = gload<T, KIND, CIN, COUT, ODD>(c, j + r * NB);
 					}
 				}
 			}
 		}
+		loaded();
 #pragma unroll
 		for (int i = 0; i < NBPT; ++i) {
 			const int j = jof(i);
@@ -662,7 +694,7 @@ __device__ __forceinline__ void pass(const Ctx<T, KIND, CIN, COUT> &c, const typ
 				dft<R>(v[i]);
 			}
 		}
-		if constexpr (SRC == kSmem && DST == kSmem) __syncthreads();
+		if constexpr (IN_PLACE) __syncthreads();
 		if constexpr (PAIRED && DST == kGlobal) {
 			// the last pass (NS = NB): butterfly j writes outputs j + r NS, so a pair's outputs sit
 			// side by side
@@ -713,13 +745,13 @@ __device__ __forceinline__ void pass(const Ctx<T, KIND, CIN, COUT> &c, const typ
 				const int k = e / NB, j = e - (e / NB) * NB, m = j % NS;
 				C s;
 				if constexpr (SRC == kSmem) s = c.sm[pidx<PS>(j)];
-				else if constexpr (SRC == kStage) s = sload(c, j);
+				else if constexpr (is_stage(SRC)) s = sload_row<SRC, NB>(c, j, 0);
 				else s = gload<T, KIND, CIN, COUT, ODD>(c, j);
 				int w = 0;
 				for (int r = 1; r < R; ++r) {
 					C x;
 					if constexpr (SRC == kSmem) x = c.sm[pidx<PS>(j + r * NB)];
-					else if constexpr (SRC == kStage) x = sload(c, j + r * NB);
+					else if constexpr (is_stage(SRC)) x = sload_row<SRC, NB>(c, j, r);
 					else x = gload<T, KIND, CIN, COUT, ODD>(c, j + r * NB);
 					if constexpr (NS > 1) x = mul(x, __ldg(tw + TWO + (r - 1) * NS + m));
 					w += k;
@@ -729,7 +761,8 @@ __device__ __forceinline__ void pass(const Ctx<T, KIND, CIN, COUT> &c, const typ
 				acc[i] = s;
 			}
 		}
-		if constexpr (SRC == kSmem && DST == kSmem) __syncthreads();
+		loaded();
+		if constexpr (IN_PLACE) __syncthreads();
 #pragma unroll
 		for (int i = 0; i < OPT; ++i) {
 			const int e = c.t + i * THREADS;
@@ -754,10 +787,6 @@ struct TwCount {
 template <int R>
 struct RootCount {
 	static constexpr int value = Specialised<R>::value ? 0 : R;
-};
-
-struct NoHook {
-	__device__ __forceinline__ void operator()() const {}
 };
 
 // ------------------------------------------------------------------ real split fused into a pass
@@ -949,22 +978,25 @@ __device__ __forceinline__ void pass_first_c2r(const Ctx<T, KIND, CIN, COUT> &c)
 }
 
 // All passes of the transform; `after_first` runs (on every thread) once the first pass has
-// consumed its input.
+// consumed its input, `last_loaded` once every thread holds the inputs of the last (register or
+// direct) pass.
 template <typename T, int N, int THREADS, int NS, int TWO, int ROOTS, int FIRST_SRC, int LAST_DST, int KIND, bool CIN,
-          bool COUT, bool ODD, int EMAX, int R, int... Rest, class Hook = NoHook>
+          bool COUT, bool ODD, int EMAX, int R, int... Rest, class Hook = NoHook, class LastLoaded = NoHook>
 __device__ __forceinline__ void passes(const Ctx<T, KIND, CIN, COUT> &c, const typename Cx<T>::C *tw,
-                                       const typename Cx<T>::C *roots, const Hook &after_first = Hook()) {
+                                       const typename Cx<T>::C *roots, const Hook &after_first = Hook(),
+                                       const LastLoaded &last_loaded = LastLoaded()) {
 	constexpr bool last = sizeof...(Rest) == 0;
 	constexpr int SRC = NS == 1 ? FIRST_SRC : kSmem;
 	constexpr int DST = last ? LAST_DST : kSmem;
 	static_assert(!(SRC == kFusedC2R && last) && !(DST == kFusedR2C && NS == 1), "fused split needs two passes or more");
 	if constexpr (SRC == kFusedC2R) pass_first_c2r<T, N, THREADS, R, KIND, CIN, COUT>(c);
 	else if constexpr (DST == kFusedR2C) pass_last_r2c<T, N, THREADS, R, NS, TWO, KIND, CIN, COUT>(c, tw);
+	else if constexpr (last) pass<T, N, THREADS, R, NS, TWO, ROOTS, SRC, DST, KIND, CIN, COUT, ODD, EMAX>(c, tw, roots, last_loaded);
 	else pass<T, N, THREADS, R, NS, TWO, ROOTS, SRC, DST, KIND, CIN, COUT, ODD, EMAX>(c, tw, roots);
 	if constexpr (NS == 1) after_first();
 	if constexpr (!last)
 		passes<T, N, THREADS, NS * R, TWO + TwCount<T, R, NS>::value, ROOTS + RootCount<R>::value, FIRST_SRC, LAST_DST,
-		       KIND, CIN, COUT, ODD, EMAX, Rest...>(c, tw, roots, NoHook());
+		       KIND, CIN, COUT, ODD, EMAX, Rest...>(c, tw, roots, NoHook(), last_loaded);
 }
 
 // ------------------------------------------------------------------ real split / merge
@@ -1289,6 +1321,11 @@ inline bool mbar_wait_bounded(unsigned long long *bar, unsigned phase, unsigned 
 }
 #endif
 
+template <int R, int... Rest>
+struct FirstRadix {
+	static constexpr int value = R;
+};
+
 // The batch kernel with asynchronous input staging: persistent CTAs walk the groups of PER_CTA
 // transforms; each group's input (contiguous in HBM) arrives in an unpadded staging buffer by
 // one bulk copy, and the copy of the next group is issued as soon as the first pass (or the
@@ -1296,17 +1333,28 @@ inline bool mbar_wait_bounded(unsigned long long *bar, unsigned phase, unsigned 
 // Requires in_bytes % 16 == 0 and 16-byte aligned input.  A bounded wait that runs out sets
 // *err and the CTA returns without writing.  (Inside the persistent loop the compiler keeps far
 // more registers live than one pass needs; MINB caps them.)
-template <typename T, int N, int THREADS, int PER_CTA, int SMEM_STRIDE, int KIND, bool INV, int EMAX, int MINB,
+//
+// SK > 0 (complex, one transform per CTA, a transform too long for a staging buffer and a work
+// buffer of its whole size): only rows r < SK of the first pass (elements j + r NB, the first
+// SK NB elements) are staged; rows r >= SK arrive by a second bulk copy into the start of the work
+// buffer, issued once every thread holds the previous group's last-pass inputs.  The first pass
+// reads both and, after a barrier, writes the work buffer.
+template <typename T, int N, int THREADS, int PER_CTA, int SMEM_STRIDE, int KIND, bool INV, int EMAX, int MINB, int SK,
           int... Rs>
 __global__ void __launch_bounds__(THREADS *PER_CTA, MINB) batch_staged(const Args a) {
 	using C = typename Cx<T>::C;
 	constexpr bool REAL = KIND != kComplex;
 	constexpr bool R2C = REAL && !INV, C2R = REAL && INV;
+	constexpr int NB0 = N / FirstRadix<Rs...>::value;
+	static_assert(SK == 0 || (!REAL && PER_CTA == 1 && SK < FirstRadix<Rs...>::value),
+	              "split staging: complex, one transform per CTA, some rows in the work buffer");
+	constexpr unsigned kStageBytes = (unsigned)SK * NB0 * sizeof(C);  // SK > 0: staged bytes per transform
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	__shared__ __align__(8) unsigned long long bar;
+	__shared__ __align__(8) unsigned long long bar[2];  // staging buffer, rows in the work buffer
 	const unsigned in_bytes = a.in_bytes;
 	unsigned char *stage = smem_raw;
-	C *work = reinterpret_cast<C *>(smem_raw + ((PER_CTA * in_bytes + 127u) & ~127u));
+	const unsigned stage_bytes = SK ? kStageBytes : PER_CTA * in_bytes;
+	C *work = reinterpret_cast<C *>(smem_raw + ((stage_bytes + 127u) & ~127u));
 	const long long ngroups = (a.batch + PER_CTA - 1) / PER_CTA;
 	const unsigned char *in = reinterpret_cast<const unsigned char *>(a.in);
 	const int g = threadIdx.x / THREADS;
@@ -1314,26 +1362,40 @@ __global__ void __launch_bounds__(THREADS *PER_CTA, MINB) batch_staged(const Arg
 	c.t = threadIdx.x - g * THREADS;
 	c.sm = work + g * SMEM_STRIDE;
 	c.st = reinterpret_cast<const C *>(stage + g * in_bytes);
+	c.st2 = work;
 	c.rot = reinterpret_cast<const C *>(a.rot);
 	c.gin = nullptr;
 	const C *tw = reinterpret_cast<const C *>(a.tw);
 	const C *roots = reinterpret_cast<const C *>(a.roots);
 	const C *rtw = reinterpret_cast<const C *>(a.rtw);
+	// the staged part of group grp (all of it unless SK > 0) and, SK > 0, the rest
 	auto issue = [&](long long grp) {
 		const long long nt = a.batch - grp * PER_CTA < PER_CTA ? a.batch - grp * PER_CTA : PER_CTA;
-		bulk_load(stage, in + grp * PER_CTA * (long long)in_bytes, (unsigned)(nt * in_bytes), &bar, a.drop_copy != 0);
+		const unsigned char *src = in + grp * PER_CTA * (long long)in_bytes;
+		bulk_load(stage, src, SK ? kStageBytes : (unsigned)(nt * in_bytes), &bar[0], a.drop_copy != 0);
+	};
+	auto issue_rest = [&](long long grp) {
+		const unsigned char *src = in + grp * (long long)in_bytes + kStageBytes;
+		bulk_load(work, src, in_bytes - kStageBytes, &bar[1], a.drop_copy != 0);
 	};
 	if (threadIdx.x == 0) {
-		mbar_init(&bar, 1);
-		if (blockIdx.x < ngroups) issue(blockIdx.x);
+		mbar_init(&bar[0], 1);
+		if constexpr (SK > 0) mbar_init(&bar[1], 1);
+		if (blockIdx.x < ngroups) {
+			issue(blockIdx.x);
+			if constexpr (SK > 0) issue_rest(blockIdx.x);
+		}
 	}
 	__syncthreads();
 	unsigned phase = 0;
 	for (long long grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
-		const bool ok = mbar_wait_bounded(&bar, phase, a.spin_limit);
+		bool ok = mbar_wait_bounded(&bar[0], phase, a.spin_limit);
+		if constexpr (SK > 0) ok = mbar_wait_bounded(&bar[1], phase, a.spin_limit) && ok;
 		if (__syncthreads_or(!ok)) {
 			if (threadIdx.x == 0) atomicOr(a.err, 1u);
-			mbar_wait_bounded(&bar, phase, a.spin_limit);  // let the copy in flight land
+			// let the copies in flight land
+			mbar_wait_bounded(&bar[0], phase, a.spin_limit);
+			if constexpr (SK > 0) mbar_wait_bounded(&bar[1], phase, a.spin_limit);
 			return;
 		}
 		phase ^= 1u;
@@ -1346,12 +1408,25 @@ __global__ void __launch_bounds__(THREADS *PER_CTA, MINB) batch_staged(const Arg
 			if (threadIdx.x == 0 && next < ngroups) {
 				fence_async_smem();
 				issue(next);
+				// the rows the work buffer takes later: towards L2 now
+				if constexpr (SK > 0)
+					prefetch_l2_bulk(in + next * (long long)in_bytes + kStageBytes, in_bytes - kStageBytes);
 			}
 		};
 		if constexpr (C2R) {
 			real_pre<T, N, THREADS, KIND, INV, INV, true>(c, rtw);
 			refill();
 			passes<T, N, THREADS, 1, 0, 0, kSmem, kGlobal, KIND, INV, INV, false, EMAX, Rs...>(c, tw, roots);
+		} else if constexpr (SK > 0) {
+			auto refill_rest = [&]() {
+				__syncthreads();  // every thread holds its last-pass inputs: the work buffer is free
+				if (threadIdx.x == 0 && next < ngroups) {
+					fence_async_smem();
+					issue_rest(next);
+				}
+			};
+			passes<T, N, THREADS, 1, 0, 0, kStageSplit + SK, kGlobal, KIND, INV, INV, false, EMAX, Rs...>(
+			    c, tw, roots, refill, refill_rest);
 		} else {
 			passes<T, N, THREADS, 1, 0, 0, kStage, R2C ? kSmem : kGlobal, KIND, INV, INV, false, EMAX, Rs...>(c, tw, roots,
 			                                                                                                refill);

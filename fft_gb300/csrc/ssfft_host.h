@@ -17,6 +17,13 @@ namespace ssfft {
 constexpr int kElemsPerThread = 16;     // complex values a thread holds in one pass
 constexpr int kMaxCtaThreads = 1024;
 constexpr int kMaxSubTransform = 16384; // longest transform one CTA runs (FP32)
+// Staged (bulk-copy) kernels: dynamic shared memory at most 227 KiB less the kernel's static
+// barriers; long complex FP32 transforms (>= kLongStagedMin points) stage at <= kLongStagedThreads
+// threads per transform
+constexpr size_t kStagedSmemMax = 227 * 1024 - 256;
+constexpr int kLongStagedMin = 8192;
+constexpr int kLongStagedThreads = 384;
+constexpr int kLongStagedLocalMax = 64;  // spill bytes per thread a default long staged kernel may have
 
 // A size-specialised kernel schedule: the compile-time parameters of one ssfft_cl::batch (or
 // ssfft_cl::strided) instantiation.
@@ -35,6 +42,7 @@ struct Schedule {
 	int minb = 1;             // launch-bound CTAs per SM (register cap)
 	int emax = 16;            // complex values a thread holds in one pass
 	unsigned in_bytes = 0;    // staged: input bytes of one transform
+	int stage_rows = 0;       // staged, > 0: only the first pass's rows r < stage_rows are staged
 	size_t smem_bytes = 0;
 	int pair = 0;             // ssfft_cl::pair (two-CTA cluster): the first `pair` radices are phase A
 	int n1 = 0;               // pair: phase A length (product of its radices)
@@ -157,6 +165,8 @@ ssfft_status jit_launch(CUfunction f, unsigned grid, unsigned block, size_t smem
 ssfft_status jit_launch_grid(CUfunction f, unsigned grid_x, unsigned grid_y, unsigned block, size_t smem,
                              cudaStream_t stream, void *args);
 int jit_occupancy(CUfunction f, int block, size_t smem);
+// local (spill and stack) bytes per thread of a loaded kernel
+int jit_local_bytes(CUfunction f);
 const char *jit_last_log();
 std::string jit_cache_dir();
 uint64_t codelet_hash();

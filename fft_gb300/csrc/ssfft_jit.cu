@@ -43,6 +43,7 @@ struct Driver {
 	CUresult (*moduleUnload)(CUmodule) = nullptr;
 	CUresult (*moduleGetFunction)(CUfunction *, CUmodule, const char *) = nullptr;
 	CUresult (*funcSetAttribute)(CUfunction, CUfunction_attribute, int) = nullptr;
+	CUresult (*funcGetAttribute)(int *, CUfunction_attribute, CUfunction) = nullptr;
 	CUresult (*launchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, CUstream,
 	                         void **, void **) = nullptr;
 	CUresult (*getErrorString)(CUresult, const char **) = nullptr;
@@ -69,7 +70,8 @@ const Driver &driver() {
 		Driver d;
 		d.ok = resolve("cuModuleLoadData", d.moduleLoadData) && resolve("cuModuleUnload", d.moduleUnload) &&
 		       resolve("cuModuleGetFunction", d.moduleGetFunction) &&
-		       resolve("cuFuncSetAttribute", d.funcSetAttribute) && resolve("cuLaunchKernel", d.launchKernel) &&
+		       resolve("cuFuncSetAttribute", d.funcSetAttribute) && resolve("cuFuncGetAttribute", d.funcGetAttribute) &&
+		       resolve("cuLaunchKernel", d.launchKernel) &&
 		       resolve("cuGetErrorString", d.getErrorString) &&
 		       resolve("cuOccupancyMaxActiveBlocksPerMultiprocessor", d.occupancy);
 		g_drv = d;
@@ -325,6 +327,13 @@ int jit_occupancy(CUfunction f, int block, size_t smem) {
 
 ssfft_status jit_launch(CUfunction f, unsigned grid, unsigned block, size_t smem, cudaStream_t stream, void *args) {
 	return jit_launch_grid(f, grid, 1, block, smem, stream, args);
+}
+
+int jit_local_bytes(CUfunction f) {
+	int n = 0;
+	if (!driver().funcGetAttribute || driver().funcGetAttribute(&n, CU_FUNC_ATTRIBUTE_LOCAL_SIZE_BYTES, f) != CUDA_SUCCESS)
+		return 0;
+	return n;
 }
 
 std::string jit_cache_dir() { return cache_dir(); }

@@ -495,29 +495,71 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	// a whole number of 16-byte units and a group of them fits the copy and shared-memory limits.
 	const size_t sb = eb / 2;
 	const size_t in_bytes = kind == 0 ? (size_t)n * eb : (size_t)2 * n * sb;  // real: n_real = 2h reals or h bins
-	// Opt-in (debug switch staged=1, read when a plan is made): measured slower than the unstaged
-	// kernel on GB300 so far.
+	// Opt-in for every size (debug switch staged=1, read when a plan is made): measured slower than
+	// the unstaged kernel on GB300 below 8192 points.  Long complex FP32 transforms (debug switch
+	// long_staged) run one transform per CTA at <= 384 threads, where the persistent loop does not
+	// spill, with the whole input staged when it fits beside the work buffer and the first pass's
+	// leading rows otherwise.
+	auto staged_smem = [&](int gg) { return (((size_t)gg * in_bytes + 127) & ~(size_t)127) + (size_t)gg * per; };
 	const bool staged_enabled = debug_knob("staged", 0) == 1;
-	if (((allow_staged == 1 && staged_enabled) || allow_staged == 2) && !s.tc && !odd && in_bytes % 16 == 0 && n >= 16) {
+	const bool long_ok = kind == 0 && dtype == SSFFT_F32 && n >= kLongStagedMin && s.per_cta == 1 &&
+	                     !(knobs && (knobs->cta_threads || knobs->emax || knobs->minb)) &&
+	                     debug_knob("long_staged", 0) == 1;
+	if (((allow_staged == 1 && (staged_enabled || long_ok)) || allow_staged == 2) && !s.tc && !odd &&
+	    in_bytes % 16 == 0 && n >= 16) {
 		int gs = s.per_cta;
-		auto staged_smem = [&](int gg) { return (((size_t)gg * in_bytes + 127) & ~(size_t)127) + (size_t)gg * per; };
 		while (gs > 1 && staged_smem(gs) > 76 * 1024) --gs;
-		if ((size_t)gs * in_bytes < (1u << 20) && staged_smem(gs) <= 200 * 1024) {
+		if ((size_t)gs * in_bytes < (1u << 20) && staged_smem(gs) <= kStagedSmemMax) {
 			s.staged = true;
 			s.per_cta = gs;
 			s.in_bytes = (unsigned)in_bytes;
 			s.smem_bytes = staged_smem(gs);
+		} else if (gs == 1 && kind == 0 && dtype == SSFFT_F32) {
+			// split staging: rows r < K of the first pass (K NB elements) staged, the rest copied
+			// into the work buffer once the previous group's last pass has read it
+			const int r0 = s.radices[0];
+			const size_t row = (size_t)(n / r0) * eb;
+			int k = per + 128 < kStagedSmemMax ? (int)((kStagedSmemMax - per - 128) / row) : 0;
+			k = std::min(k, r0 - 1);
+			if (row % 16) k &= ~1;  // staged and remaining bytes on 16-byte boundaries
+			if (2 * k >= r0) {
+				s.staged = true;
+				s.stage_rows = k;
+				s.in_bytes = (unsigned)in_bytes;
+				s.smem_bytes = (((size_t)k * row + 127) & ~(size_t)127) + per;
+			}
+		}
+		if (s.staged && s.per_cta == 1 && n >= kLongStagedMin && s.threads > kLongStagedThreads) {
+			// fewer threads holding more values each: the persistent loop spills at 512 threads
+			bool fits = false;
+			for (int em : {48, 64}) {
+				const int t2 = threads_for(em);
+				if (t2 <= kLongStagedThreads) {
+					s.emax = em;
+					s.threads = t2;
+					fits = true;
+					break;
+				}
+			}
+			if (!fits && !staged_enabled && allow_staged != 2) {
+				s.staged = false;
+				s.stage_rows = 0;
+				s.in_bytes = 0;
+				s.smem_bytes = per;
+			}
 		}
 	}
 	const int minb_env = (int)debug_knob("minb", 0);
 	// Measured on GB300: forcing more resident CTAs (register caps with small spills) did not
 	// beat the compiler's own allocation for the plain kernel of small transforms; the staged
-	// kernel's loop needs a cap of two CTAs.  A FP32 transform holding 32 values a thread in a CTA
+	// kernel's loop needs a cap of two CTAs where two fit in shared memory (a long transform whose
+	// stage and work buffers leave room for one CTA keeps the compiler's allocation: a cap of two
+	// there spills).  A FP32 transform holding 32 values a thread in a CTA
 	// of at most 256 threads (8192 points and up) compiles to 128-170 registers, one CTA per SM:
 	// capped at two CTAs (128 registers, no spills) it overlaps one CTA's HBM phase with the
 	// other's arithmetic (complex 8192: 51% -> 74% of the copy bandwidth).  debug switch minb overrides
 	// for experiments.
-	int mb = s.staged ? 2 : 1;
+	int mb = s.staged && 2 * s.smem_bytes <= 227 * 1024 ? 2 : 1;
 	if (!s.staged && dtype == SSFFT_F32 && s.emax == 2 * kElemsPerThread && s.per_cta * s.threads <= 256 &&
 	    2 * s.smem_bytes <= 227 * 1024)
 		mb = 2;
@@ -559,6 +601,7 @@ std::string Schedule::name(bool inverse) const {
 	if (!staged) r += std::string(odd ? "true" : "false") + ", ";
 	r += std::to_string(emax) + ", " + std::to_string(minb);
 	if (!staged) r += std::string(", ") + (fuse ? "true" : "false");
+	else r += ", " + std::to_string(stage_rows);
 	for (int x : radices) r += ", " + std::to_string(x);
 	r += ">";
 	return r;
@@ -857,6 +900,13 @@ bool plan_single_cta(size_t n, ssfft_dtype dtype, ssfft_kind kind) {
 	return true;
 }
 
+// Whether `s` is a long staged schedule the planner chose by itself (not asked for by the debug
+// switch staged=1 or by shape knobs).
+static bool long_staged_default(const Schedule &s, const Knobs &k) {
+	return s.staged && s.kind == 0 && s.dtype == SSFFT_F32 && s.n >= kLongStagedMin && s.per_cta == 1 &&
+	       debug_knob("staged", 0) != 1 && !k.cta_threads && !k.emax && !k.minb;
+}
+
 static ssfft_status plan_build_single(Plan *p) {
 	Schedule &s = p->main.sch;
 	// the default schedule decides whether n runs in one CTA; explicit or tuned knobs refine it
@@ -875,6 +925,18 @@ static ssfft_status plan_build_single(Plan *p) {
 		return SSFFT_ERR_INVALID_VALUE;  // explicit knobs that do not fit this size
 	const size_t smem_limit = device_smem_limit(p->device);
 	if (s.smem_bytes > smem_limit || si.smem_bytes > smem_limit) return SSFFT_ERR_UNSUPPORTED;
+	if ((s.staged || si.staged) && long_staged_default(s, p->knobs) && long_staged_default(si, p->knobs_inv)) {
+		// a long staged schedule the planner chose on its own stays only if its kernels compile
+		// without spilling (the persistent loop holds more registers than one pass list)
+		std::vector<CUfunction> fns;
+		ssfft_status st = jit_kernels({s.name(false), si.name(true)}, std::max(s.smem_bytes, si.smem_bytes), fns);
+		if (st != SSFFT_SUCCESS) return st;
+		if (jit_local_bytes(fns[0]) > kLongStagedLocalMax || jit_local_bytes(fns[1]) > kLongStagedLocalMax) {
+			if (!single_schedule(p->n, p->dtype, p->kind, p->batch, s, &p->knobs, 0, 0) ||
+			    !single_schedule(p->n, p->dtype, p->kind, p->batch, si, &p->knobs_inv, 0, 1))
+				return SSFFT_ERR_INVALID_VALUE;
+		}
+	}
 	// the inverse has its own pass tables when its passes differ
 	const bool split = si.radices != s.radices || si.pair != s.pair;
 	std::vector<double> tw, roots, rtw, rot, tw_i, roots_i, unused_rtw, unused_rot;
@@ -1205,6 +1267,16 @@ ssfft_status ssfft_plan_tuning(ssfft_plan_t plan, char *choice, size_t choice_le
 	return SSFFT_SUCCESS;
 }
 
+ssfft_status ssfft_plan_kernel(ssfft_plan_t plan, int inverse, char *name, size_t len) {
+	if (!plan || !name || !len) return SSFFT_ERR_INVALID_VALUE;
+	const Plan *p = reinterpret_cast<const Plan *>(plan);
+	const std::string k = p->large ? std::string("multi-pass") : (inverse ? p->main.sch_inv : p->main.sch).name(inverse != 0);
+	const size_t m = std::min(len - 1, k.size());
+	std::memcpy(name, k.data(), m);
+	name[m] = 0;
+	return SSFFT_SUCCESS;
+}
+
 ssfft_status ssfft_plan_destroy(ssfft_plan_t plan) {
 	if (!plan) return SSFFT_ERR_INVALID_VALUE;
 	Plan *p = reinterpret_cast<Plan *>(plan);
@@ -1288,7 +1360,7 @@ ssfft_status ssfft_exec(ssfft_plan_t plan, int inverse, const void *d_in, void *
 // `spin_limit` wait attempts.  The kernel must give up, raise the error flag (returned in *flags)
 // and return; nothing is in flight when it does, and the context stays usable.
 ssfft_status ssfft_diag_staged_timeout(size_t n, unsigned spin_limit, unsigned *flags) {
-	if (!flags || n < 16 || n > 4096) return SSFFT_ERR_INVALID_VALUE;
+	if (!flags || n < 16 || n > (size_t)kMaxSubTransform) return SSFFT_ERR_INVALID_VALUE;
 	*flags = 0;
 	Schedule s;
 	if (!make_schedule(SSFFT_F32, (int)n, 0, false, 4, s, 2) || !s.staged) return SSFFT_ERR_UNSUPPORTED;

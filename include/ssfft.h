@@ -134,6 +134,9 @@ size_t ssfft_plan_device_bytes(ssfft_plan_t plan);
  * transform and transforms per CTA.  radices may be NULL; cap is its length. */
 ssfft_status ssfft_plan_describe(ssfft_plan_t plan, int *npasses, int *radices, int cap, int *threads_per_transform,
                                  int *transforms_per_cta, int *kernel_launches);
+/* The kernel template a single-CTA plan launches in direction `inverse` (text truncated to
+ * len-1 bytes; "multi-pass" for plans beyond one CTA).  No reference counterpart. */
+ssfft_status ssfft_plan_kernel(ssfft_plan_t plan, int inverse, char *name, size_t len);
 
 /* ---------------------------------------------------------------- execution
  * Replaces FFT<V>::fft / ifft (signalsmith-fft.h:374-386, run :295-315) and RealFFT<V>::fft /
@@ -308,9 +311,10 @@ ssfft_status ssfft_schedule_info(size_t n, ssfft_dtype dtype, ssfft_kind kind, s
 ssfft_status ssfft_schedule_name(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, int inverse, char *buf,
                                  size_t cap);
 /* Failure-detection check (GPU): one staged launch of four n-point complex FP32 transforms
- * (16 <= n <= 4096) whose barrier waits for a copy that is never issued, bounded by spin_limit
- * attempts; the kernel must set the error flag (returned in *flags) and return.  No reference
- * counterpart. */
+ * (16 <= n <= 16384; lengths whose input does not fit beside the work buffer stage the first
+ * pass's leading rows and copy the rest into the work buffer, with a second barrier) whose
+ * barriers wait for copies that are never issued, bounded by spin_limit attempts; the kernel must
+ * set the error flag (returned in *flags) and return.  No reference counterpart. */
 ssfft_status ssfft_diag_staged_timeout(size_t n, unsigned spin_limit, unsigned *flags);
 ssfft_status ssfft_schedule_tables(size_t n, ssfft_dtype dtype, ssfft_kind kind, size_t batch, double *tw,
                                    size_t *ntw, double *roots, size_t *nroots, double *rtw, size_t *nrtw, double *rot,

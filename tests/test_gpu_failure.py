@@ -20,6 +20,10 @@ def test_lost_copy_raises_flag_and_context_survives():
     import fft_gb300 as ff
     assert ff.diag_staged_timeout(1024, 500) == 1
     assert ff.diag_staged_timeout(256, 50) == 1
+    # long transforms: whole input staged (12288), leading rows staged with the rest copied into
+    # the work buffer behind a second barrier (16384)
+    assert ff.diag_staged_timeout(12288, 200) == 1
+    assert ff.diag_staged_timeout(16384, 200) == 1
     # the context is still usable: an ordinary transform runs and is correct
     rng = np.random.default_rng(7)
     x = (rng.standard_normal((8, 1024)) + 1j * rng.standard_normal((8, 1024))).astype(np.complex64)
@@ -33,4 +37,4 @@ def test_diag_rejects_bad_arguments():
     with pytest.raises(ff.SsfftError):
         ff.diag_staged_timeout(8, 10)
     with pytest.raises(ff.SsfftError):
-        ff.diag_staged_timeout(8192, 10)
+        ff.diag_staged_timeout(32768, 10)

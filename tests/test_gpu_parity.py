@@ -288,6 +288,41 @@ def test_reference_shaped_api(F):
     assert rel_l2(F.rfft(t).cpu().numpy(), oracle.rfft(xr)) <= F64_TOL
 
 
+LONG_STAGED = [8192, 10240, 11520, 12288, 13824, 14400, 15000, 15360, 16000, 16384]
+
+
+@pytest.mark.parametrize("n", LONG_STAGED)
+def test_long_staged_kernels_match_oracle(F, n, monkeypatch):
+    """Long complex FP32 transforms on the bulk-copy staged kernel (SSFFT_DEBUG=long_staged=1 when
+    the plan is made): the whole input staged where it fits beside the work buffer, the first
+    pass's leading rows otherwise (the rest copied into the work buffer once the previous group's
+    last pass has read it).  More transforms than resident CTAs, so every persistent CTA walks
+    several groups and issues the next group's copies; forward and inverse against the oracle
+    on a sample of the transforms, the plan's error flag zero.  A schedule whose staged kernel
+    would spill runs the plain kernel instead (same check)."""
+    import ctypes
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    b = 2 * sms + 7
+    rng = np.random.default_rng(n + 5)
+    x = (rng.uniform(-1, 1, (b, n)) + 1j * rng.uniform(-1, 1, (b, n))).astype(np.complex64)
+    monkeypatch.setenv("SSFFT_DEBUG", "long_staged=1")
+    p = F.Plan(n, "f32", "complex", b)
+    monkeypatch.delenv("SSFFT_DEBUG")
+    name = p.kernel(False)
+    xi = dev(x)
+    xo = torch.empty_like(xi)
+    rows = list(range(0, b, 17)) + [b - 1]
+    for inv in (False, True):
+        p.exec(inv, xi.data_ptr(), xo.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        got = xo.cpu().numpy()[rows]
+        ref = np.stack([oracle.fft(x[r].astype(np.complex128), inv) for r in rows])
+        assert rel_l2(got, ref) <= F32_TOL, (n, inv, name, rel_l2(got, ref))
+    flags = ctypes.c_uint(99)
+    assert F.lib().ssfft_plan_error(p.handle, ctypes.byref(flags)) == 0 and flags.value == 0, name
+    p.destroy()
+
+
 def test_staged_kernels_report_no_error(F, monkeypatch):
     """The bulk-copy staged kernels (SSFFT_DEBUG=staged=1 when the plan is made) bound their waits and
     report a per-plan flag; after normal runs (aligned and misaligned inputs, partial last
