@@ -54,15 +54,16 @@ class PlanOptions(ctypes.Structure):
     _fields_ = [("autotune", ctypes.c_int), ("cta_threads", ctypes.c_int), ("values_per_thread", ctypes.c_int),
                 ("min_ctas_per_sm", ctypes.c_int), ("radices", ctypes.c_int * 24), ("precision", ctypes.c_int),
                 ("prefetch_quarter_waves", ctypes.c_int), ("fuse_split", ctypes.c_int),
-                ("cluster_split", ctypes.c_int)]
+                ("cluster_split", ctypes.c_int), ("staging", ctypes.c_int)]
 
 
 PRECISION = {"fp32": 0, "split_bf16": 1}
 
 
 def _options(autotune=0, radices=None, cta_threads=0, values_per_thread=0, min_ctas_per_sm=0, precision="fp32",
-             prefetch_quarter_waves=0, fuse_split=0, cluster_split=0):
+             prefetch_quarter_waves=0, fuse_split=0, cluster_split=0, staging=0):
     o = PlanOptions()
+    o.staging = int(staging)
     o.prefetch_quarter_waves = int(prefetch_quarter_waves)
     o.fuse_split = int(fuse_split)
     o.cluster_split = int(cluster_split)
@@ -311,19 +312,20 @@ class Plan:
     Keyword options map onto ``ssfft_plan_options`` (0 = planner default): ``autotune`` (1, 2),
     ``radices`` (explicit pass order), ``cta_threads``, ``values_per_thread``,
     ``min_ctas_per_sm`` (register cap), ``precision`` ("fp32" / "split_bf16"),
-    ``prefetch_quarter_waves``, ``fuse_split`` (1 / -1) and ``cluster_split`` (-1 never, k > 0
-    with ``radices``: the first k radices as the first phase of the two-CTA cluster kernel)."""
+    ``prefetch_quarter_waves``, ``fuse_split`` (1 / -1), ``cluster_split`` (-1 never, k > 0
+    with ``radices``: the first k radices as the first phase of the two-CTA cluster kernel) and
+    ``staging`` (bulk-copy input staging: -1 never, 1 wherever the input fits)."""
 
     def __init__(self, n: int, dtype="f32", kind="complex", batch: int = 1, *, autotune: int = 0, radices=None,
                  cta_threads: int = 0, values_per_thread: int = 0, min_ctas_per_sm: int = 0, precision="fp32",
-                 prefetch_quarter_waves: int = 0, fuse_split: int = 0, cluster_split: int = 0):
+                 prefetch_quarter_waves: int = 0, fuse_split: int = 0, cluster_split: int = 0, staging: int = 0):
         self.n = int(n)
         self.dtype = _dtype_code(dtype)
         self.kind = _kind_code(kind)
         self.batch = max(1, int(batch))
         h = _vp()
         opt = _options(autotune, radices, cta_threads, values_per_thread, min_ctas_per_sm, precision,
-                       prefetch_quarter_waves, fuse_split, cluster_split)
+                       prefetch_quarter_waves, fuse_split, cluster_split, staging)
         check(lib().ssfft_plan_create_ex(ctypes.byref(h), self.n, self.dtype, self.kind, self.batch,
                                          ctypes.byref(opt)),
               f"plan_create(n={n}, kind={kind}, batch={batch})")

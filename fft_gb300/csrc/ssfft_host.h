@@ -23,6 +23,7 @@ constexpr int kMaxSubTransform = 16384; // longest transform one CTA runs (FP32)
 constexpr size_t kStagedSmemMax = 227 * 1024 - 256;
 constexpr int kLongStagedMin = 8192;
 constexpr int kLongStagedThreads = 384;
+constexpr int kLongStagedMinThreads = 224;
 constexpr int kLongStagedLocalMax = 64;  // spill bytes per thread a default long staged kernel may have
 
 // A size-specialised kernel schedule: the compile-time parameters of one ssfft_cl::batch (or
@@ -64,6 +65,7 @@ struct Knobs {
 	                           // explicit radix order from the caller is kept as given), 1 always
 	int pair = -1;             // two-CTA cluster schedule: -1 planner default, 0 never, k > 0 with the
 	                           // first k of `radices` as phase A
+	int staging = 0;           // bulk-copy input staging: 0 planner default, -1 never, 1 wherever it fits
 	// no shape choice made (precision is not a shape choice)
 	bool empty() const { return radices.empty() && !cta_threads && !emax && !minb && prefetch < 0 && pair < 0; }
 	std::string str() const;

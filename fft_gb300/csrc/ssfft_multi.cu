@@ -472,7 +472,12 @@ ssfft_status ssfft_multi_create_ex(ssfft_multi_t *out, const size_t *sizes, size
 		g.work = (double)g.count * (double)g.n * std::log2((double)std::max<size_t>(g.n, 2));
 		m->groups.push_back(g);
 	}
-	// per-size plans, compiled concurrently
+	// per-size plans, compiled concurrently; they run offset-table launches, which the staged
+	// (bulk-copy) kernels do not take, so none stages
+	ssfft_plan_options po;
+	if (opt) po = *opt;
+	else std::memset(&po, 0, sizeof po);
+	po.staging = -1;
 	std::atomic<size_t> next{0};
 	std::atomic<int> bad{0};
 	std::vector<std::thread> th;
@@ -484,7 +489,7 @@ ssfft_status ssfft_multi_create_ex(ssfft_multi_t *out, const size_t *sizes, size
 			cudaSetDevice(dev);
 			for (size_t i = next++; i < mp->groups.size(); i = next++) {
 				Group &g = mp->groups[i];
-				if (ssfft_plan_create_ex(&g.plan, g.n, mp->dtype, SSFFT_COMPLEX, g.count, opt) != SSFFT_SUCCESS) bad = 1;
+				if (ssfft_plan_create_ex(&g.plan, g.n, mp->dtype, SSFFT_COMPLEX, g.count, &po) != SSFFT_SUCCESS) bad = 1;
 			}
 		});
 	for (auto &x : th) x.join();

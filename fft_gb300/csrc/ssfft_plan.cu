@@ -393,6 +393,7 @@ std::string Knobs::str() const {
 	if (prefetch >= 0) r += " prefetch=" + std::to_string(prefetch) + "/4";
 	if (precision == 1) r += " precision=split_bf16";
 	if (pair >= 0) r += " pair=" + std::to_string(pair);
+	if (staging) r += " staging=" + std::to_string(staging);
 	return r;
 }
 
@@ -496,16 +497,24 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	const size_t sb = eb / 2;
 	const size_t in_bytes = kind == 0 ? (size_t)n * eb : (size_t)2 * n * sb;  // real: n_real = 2h reals or h bins
 	// Opt-in for every size (debug switch staged=1, read when a plan is made): measured slower than
-	// the unstaged kernel on GB300 below 8192 points.  Long complex FP32 transforms (debug switch
-	// long_staged) run one transform per CTA at <= 384 threads, where the persistent loop does not
-	// spill, with the whole input staged when it fits beside the work buffer and the first pass's
-	// leading rows otherwise.
+	// the unstaged kernel on GB300 below 8192 points.  Long complex FP32 transforms whose plain
+	// kernel runs one CTA per SM stage by default (debug switch long_staged=0 turns it off): one
+	// transform per CTA at 224-384 threads, where the persistent loop does not spill (checked
+	// when the kernels are built), with the whole input staged when it fits beside the work buffer
+	// and the first pass's leading rows otherwise.  Measured on GB300 (complex, 512 MB per launch,
+	// fraction of the copy bandwidth): 8640 0.49 -> 0.65, 9216 0.53 -> 0.67, 10240 0.49 -> 0.67,
+	// 11520 0.48 -> 0.53, 13824 0.57 -> 0.65, 16384 0.57 -> 0.59 (leading rows); at 200 threads
+	// (10000) 0.46 -> 0.39, and where the plain kernel runs two CTAs per SM (8192) 0.68 -> 0.66.
 	auto staged_smem = [&](int gg) { return (((size_t)gg * in_bytes + 127) & ~(size_t)127) + (size_t)gg * per; };
-	const bool staged_enabled = debug_knob("staged", 0) == 1;
+	const int staging = knobs ? knobs->staging : 0;
+	const bool staged_enabled = staging == 1 || (staging == 0 && debug_knob("staged", 0) == 1);
+	const bool plain_two_per_sm = dtype == SSFFT_F32 && s.emax == 2 * kElemsPerThread &&
+	                              s.per_cta * s.threads <= 256 && 2 * s.smem_bytes <= 227 * 1024;
 	const bool long_ok = kind == 0 && dtype == SSFFT_F32 && n >= kLongStagedMin && s.per_cta == 1 &&
-	                     !(knobs && (knobs->cta_threads || knobs->emax || knobs->minb)) &&
-	                     debug_knob("long_staged", 0) == 1;
-	if (((allow_staged == 1 && (staged_enabled || long_ok)) || allow_staged == 2) && !s.tc && !odd &&
+	                     !plain_two_per_sm && !(knobs && (knobs->cta_threads || knobs->emax || knobs->minb)) &&
+	                     staging == 0 && debug_knob("long_staged", 1) == 1;
+	const Schedule plain = s;
+	if (((allow_staged == 1 && staging >= 0 && (staged_enabled || long_ok)) || allow_staged == 2) && !s.tc && !odd &&
 	    in_bytes % 16 == 0 && n >= 16) {
 		int gs = s.per_cta;
 		while (gs > 1 && staged_smem(gs) > 76 * 1024) --gs;
@@ -531,23 +540,19 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 		}
 		if (s.staged && s.per_cta == 1 && n >= kLongStagedMin && s.threads > kLongStagedThreads) {
 			// fewer threads holding more values each: the persistent loop spills at 512 threads
-			bool fits = false;
 			for (int em : {48, 64}) {
 				const int t2 = threads_for(em);
 				if (t2 <= kLongStagedThreads) {
 					s.emax = em;
 					s.threads = t2;
-					fits = true;
 					break;
 				}
 			}
-			if (!fits && !staged_enabled && allow_staged != 2) {
-				s.staged = false;
-				s.stage_rows = 0;
-				s.in_bytes = 0;
-				s.smem_bytes = per;
-			}
 		}
+		// a long staging the planner chose by itself keeps 224-384 threads per transform
+		if (s.staged && long_ok && !staged_enabled && allow_staged != 2 &&
+		    (s.threads < kLongStagedMinThreads || s.threads > kLongStagedThreads))
+			s = plain;
 	}
 	const int minb_env = (int)debug_knob("minb", 0);
 	// Measured on GB300: forcing more resident CTAs (register caps with small spills) did not
@@ -904,7 +909,7 @@ bool plan_single_cta(size_t n, ssfft_dtype dtype, ssfft_kind kind) {
 // switch staged=1 or by shape knobs).
 static bool long_staged_default(const Schedule &s, const Knobs &k) {
 	return s.staged && s.kind == 0 && s.dtype == SSFFT_F32 && s.n >= kLongStagedMin && s.per_cta == 1 &&
-	       debug_knob("staged", 0) != 1 && !k.cta_threads && !k.emax && !k.minb;
+	       k.staging == 0 && debug_knob("staged", 0) != 1 && !k.cta_threads && !k.emax && !k.minb;
 }
 
 static ssfft_status plan_build_single(Plan *p) {
@@ -916,6 +921,7 @@ static ssfft_status plan_build_single(Plan *p) {
 		Knobs best, best_inv;
 		ssfft_status st = autotune_single(p, p->autotune, best, best_inv, p->tune_log);
 		if (st != SSFFT_SUCCESS) return st;
+		best.staging = best_inv.staging = p->knobs.staging;  // not a tuned choice
 		p->knobs = best;
 		p->knobs_inv = best_inv;
 	}
@@ -1232,6 +1238,11 @@ ssfft_status ssfft_plan_create_ex(ssfft_plan_t *out, size_t n, ssfft_dtype dtype
 			return SSFFT_ERR_INVALID_VALUE;
 		}
 		if (opt->cluster_split) p->knobs.pair = opt->cluster_split > 0 ? opt->cluster_split : 0;
+		if (opt->staging < -1 || opt->staging > 1) {
+			delete p;
+			return SSFFT_ERR_INVALID_VALUE;
+		}
+		p->knobs.staging = opt->staging;
 	}
 	cudaError_t e = cudaGetDevice(&p->device);
 	ssfft_status st = e == cudaSuccess ? SSFFT_SUCCESS : cuda_fail(e, "cudaGetDevice");
@@ -1433,6 +1444,8 @@ ssfft_status ssfft_schedule_options(const ssfft_plan_options *opt) {
 	if (!g_diag_knobs.radices.empty()) g_diag_knobs.fuse = 0;
 	if (opt->fuse_split) g_diag_knobs.fuse = opt->fuse_split > 0 ? 1 : 0;
 	if (opt->cluster_split) g_diag_knobs.pair = opt->cluster_split > 0 ? opt->cluster_split : 0;
+	if (opt->staging < -1 || opt->staging > 1) return SSFFT_ERR_INVALID_VALUE;
+	g_diag_knobs.staging = opt->staging;
 	return SSFFT_SUCCESS;
 }
 

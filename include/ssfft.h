@@ -112,6 +112,9 @@ typedef struct ssfft_plan_options {
                             * the cluster, half a transform per CTA): 0 planner default (off),
                             * -1 never, k > 0 with `radices` given: its first k radices are the
                             * first phase (their product n1 and n / n1 both even) */
+    int staging;           /* input staged in shared memory by bulk (TMA) copies, persistent CTAs:
+                            * 0 planner default (long complex FP32 transforms whose plain kernel
+                            * runs one CTA per SM), -1 never, 1 wherever the input fits */
 } ssfft_plan_options;
 /* SSFFT_PRECISION_SPLIT_BF16 (complex FP32 plans that run in one CTA): the first radix pass
  * (radix <= 16) runs as tensor-core matrix products (tcgen05) on FP32 values split into three

@@ -291,24 +291,26 @@ def test_reference_shaped_api(F):
 LONG_STAGED = [8192, 10240, 11520, 12288, 13824, 14400, 15000, 15360, 16000, 16384]
 
 
+@pytest.mark.parametrize("staging", [0, 1])
 @pytest.mark.parametrize("n", LONG_STAGED)
-def test_long_staged_kernels_match_oracle(F, n, monkeypatch):
-    """Long complex FP32 transforms on the bulk-copy staged kernel (SSFFT_DEBUG=long_staged=1 when
-    the plan is made): the whole input staged where it fits beside the work buffer, the first
-    pass's leading rows otherwise (the rest copied into the work buffer once the previous group's
-    last pass has read it).  More transforms than resident CTAs, so every persistent CTA walks
-    several groups and issues the next group's copies; forward and inverse against the oracle
-    on a sample of the transforms, the plan's error flag zero.  A schedule whose staged kernel
-    would spill runs the plain kernel instead (same check)."""
+def test_long_staged_kernels_match_oracle(F, n, staging):
+    """Long complex FP32 transforms on the bulk-copy staged kernel: the planner's default (staging
+    where it measured faster and the kernel does not spill, the plain kernel otherwise) and
+    staging forced wherever the input fits (plan option staging=1).  The whole input is staged
+    where it fits beside the work buffer, the first pass's leading rows otherwise (the rest copied
+    into the work buffer once the previous group's last pass has read it).  More transforms than
+    resident CTAs, so every persistent CTA walks several groups and issues the next group's
+    copies; forward and inverse against the oracle on a sample of the transforms, the plan's
+    error flag zero."""
     import ctypes
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     b = 2 * sms + 7
     rng = np.random.default_rng(n + 5)
     x = (rng.uniform(-1, 1, (b, n)) + 1j * rng.uniform(-1, 1, (b, n))).astype(np.complex64)
-    monkeypatch.setenv("SSFFT_DEBUG", "long_staged=1")
-    p = F.Plan(n, "f32", "complex", b)
-    monkeypatch.delenv("SSFFT_DEBUG")
+    p = F.Plan(n, "f32", "complex", b, staging=staging)
     name = p.kernel(False)
+    if staging == 1:
+        assert "batch_staged" in name, name
     xi = dev(x)
     xo = torch.empty_like(xi)
     rows = list(range(0, b, 17)) + [b - 1]

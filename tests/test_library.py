@@ -216,6 +216,39 @@ def test_cluster_split_options_in_the_planner():
         with pytest.raises(F.SsfftError):
             F.schedule_name(10000, "f32", "complex", 8)
         F.schedule_options(cluster_split=-1)
+        assert F.schedule_name(16384, "f32", "complex", 8).startswith(("ssfft_cl::batch<", "ssfft_cl::batch_staged<"))
+        F.schedule_options(cluster_split=-1, staging=-1)
         assert F.schedule_name(16384, "f32", "complex", 8).startswith("ssfft_cl::batch<")
+    finally:
+        F.schedule_options()
+
+
+def test_long_staging_in_the_planner():
+    """Long complex FP32 transforms stage their input by default where the plain kernel runs one
+    CTA per SM and the staged one keeps 224-384 threads (the whole input when it fits beside the
+    work buffer, else the first pass's leading rows); the plan option staging=-1 keeps the plain
+    kernel and staging=1 stages wherever the input fits.  (No GPU: the build-time spill check is
+    covered by the GPU parity tests.)"""
+    try:
+        name = F.schedule_name(16384, "f32", "complex", 4096)
+        args = name[name.index("<") + 1:-1].split(", ")
+        assert name.startswith("ssfft_cl::batch_staged<float, 16384,") and int(args[2]) == 256, name
+        assert 0 < int(args[9]) < 32, name  # leading rows of the radix-32 first pass
+        assert F.schedule_name(10240, "f32", "complex", 4096).startswith("ssfft_cl::batch_staged<float, 10240, 320,")
+        assert ", 0, 16, 16, 40>" in F.schedule_name(10240, "f32", "complex", 4096)  # whole input staged
+        # two CTAs per SM for the plain kernel (8192), or too few threads staged (10000): plain
+        assert F.schedule_name(8192, "f32", "complex", 4096).startswith("ssfft_cl::batch<")
+        assert F.schedule_name(10000, "f32", "complex", 4096).startswith("ssfft_cl::batch<")
+        # real, FP64 and short transforms keep the plain kernel
+        assert F.schedule_name(8192, "f64", "complex", 64).startswith("ssfft_cl::batch<")
+        assert not F.schedule_name(32768, "f32", "real", 64).startswith("ssfft_cl::batch_staged")
+        assert F.schedule_name(4096, "f32", "complex", 64).startswith("ssfft_cl::batch<")
+        assert F.jit_check(16384, "f32", "complex", 4096) > 0
+        F.schedule_options(staging=-1)
+        assert F.schedule_name(16384, "f32", "complex", 4096).startswith("ssfft_cl::batch<")
+        F.schedule_options(staging=1)
+        assert F.schedule_name(4096, "f32", "complex", 64).startswith("ssfft_cl::batch_staged<")
+        with pytest.raises(F.SsfftError):
+            F.schedule_options(staging=2)
     finally:
         F.schedule_options()
