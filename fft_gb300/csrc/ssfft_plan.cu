@@ -516,6 +516,21 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	const Schedule plain = s;
 	if (((allow_staged == 1 && staging >= 0 && (staged_enabled || long_ok)) || allow_staged == 2) && !s.tc && !odd &&
 	    in_bytes % 16 == 0 && n >= 16) {
+		// long lengths whose default list spills in the staged kernel but another three-pass list
+		// does not (found by compiling the candidate lists of radices <= 32 for sm_103a with
+		// the compiler's register report: 8748 27-18-18 268 B, 9600 25-16-24 376 B, 12288
+		// 32-16-24 196 B of spills a thread against none for these)
+		if (long_ok && !(knobs && !knobs->radices.empty())) {
+			static const struct {
+				int n, r[3];
+			} kLongStagedLists[] = {{8748, {27, 12, 27}}, {9600, {24, 20, 20}}, {12288, {32, 12, 32}}};
+			for (const auto &e : kLongStagedLists)
+				if (e.n == n) {
+					s.radices.assign(e.r, e.r + 3);
+					s.emax = 2 * kElemsPerThread;
+					s.threads = threads_for(s.emax);
+				}
+		}
 		int gs = s.per_cta;
 		while (gs > 1 && staged_smem(gs) > 76 * 1024) --gs;
 		if ((size_t)gs * in_bytes < (1u << 20) && staged_smem(gs) <= kStagedSmemMax) {
