@@ -465,6 +465,54 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	}
 	if (t > kMaxCtaThreads) return false;
 	s.threads = t;
+	// Mid-length FP32 transforms (4097-8191 complex points, three passes, largest radix 17-25,
+	// planner's own shape): 16 values a thread with the largest radix in the middle pass, and
+	// as many CTAs per SM (<= 3) as leave each thread the registers its values need (about 2 per
+	// complex value plus 12).  Measured on GB300 (complex, 512 MB per launch, fraction of the copy
+	// bandwidth, against the 32-values-a-thread default): 5120 0.63 -> 0.81, 6144 0.67 -> 0.73,
+	// 6400 0.64 -> 0.68, 7680 0.51 -> 0.66, 8000 0.47 -> 0.59, 5000 0.59 -> 0.64, 4608 0.64 ->
+	// 0.71, 6000 0.58 -> 0.62; RealFFT 10240 / 12288 / 15360 0.53 / 0.55 / 0.43 -> 0.65 / 0.60 /
+	// 0.54.  Beyond 512 threads (7200) the default stays.  debug switch mid_rule=0 turns it off.
+	int mid_minb = 0;
+	{
+		const bool own_shape = !knobs || (knobs->radices.empty() && !knobs->emax && !knobs->cta_threads &&
+		                                  !knobs->minb && knobs->precision == 0);
+		const int rmax = *std::max_element(s.radices.begin(), s.radices.end());
+		if (own_shape && dtype == SSFFT_F32 && n > 4096 && n < 8192 && s.radices.size() == 3 && rmax > 16 &&
+		    rmax <= 25 && !s.tc && debug_knob("mid_rule", 1) != 0) {
+			Schedule m = s;
+			std::vector<int> rest = m.radices;
+			rest.erase(std::find(rest.begin(), rest.end(), rmax));
+			m.radices = {rest[0], rmax, rest[1]};
+			const std::vector<int> saved = s.radices;
+			s.radices = m.radices;
+			const int t16 = threads_for(kElemsPerThread);
+			s.radices = saved;
+			int v = 0;  // most complex values a thread holds in a pass
+			for (int r : m.radices) {
+				const int nb = n / r;
+				v = std::max(v, r * ((nb + t16 - 1) / t16));
+			}
+			const int w = (t16 + 31) / 32;
+			const size_t smem1 = (size_t)((n - 1) + ((n - 1) >> 4) + 2) * 8;  // one FP32 transform's slots
+			int k = 0;
+			for (int c = 1; c <= 3; ++c) {
+				// registers a thread gets at c CTAs per SM (the warps share four schedulers'
+				// 16K-register files), rounded down to the allocation unit of 8
+				const int per_smsp = (c * w + 3) / 4;
+				const int cap = (16384 / (32 * per_smsp)) & ~7;
+				if (cap >= 2 * v + 12 && (size_t)c * smem1 <= 227 * 1024) k = c;
+			}
+			const int w0 = (s.threads + 31) / 32;
+			const int k0 = s.emax == 2 * kElemsPerThread && s.threads <= 256 ? 2 : 1;  // the default's CTAs per SM
+			if (t16 <= 512 && k > 0 && k * w > k0 * w0) {
+				s.radices = m.radices;
+				s.emax = kElemsPerThread;
+				s.threads = t = t16;
+				mid_minb = k;
+			}
+		}
+	}
 	const size_t eb = dtype == SSFFT_F32 ? 8 : 16;
 	const int shift = dtype == SSFFT_F32 ? 4 : 3;
 	s.smem_stride = (n - 1) + ((n - 1) >> shift) + 1;
@@ -590,6 +638,7 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	if (!s.staged && !s.tc && dtype == SSFFT_F32 && s.emax == kElemsPerThread && s.per_cta == 1 &&
 	    s.threads == 256 && 5 * s.smem_bytes <= 227 * 1024)
 		mb = 5;
+	if (mid_minb > 0 && !s.staged) mb = mid_minb;
 	if (minb_env > 0) mb = minb_env;
 	if (knobs && knobs->minb > 0) mb = knobs->minb;
 	s.minb = std::max(1, mb);

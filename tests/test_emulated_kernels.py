@@ -38,6 +38,9 @@ CASES = [
     (13122, "f32", "complex", 1, 1), (12800, "f32", "complex", 1, 1), (15000, "f32", "complex", 1, 1),
     (8100, "f64", "complex", 1, 1), (8748, "f32", "complex", 1, 1), (9720, "f32", "complex", 1, 1),
     (10240, "f32", "complex", 1, 1), (11664, "f32", "complex", 1, 1),
+    # mid-length schedules (16 values a thread, largest radix in the middle pass)
+    (5120, "f32", "complex", 2, 2), (6000, "f32", "complex", 1, 1), (7680, "f32", "complex", 1, 1),
+    (12288, "f32", "real", 1, 1),
     (2, "f64", "real_halfshift", 1, 1), (4, "f64", "real_halfshift", 2, 2), (9, "f64", "real_halfshift", 1, 1),
     (12, "f32", "real_halfshift", 2, 2), (98, "f64", "real_halfshift", 1, 1), (960, "f32", "real_halfshift", 2, 2),
 ]
@@ -55,7 +58,8 @@ PAIR_CASES = [(16384, 1, 1, [16, 8, 16, 8], 2), (12288, 2, 2, [32, 16, 24], 1), 
 # "offs" compiles the plain kernel of the case (not the staged one this module's plans pick)
 OFFS_CASES = [((240, "f32", "complex", 2, 2), "offs"), ((64, "f32", "complex", 300, 300), "offs"),
               ((1920, "f32", "complex", 1, 1), "offs"), ((4096, "f32", "complex", 1, 1), "offs"),
-              ((16384, "f32", "complex", 1, 1), "pair16384"), ((1024, "f64", "complex", 7, 7), "offs")]
+              ((16384, "f32", "complex", 1, 1), "pair16384"), ((1024, "f64", "complex", 7, 7), "offs"),
+              ((5120, "f32", "complex", 2, 2), "offs"), ((7680, "f32", "complex", 1, 1), "offs")]
 VARIANTS = {"default": {"fuse_split": 1}, "tc": {"precision": "split_bf16"}, "offs": {}}
 for _c in PAIR_CASES:
     VARIANTS[f"pair{_c[0]}"] = ({"cluster_split": _c[4], "radices": _c[3]} if _c[3] else {})

@@ -154,7 +154,8 @@ def test_round_trip_is_n_times_input(F):
         assert rel_l2(back, n * x) <= 1e-13, n
 
 
-@pytest.mark.parametrize("n", [256, 768, 1000, 1024, 2048, 3072, 4096, 4800, 8192, 9216, 15000, 15360, 16200, 16384, 2187, 6561])
+@pytest.mark.parametrize("n", [256, 768, 1000, 1024, 2048, 3072, 4096, 4608, 4800, 5000, 5120, 6000, 6144, 6400, 7680,
+                               8000, 8192, 9216, 15000, 15360, 16200, 16384, 2187, 6561])
 def test_complex_f32_vs_oracle(F, n):
     rng = np.random.default_rng(n)
     b = 6
@@ -163,6 +164,29 @@ def test_complex_f32_vs_oracle(F, n):
         got, _ = run_complex(F, x, inv)
         ref = np.stack([oracle.fft(r.astype(np.complex128), inv) for r in x])
         assert rel_l2(got, ref) <= F32_TOL, (n, inv, rel_l2(got, ref))
+
+
+@pytest.mark.parametrize("n", [10240, 12288, 15360, 16384])
+def test_real_f32_mid_lengths_vs_oracle(F, n):
+    """RealFFT<float> lengths whose half runs the mid-length schedules (16 values a thread, the
+    largest radix in the middle pass, 2-3 CTAs per SM) or the fused 32-32-8 list: forward and
+    inverse of 40 frames against the oracle."""
+    rng = np.random.default_rng(n + 11)
+    b, h = 40, n // 2
+    x = rng.standard_normal((b, n)).astype(np.float32)
+    p = F.Plan(n, "f32", "real", b)
+    xi = dev(x)
+    s = torch.empty((b, h), dtype=torch.complex64, device="cuda")
+    back = torch.empty_like(xi)
+    st = torch.cuda.current_stream().cuda_stream
+    p.exec(False, xi.data_ptr(), s.data_ptr(), st)
+    p.exec(True, s.data_ptr(), back.data_ptr(), st)
+    torch.cuda.synchronize()
+    ref = np.stack([oracle.rfft(r.astype(np.float64)) for r in x])
+    assert rel_l2(s.cpu().numpy(), ref) <= F32_TOL
+    sb = s.cpu().numpy()
+    refi = np.stack([oracle.irfft(r.astype(np.complex128), n) for r in sb])
+    assert rel_l2(back.cpu().numpy(), refi) <= F32_TOL
 
 
 def test_config_fp64_1024_x256(F):
