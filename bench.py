@@ -971,6 +971,7 @@ def run_sizes(args):
     peak, kind_src = measured_peak_hbm()
     opts = json.loads(args.plan_options)
     sh = int(torch.cuda.current_stream().cuda_stream)
+    failures = []
     for kind in args.kinds.split(","):
         for n in (int(v) for v in args.sizes.split(",")):
             per = 16 * n if kind == "complex" else 8 * n  # algorithmic bytes per transform / frame
@@ -987,17 +988,28 @@ def run_sizes(args):
                 x = torch.randn(batch, n, device="cuda")
                 y = torch.empty(batch, n // 2, dtype=torch.complex64, device="cuda")
             res = {}
-            for inv, (a, b) in ((False, (x, y)), (True, (y, x))):
-                t = _time_device(lambda: p.exec(inv, a.data_ptr(), b.data_ptr(), sh), 10, 3)
-                res["inverse" if inv else "forward"] = {"us": round(t * 1e6, 1),
-                                                        "GB_s": round(batch * per / t / 1e9),
-                                                        "frac": round(batch * per / t / 1e9 / peak, 3)}
+            try:
+                for inv, (a, b) in ((False, (x, y)), (True, (y, x))):
+                    t = _time_device(lambda: p.exec(inv, a.data_ptr(), b.data_ptr(), sh), 10, 3)
+                    res["inverse" if inv else "forward"] = {"us": round(t * 1e6, 1),
+                                                            "GB_s": round(batch * per / t / 1e9),
+                                                            "frac": round(batch * per / t / 1e9 / peak, 3)}
+            except Exception as e:  # reported with the plan's kernels; the sweep goes on, exit status 1
+                failures.append(n)
+                print(json.dumps({"n": n, "kind": kind, "batch": batch, "error": str(e),
+                                  "schedule": p.tuning()["choice"], "kernel": p.kernel(False),
+                                  "kernel_inverse": p.kernel(True), "tune_log": p.tuning()["log"][-4:]}), flush=True)
+                del x, y, p
+                torch.cuda.empty_cache()
+                continue
             d = p.describe()
             print(json.dumps({"n": n, "kind": kind, "batch": batch, **res, "peak_GB_s": peak, "peak_source": kind_src,
                               "radices": d["radices"], "threads": d["threads"], "per_cta": d["per_cta"],
                               "schedule": p.tuning()["choice"], "kernel": p.kernel(False)}), flush=True)
             del x, y, p
             torch.cuda.empty_cache()
+    if failures:
+        sys.exit(1)
 
 
 def main():

@@ -83,7 +83,7 @@ struct SubPlan {
 	Schedule sch, sch_inv;
 	Tables tab, tab_inv;
 	CUfunction fwd = nullptr, inv = nullptr;
-	int grid_cap = 0;        // staged: resident CTAs (persistent grid)
+	int grid_cap = 0, grid_cap_inv = 0;  // staged (per direction): resident CTAs (persistent grid)
 	long long pf_dist = 0, pf_dist_inv = 0;  // batch kernel: L2 prefetch distance in CTAs
 	unsigned *err = nullptr; // staged: device error word
 };

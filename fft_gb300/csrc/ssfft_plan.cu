@@ -995,14 +995,19 @@ static ssfft_status plan_build_single(Plan *p) {
 		return SSFFT_ERR_INVALID_VALUE;  // explicit knobs that do not fit this size
 	const size_t smem_limit = device_smem_limit(p->device);
 	if (s.smem_bytes > smem_limit || si.smem_bytes > smem_limit) return SSFFT_ERR_UNSUPPORTED;
-	if ((s.staged || si.staged) && long_staged_default(s, p->knobs) && long_staged_default(si, p->knobs_inv)) {
-		// a long staged schedule the planner chose on its own stays only if its kernels compile
-		// without spilling (the persistent loop holds more registers than one pass list)
-		std::vector<CUfunction> fns;
-		ssfft_status st = jit_kernels({s.name(false), si.name(true)}, std::max(s.smem_bytes, si.smem_bytes), fns);
-		if (st != SSFFT_SUCCESS) return st;
-		if (jit_local_bytes(fns[0]) > kLongStagedLocalMax || jit_local_bytes(fns[1]) > kLongStagedLocalMax) {
-			if (!single_schedule(p->n, p->dtype, p->kind, p->batch, s, &p->knobs, 0, 0) ||
+	{
+		// a long staged schedule the planner chose on its own (per direction: tuned forward and
+		// inverse knobs may differ) stays only if its kernel compiles without spilling (the
+		// persistent loop holds more registers than one pass list)
+		const bool chk = long_staged_default(s, p->knobs), chk_i = long_staged_default(si, p->knobs_inv);
+		if (chk || chk_i) {
+			std::vector<CUfunction> fns;
+			ssfft_status st = jit_kernels({s.name(false), si.name(true)}, std::max(s.smem_bytes, si.smem_bytes), fns);
+			if (st != SSFFT_SUCCESS) return st;
+			if (chk && jit_local_bytes(fns[0]) > kLongStagedLocalMax &&
+			    !single_schedule(p->n, p->dtype, p->kind, p->batch, s, &p->knobs, 0, 0))
+				return SSFFT_ERR_INVALID_VALUE;
+			if (chk_i && jit_local_bytes(fns[1]) > kLongStagedLocalMax &&
 			    !single_schedule(p->n, p->dtype, p->kind, p->batch, si, &p->knobs_inv, 0, 1))
 				return SSFFT_ERR_INVALID_VALUE;
 		}
@@ -1058,7 +1063,8 @@ static ssfft_status plan_build_single(Plan *p) {
 	{
 		const long long resident = resident_ctas(fns[0], fns[0], s, p->device);
 		const long long resident_i = resident_ctas(fns[1], fns[1], si, p->device);
-		if (s.staged) p->main.grid_cap = (int)std::min(resident, resident_i);
+		if (s.staged) p->main.grid_cap = (int)resident;
+		if (si.staged) p->main.grid_cap_inv = (int)resident_i;
 		p->main.pf_dist = prefetch_distance(s, p->knobs, resident);
 		p->main.pf_dist_inv = prefetch_distance(si, p->knobs_inv, resident_i);
 	}
@@ -1096,18 +1102,24 @@ size_t plan_out_bytes(const Plan *p, int inverse, size_t batch) {
 // schedule (compiled on first use): u / ui the forward / inverse schedules (each direction with
 // its own knobs, so that its pass tables match), fns their kernels.
 static ssfft_status unstaged_kernels(const Plan *p, Schedule &u, Schedule &ui, std::vector<CUfunction> &fns) {
-	const Schedule &st = p->main.sch;
-	if (!make_schedule(st.dtype, st.n, st.kind, st.odd, p->batch, u, 0, p->knobs.empty() ? nullptr : &p->knobs) ||
-	    !make_schedule(st.dtype, st.n, st.kind, st.odd, p->batch, ui, 0,
-	                   p->knobs_inv.empty() ? nullptr : &p->knobs_inv))
+	const Schedule &st = p->main.sch, &sti = p->main.sch_inv;
+	// the plan's own radix order per direction (its pass tables follow it)
+	Knobs k = p->knobs, ki = p->knobs_inv;
+	k.radices = st.radices;
+	ki.radices = sti.radices;
+	if (!make_schedule(st.dtype, st.n, st.kind, st.odd, p->batch, u, 0, &k) ||
+	    !make_schedule(sti.dtype, sti.n, sti.kind, sti.odd, p->batch, ui, 0, &ki))
 		return SSFFT_ERR_UNSUPPORTED;
+	// a direction that is not staged keeps its own kernel
+	if (!st.staged) u = st;
+	if (!sti.staged) ui = sti;
 	return jit_kernels({u.name(false), ui.name(true)}, std::max(u.smem_bytes, ui.smem_bytes), fns);
 }
 
 // Compiles (and loads) what a later launch of `p` may need beyond the plan's own kernels, so that
 // the launch makes no module-loading call (e.g. inside a stream capture).
 ssfft_status plan_prepare_launch(const Plan *p) {
-	if (!p->main.sch.staged) return SSFFT_SUCCESS;
+	if (!p->main.sch.staged && !p->main.sch_inv.staged) return SSFFT_SUCCESS;
 	Schedule u, ui;
 	std::vector<CUfunction> fns;
 	return unstaged_kernels(p, u, ui, fns);
@@ -1146,8 +1158,8 @@ ssfft_status launch_batch_offs(const Plan *p, int inverse, const void *in, void 
                                const long long *d_offs, cudaStream_t s, const long long *d_offs_out) {
 	if (batch == 0) return SSFFT_SUCCESS;
 	if (p->large) return SSFFT_ERR_UNSUPPORTED;
-	if (p->main.sch.staged) return launch_unstaged(p, inverse, in, out, batch, s, d_offs, d_offs_out);
 	const Schedule &sch = inverse ? p->main.sch_inv : p->main.sch;
+	if (sch.staged) return launch_unstaged(p, inverse, in, out, batch, s, d_offs, d_offs_out);
 	const Tables &tab = inverse ? p->main.tab_inv : p->main.tab;
 	ssfft_cl::Args a;
 	std::memset(&a, 0, sizeof a);
@@ -1193,7 +1205,8 @@ ssfft_status launch_batch(const Plan *p, int inverse, const void *in, void *out,
 	long long grid = sch.grid((long long)batch);
 	if (sch.staged) {
 		if ((uintptr_t)in % 16) return launch_unstaged(p, inverse, in, out, batch, s);
-		grid = std::min<long long>(grid, p->main.grid_cap);
+		grid = std::min<long long>(grid, inverse ? p->main.grid_cap_inv : p->main.grid_cap);
+		if (grid < 1) return SSFFT_ERR_INVALID_VALUE;
 	}
 	if (grid > 0x7fffffffLL) return SSFFT_ERR_INVALID_SIZE;
 	return jit_launch(inverse ? p->main.inv : p->main.fwd, (unsigned)grid, (unsigned)sch.cta_threads(),

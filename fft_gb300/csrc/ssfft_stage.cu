@@ -132,7 +132,7 @@ static ssfft_status exec_host_small(Plan *p, int inverse, const void *h_in, void
 	// one-CTA plans with plain loads and stores (not the bulk-copy staged, tensor-core or cluster
 	// kernels) run the kernel on the mapped bounce buffers themselves, over the host link: no copy
 	// calls, one launch (debug switch small_zc=0 copies through device buffers instead)
-	const Schedule &sch = p->main.sch;
+	const Schedule &sch = inverse ? p->main.sch_inv : p->main.sch;
 	if (!p->large && !sch.staged && !sch.tc && !sch.pair && debug_knob("small_zc", 1) != 0) {
 		void *d_bin = nullptr, *d_bout = nullptr;
 		cudaError_t e = cudaHostGetDevicePointer(&d_bin, sg->bounce_in, 0);

@@ -349,6 +349,25 @@ def test_long_staged_kernels_match_oracle(F, n, staging):
     p.destroy()
 
 
+@pytest.mark.parametrize("n", [8748, 9600, 12288, 16384])
+def test_long_staged_unaligned_input_runs_plain_kernel_of_same_order(F, n):
+    """A staged plan given an input off a 16-byte boundary runs the plain kernel with the plan's own
+    radix order (its pass tables follow that order; 8748 / 9600 / 12288 stage with a list other
+    than the planner's plain default)."""
+    rng = np.random.default_rng(n + 3)
+    b = 9
+    x = (rng.uniform(-1, 1, (b, n)) + 1j * rng.uniform(-1, 1, (b, n))).astype(np.complex64)
+    p = F.Plan(n, "f32", "complex", b)
+    buf = torch.zeros(b * n + 1, dtype=torch.complex64, device="cuda")
+    buf[1:] = dev(x).reshape(-1)
+    out = torch.empty((b, n), dtype=torch.complex64, device="cuda")
+    for inv in (False, True):
+        assert F.lib().ssfft_exec(p.handle, int(inv), F._vp(buf.data_ptr() + 8), F._vp(out.data_ptr()), None) == 0
+        torch.cuda.synchronize()
+        ref = np.stack([oracle.fft(r.astype(np.complex128), inv) for r in x])
+        assert rel_l2(out.cpu().numpy(), ref) <= F32_TOL, (n, inv, p.kernel(inv))
+
+
 def test_staged_kernels_report_no_error(F, monkeypatch):
     """The bulk-copy staged kernels (SSFFT_DEBUG=staged=1 when the plan is made) bound their waits and
     report a per-plan flag; after normal runs (aligned and misaligned inputs, partial last
