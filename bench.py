@@ -155,6 +155,53 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def gpu_local_cpus(device_index: int):
+    """The CPUs of the host node the GPU is attached to (its PCI function's `local_cpulist` in
+    sysfs) that this process may run on, or None when that is unknown or every CPU."""
+    try:
+        import torch
+        pr = torch.cuda.get_device_properties(device_index)
+        dev = "%04x:%02x:%02x.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+        with open(f"/sys/bus/pci/devices/{dev}/local_cpulist") as f:
+            txt = f.read().strip()
+    except Exception:
+        return None
+    cpus = set()
+    for part in txt.split(","):
+        if "-" in part:
+            a, b = part.split("-")
+            cpus.update(range(int(a), int(b) + 1))
+        elif part:
+            cpus.add(int(part))
+    mine = os.sched_getaffinity(0)
+    usable = cpus & mine
+    return usable if usable and usable != mine else None
+
+
+class HostAffinity:
+    """Runs the host-buffer legs (pinned buffers, copy threads, the request server) on the CPUs
+    local to the GPU, so that page-locked buffers are allocated in the memory next to it; the
+    calling thread's affinity is restored on exit (the CPU baseline keeps every core)."""
+
+    def __init__(self, device_index: int):
+        self.cpus = gpu_local_cpus(device_index)
+        self.old = None
+
+    def note(self) -> str:
+        return f"{len(self.cpus)} CPUs local to the GPU" if self.cpus else "not bound (no local CPU list, or all CPUs)"
+
+    def __enter__(self):
+        if self.cpus:
+            self.old = os.sched_getaffinity(0)
+            os.sched_setaffinity(0, self.cpus)
+        return self
+
+    def __exit__(self, *exc):
+        if self.old:
+            os.sched_setaffinity(0, self.old)
+        return False
+
+
 def measured_peak_hbm() -> tuple[float, str]:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -401,6 +448,8 @@ def run_gpu(args, rank: int, world: int):
     rel = max(max(v.values()) for v in rel_sizes.values())
 
     # end to end through the C ABI with pinned host buffers
+    affinity = HostAffinity(local)
+    affinity.__enter__()
     e2e_steps = args.e2e_steps or max(3, args.steps // 10)
     hin = [torch.from_numpy(x.cpu().numpy()).pin_memory() for x in xs]
     hspec = [torch.empty(s.shape, dtype=s.dtype).pin_memory() for s in specs]
@@ -432,7 +481,10 @@ def run_gpu(args, rank: int, world: int):
     d2h = sum(s.numel() * 8 for s in hspec) + sum(b.numel() * 4 for b in hback)
     e2e = {"value": flops_per_step(frames) * e2e_steps * world / te / 1e9, "unit": "GFLOP/s",
            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
-           "path": "ssfft_exec_host (pinned host buffers, 3-stream copy/compute pipeline)"}
+           "path": "ssfft_exec_host (pinned host buffers, 3-stream copy/compute pipeline)",
+           "host_cpus": affinity.note()}
+    del hin, hspec, hback
+    affinity.__exit__(None, None, None)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -446,7 +498,9 @@ def run_gpu(args, rank: int, world: int):
 
     served = uneven = None
     if rank == 0 and not args.no_served:
-        served = served_block(args)
+        with HostAffinity(local) as aff:
+            served = served_block(args)
+            served["host_cpus"] = aff.note()
     if rank == 0 and not args.no_uneven:
         uneven = uneven_block(args, steps=50)
 
