@@ -239,14 +239,19 @@ def traffic_for(kernel: str):
 CPU_KIND = "port_native"  # the oracle's C restatement built -O3 with the host's vector ISA (timing only)
 
 
+_CPU_DATA: dict = {}
+
+
 def cpu_leg(frames: int, threads: int, kind: str = CPU_KIND, seed: int = 7, min_seconds: float = 0.0) -> dict:
     """Time the reference algorithm on the host cores: forward + inverse of every size over
     `frames` frames, one plan instance per thread; repeated until `min_seconds` of work."""
     import oracle
-    data = []
-    for i, n in enumerate(SIZES):
-        x = frames_for(n, frames, seed + i)
-        data.append((n, x, np.empty((frames, n // 2), dtype=np.complex64), np.empty((frames, n), dtype=np.float32)))
+    key = (frames, seed)
+    if key not in _CPU_DATA:  # the same frames for every step of a run (generating them costs more than a step)
+        _CPU_DATA.clear()
+        _CPU_DATA[key] = [(n, frames_for(n, frames, seed + i), np.empty((frames, n // 2), dtype=np.complex64),
+                           np.empty((frames, n), dtype=np.float32)) for i, n in enumerate(SIZES)]
+    data = _CPU_DATA[key]
     total_t, total_f, reps = 0.0, 0.0, 0
     while True:
         for n, x, spec, back in data:
