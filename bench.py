@@ -630,7 +630,7 @@ def run_large(args):
                       "peak_source": kind}), flush=True)
 
 
-SERVE_LOADS = (1e4, 1e5, 5e5, 1e6, 1.25e6, 1.5e6, 2e6)
+SERVE_LOADS = (1e4, 1e5, 5e5, 1e6, 1.25e6, 1.375e6, 1.5e6, 1.75e6, 2e6)
 P99_BOUND_US = 2000.0  # a load is "sustained" when the batched p99 stays within this and it keeps up
 
 
