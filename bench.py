@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--queue-mode", default="queue", choices=["queue", "pergraph"],
                     help="uneven_class workload: one queue-class launch or one launch per size")
     ap.add_argument("--members", type=int, default=16, help="uneven_members workload: sizes in the class")
+    ap.add_argument("--uneven-reps", type=int, default=0, help="uneven workload: timed submissions (0: auto)")
+    ap.add_argument("--uneven-fp32-only", action="store_true", help="uneven workload: skip the split-BF16 variant")
     ap.add_argument("--frames-total", type=int, default=4000, help="uneven_members workload: transforms in all")
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
                     help="CPU baseline: seconds of CPU work in the bounded sample")
@@ -791,7 +793,7 @@ def uneven_block(args, steps: int | None = None) -> dict:
     sample = list(range(0, 32768, 128))
     refs = {i: oracle.fft(xs[offs[i]:offs[i + 1]].astype(np.complex128)) for i in sample}
 
-    reps = steps or max(args.steps // 4, 50)
+    reps = args.uneven_reps or steps or max(args.steps // 4, 50)
 
     def variant(precision):
         t0 = time.perf_counter()
@@ -817,14 +819,14 @@ def uneven_block(args, steps: int | None = None) -> dict:
 
     t_all = time.perf_counter()
     fp32 = variant("fp32")
-    bf16 = variant("split_bf16")
+    bf16 = None if args.uneven_fp32_only else variant("split_bf16")
     out = {"workload": "32768 complex FP32 transforms, uneven sizes log-uniform over 2^a3^b5^c in [64,16384]",
            "alg_bytes": alg, "autotune": min(args.tune, 1), "peak_GB_s": peak, "peak_source": kind,
            "relL2_sample": f"{len(sample)} transforms (every 128th) against the FP64 oracle",
            "timing": f"CUDA events around {reps} back-to-back submissions, mean",
            "fp32_fma": fp32,
-           "split_bf16": dict(bf16, note="first radix pass (radix <= 16) on tcgen05 tensor cores, "
-                                         "three BF16 parts per operand, FP32 accumulation"),
+           "split_bf16": (dict(bf16, note="first radix pass (radix <= 16) on tcgen05 tensor cores, "
+                                          "three BF16 parts per operand, FP32 accumulation") if bf16 else None),
            "wall_s": time.perf_counter() - t_all}
     del x, y
     torch.cuda.empty_cache()
