@@ -969,6 +969,8 @@ bool plan_single_cta(size_t n, ssfft_dtype dtype, ssfft_kind kind) {
 	return true;
 }
 
+ssfft_status plan_prepare_launch(const Plan *p);
+
 // Whether `s` is a long staged schedule the planner chose by itself (not asked for by the debug
 // switch staged=1 or by shape knobs).
 static bool long_staged_default(const Schedule &s, const Knobs &k) {
@@ -1069,7 +1071,10 @@ static ssfft_status plan_build_single(Plan *p) {
 		p->main.pf_dist_inv = prefetch_distance(si, p->knobs_inv, resident_i);
 	}
 	p->launches_per_exec = 1;
-	return SSFFT_SUCCESS;
+	// a staged plan also runs the plain kernel of its order (scattered offsets, inputs off a
+	// 16-byte boundary): compile it now, so that no launch compiles (a server's first requests, a
+	// stream capture)
+	return plan_prepare_launch(p);
 }
 
 // scalar distances between consecutive transforms
