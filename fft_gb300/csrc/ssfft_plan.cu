@@ -564,18 +564,23 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	const Schedule plain = s;
 	if (((allow_staged == 1 && staging >= 0 && (staged_enabled || long_ok)) || allow_staged == 2) && !s.tc && !odd &&
 	    in_bytes % 16 == 0 && n >= 16) {
-		// long lengths whose default list spills in the staged kernel but another three-pass list
-		// does not (found by compiling the candidate lists of radices <= 32 for sm_103a with
-		// the compiler's register report: 8748 27-18-18 268 B, 9600 25-16-24 376 B, 12288
-		// 32-16-24 196 B of spills a thread against none for these)
+		// long lengths whose default list spills in the staged kernel but another list does not
+		// (found by compiling the candidate lists of three radices <= 32 and of four radices <= 16
+		// for sm_103a with the compiler's register report: 8748 27-18-18 268 B, 9600 25-16-24
+		// 376 B, 12288 32-16-24 196 B of spills a thread against none, 10800 16-45-15 556 B
+		// against 24 B for these; and measured faster than the plain kernel: 12288 0.54 -> 0.69,
+		// 9600 0.45 -> 0.59, 10800 0.42 -> 0.50 of the copy bandwidth)
 		if (long_ok && !(knobs && !knobs->radices.empty())) {
 			static const struct {
-				int n, r[3];
-			} kLongStagedLists[] = {{8748, {27, 12, 27}}, {9600, {24, 20, 20}}, {12288, {32, 12, 32}}};
+				int n, count, r[4], emax;  // radices, values a thread (the thread count follows)
+			} kLongStagedLists[] = {{8748, 3, {27, 12, 27}, 32},
+			                        {9600, 3, {24, 20, 20}, 48},
+			                        {10800, 4, {16, 15, 3, 15}, 48},
+			                        {12288, 3, {32, 12, 32}, 48}};
 			for (const auto &e : kLongStagedLists)
 				if (e.n == n) {
-					s.radices.assign(e.r, e.r + 3);
-					s.emax = 2 * kElemsPerThread;
+					s.radices.assign(e.r, e.r + e.count);
+					s.emax = e.emax;
 					s.threads = threads_for(s.emax);
 				}
 		}

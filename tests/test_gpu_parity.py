@@ -312,7 +312,7 @@ def test_reference_shaped_api(F):
     assert rel_l2(F.rfft(t).cpu().numpy(), oracle.rfft(xr)) <= F64_TOL
 
 
-LONG_STAGED = [8192, 10240, 11520, 12288, 13824, 14400, 15000, 15360, 16000, 16384]
+LONG_STAGED = [8192, 9600, 10240, 10800, 11520, 12288, 13824, 14400, 15000, 15360, 16000, 16384]
 
 
 @pytest.mark.parametrize("staging", [0, 1])
@@ -349,7 +349,7 @@ def test_long_staged_kernels_match_oracle(F, n, staging):
     p.destroy()
 
 
-@pytest.mark.parametrize("n", [8748, 9600, 12288, 16384])
+@pytest.mark.parametrize("n", [8748, 9600, 10800, 12288, 16384])
 def test_long_staged_unaligned_input_runs_plain_kernel_of_same_order(F, n):
     """A staged plan given an input off a 16-byte boundary runs the plain kernel with the plan's own
     radix order (its pass tables follow that order; 8748 / 9600 / 12288 stage with a list other
