@@ -545,20 +545,23 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	const size_t sb = eb / 2;
 	const size_t in_bytes = kind == 0 ? (size_t)n * eb : (size_t)2 * n * sb;  // real: n_real = 2h reals or h bins
 	// Opt-in for every size (debug switch staged=1, read when a plan is made): measured slower than
-	// the unstaged kernel on GB300 below 8192 points.  Long complex FP32 transforms whose plain
-	// kernel runs one CTA per SM stage by default (debug switch long_staged=0 turns it off): one
-	// transform per CTA at 224-384 threads, where the persistent loop does not spill (checked
-	// when the kernels are built), with the whole input staged when it fits beside the work buffer
-	// and the first pass's leading rows otherwise.  Measured on GB300 (complex, 512 MB per launch,
-	// fraction of the copy bandwidth): 8640 0.49 -> 0.65, 9216 0.53 -> 0.67, 10240 0.49 -> 0.67,
-	// 11520 0.48 -> 0.53, 13824 0.57 -> 0.65, 16384 0.57 -> 0.59 (leading rows); at 200 threads
-	// (10000) 0.46 -> 0.39, and where the plain kernel runs two CTAs per SM (8192) 0.68 -> 0.66.
+	// the unstaged kernel on GB300 below 8192 points.  Long FP32 transforms (8192 complex points
+	// and up, or RealFFT halves of that length) whose plain kernel runs one CTA per SM stage by
+	// default (debug switch long_staged=0 turns it off): one transform per CTA at 224-384 threads,
+	// where the persistent loop does not spill (checked when the kernels are built), with the
+	// whole input staged when it fits beside the work buffer and (complex) the first pass's
+	// leading rows otherwise.  Measured on GB300 (512 MB per launch, fraction of the copy
+	// bandwidth): complex 8640 0.49 -> 0.65, 9216 0.53 -> 0.67, 10240 0.49 -> 0.67, 11520 0.48 ->
+	// 0.53, 13824 0.57 -> 0.65, 16384 0.57 -> 0.59 (leading rows); RealFFT 20480 0.49 / 0.40 ->
+	// 0.50 / 0.45, 24576 0.48 / 0.42 -> 0.54 / 0.50 (forward / inverse; the split and pre-twiddle
+	// as separate steps); at 200 threads (10000) 0.46 -> 0.39, and where the plain kernel runs
+	// two CTAs per SM (complex 8192 0.68 -> 0.66, RealFFT 16384 0.61 -> 0.59).
 	auto staged_smem = [&](int gg) { return (((size_t)gg * in_bytes + 127) & ~(size_t)127) + (size_t)gg * per; };
 	const int staging = knobs ? knobs->staging : 0;
 	const bool staged_enabled = staging == 1 || (staging == 0 && debug_knob("staged", 0) == 1);
 	const bool plain_two_per_sm = dtype == SSFFT_F32 && s.emax == 2 * kElemsPerThread &&
 	                              s.per_cta * s.threads <= 256 && 2 * s.smem_bytes <= 227 * 1024;
-	const bool long_ok = kind == 0 && dtype == SSFFT_F32 && n >= kLongStagedMin && s.per_cta == 1 &&
+	const bool long_ok = dtype == SSFFT_F32 && kind != ssfft_cl::kRealHalfShift && n >= kLongStagedMin && s.per_cta == 1 &&
 	                     !plain_two_per_sm && !(knobs && (knobs->cta_threads || knobs->emax || knobs->minb)) &&
 	                     staging == 0 && debug_knob("long_staged", 1) == 1;
 	const Schedule plain = s;
@@ -570,7 +573,7 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 		// 376 B, 12288 32-16-24 196 B of spills a thread against none, 10800 16-45-15 556 B
 		// against 24 B for these; and measured faster than the plain kernel: 12288 0.54 -> 0.69,
 		// 9600 0.45 -> 0.59, 10800 0.42 -> 0.50 of the copy bandwidth)
-		if (long_ok && !(knobs && !knobs->radices.empty())) {
+		if (long_ok && kind == 0 && !(knobs && !knobs->radices.empty())) {
 			static const struct {
 				int n, count, r[4], emax;  // radices, values a thread (the thread count follows)
 			} kLongStagedLists[] = {{8748, 3, {27, 12, 27}, 32},
@@ -979,7 +982,7 @@ ssfft_status plan_prepare_launch(const Plan *p);
 // Whether `s` is a long staged schedule the planner chose by itself (not asked for by the debug
 // switch staged=1 or by shape knobs).
 static bool long_staged_default(const Schedule &s, const Knobs &k) {
-	return s.staged && s.kind == 0 && s.dtype == SSFFT_F32 && s.n >= kLongStagedMin && s.per_cta == 1 &&
+	return s.staged && s.dtype == SSFFT_F32 && s.n >= kLongStagedMin && s.per_cta == 1 &&
 	       k.staging == 0 && debug_knob("staged", 0) != 1 && !k.cta_threads && !k.emax && !k.minb;
 }
 

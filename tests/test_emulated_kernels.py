@@ -41,6 +41,7 @@ CASES = [
     # mid-length schedules (16 values a thread, largest radix in the middle pass)
     (5120, "f32", "complex", 2, 2), (6000, "f32", "complex", 1, 1), (7680, "f32", "complex", 1, 1),
     (12288, "f32", "real", 1, 1), (10800, "f32", "complex", 2, 2), (9600, "f32", "complex", 1, 1),
+    (20480, "f32", "real", 2, 2),
     (2, "f64", "real_halfshift", 1, 1), (4, "f64", "real_halfshift", 2, 2), (9, "f64", "real_halfshift", 1, 1),
     (12, "f32", "real_halfshift", 2, 2), (98, "f64", "real_halfshift", 1, 1), (960, "f32", "real_halfshift", 2, 2),
 ]

@@ -189,6 +189,43 @@ def test_real_f32_mid_lengths_vs_oracle(F, n):
     assert rel_l2(back.cpu().numpy(), refi) <= F32_TOL
 
 
+@pytest.mark.parametrize("n", [20480, 24576])
+def test_real_f32_long_staged_vs_oracle(F, n):
+    """RealFFT<float> lengths whose half (10240, 12288 points) runs the bulk-copy staged kernel by
+    default (split and pre-twiddle as separate steps): more frames than resident CTAs, forward
+    and inverse against the oracle on a sample of frames, the plan's error flag zero, and an
+    input off a 16-byte boundary (the plain kernel of the same radix order) giving the same
+    spectrum."""
+    import ctypes
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    b, h = 2 * sms + 7, n // 2
+    rng = np.random.default_rng(n + 21)
+    x = rng.standard_normal((b, n)).astype(np.float32)
+    p = F.Plan(n, "f32", "real", b)
+    assert "batch_staged" in p.kernel(False), p.kernel(False)
+    st = torch.cuda.current_stream().cuda_stream
+    xi = dev(x)
+    s = torch.empty((b, h), dtype=torch.complex64, device="cuda")
+    back = torch.empty_like(xi)
+    p.exec(False, xi.data_ptr(), s.data_ptr(), st)
+    p.exec(True, s.data_ptr(), back.data_ptr(), st)
+    torch.cuda.synchronize()
+    rows = list(range(0, b, 37)) + [b - 1]
+    ref = np.stack([oracle.rfft(x[r].astype(np.float64)) for r in rows])
+    assert rel_l2(s.cpu().numpy()[rows], ref) <= F32_TOL
+    sb = s.cpu().numpy()
+    refi = np.stack([oracle.irfft(sb[r].astype(np.complex128), n) for r in rows])
+    assert rel_l2(back.cpu().numpy()[rows], refi) <= F32_TOL
+    flags = ctypes.c_uint(99)
+    assert F.lib().ssfft_plan_error(p.handle, ctypes.byref(flags)) == 0 and flags.value == 0
+    buf = torch.zeros(b * n + 2, dtype=torch.float32, device="cuda")
+    buf[2:] = xi.reshape(-1)
+    s2 = torch.empty_like(s)
+    assert F.lib().ssfft_exec(p.handle, 0, F._vp(buf.data_ptr() + 8), F._vp(s2.data_ptr()), None) == 0
+    torch.cuda.synchronize()
+    assert rel_l2(s2.cpu().numpy()[rows], ref) <= F32_TOL
+
+
 def test_config_fp64_1024_x256(F):
     """FFT<double> N=1024, 256 transforms, forward then inverse, U[-1,1) (relL2 <= 1e-14)."""
     rng = np.random.default_rng(1)

@@ -224,8 +224,8 @@ def test_cluster_split_options_in_the_planner():
 
 
 def test_long_staging_in_the_planner():
-    """Long complex FP32 transforms stage their input by default where the plain kernel runs one
-    CTA per SM and the staged one keeps 224-384 threads (the whole input when it fits beside the
+    """Long FP32 transforms (complex, and RealFFT halves) stage their input by default where the
+    plain kernel runs one CTA per SM and the staged one keeps 224-384 threads (the whole input when it fits beside the
     work buffer, else the first pass's leading rows); the plan option staging=-1 keeps the plain
     kernel and staging=1 stages wherever the input fits.  (No GPU: the build-time spill check is
     covered by the GPU parity tests.)"""
@@ -239,9 +239,12 @@ def test_long_staging_in_the_planner():
         # two CTAs per SM for the plain kernel (8192), or too few threads staged (10000): plain
         assert F.schedule_name(8192, "f32", "complex", 4096).startswith("ssfft_cl::batch<")
         assert F.schedule_name(10000, "f32", "complex", 4096).startswith("ssfft_cl::batch<")
-        # real, FP64 and short transforms keep the plain kernel
+        # FP64 and short transforms keep the plain kernel
         assert F.schedule_name(8192, "f64", "complex", 64).startswith("ssfft_cl::batch<")
         assert not F.schedule_name(32768, "f32", "real", 64).startswith("ssfft_cl::batch_staged")
+        assert F.schedule_name(20480, "f32", "real", 64).startswith("ssfft_cl::batch_staged")  # half 10240
+        assert not F.schedule_name(16384, "f32", "real", 64).startswith("ssfft_cl::batch_staged")  # 2 CTAs / SM
+        assert not F.schedule_name(20480, "f32", "real_halfshift", 64).startswith("ssfft_cl::batch_staged")
         assert F.schedule_name(4096, "f32", "complex", 64).startswith("ssfft_cl::batch<")
         assert F.jit_check(16384, "f32", "complex", 4096) > 0
         F.schedule_options(staging=-1)
