@@ -552,10 +552,10 @@ bool make_schedule(ssfft_dtype dtype, int n, int kind, bool odd, size_t batch, S
 	// whole input staged when it fits beside the work buffer and (complex) the first pass's
 	// leading rows otherwise.  Measured on GB300 (512 MB per launch, fraction of the copy
 	// bandwidth): complex 8640 0.49 -> 0.65, 9216 0.53 -> 0.67, 10240 0.49 -> 0.67, 11520 0.48 ->
-	// 0.53, 13824 0.57 -> 0.65, 16384 0.57 -> 0.59 (leading rows); RealFFT 20480 0.49 / 0.40 ->
-	// 0.50 / 0.45, 24576 0.48 / 0.42 -> 0.54 / 0.50 (forward / inverse; the split and pre-twiddle
-	// as separate steps); at 200 threads (10000) 0.46 -> 0.39, and where the plain kernel runs
-	// two CTAs per SM (complex 8192 0.68 -> 0.66, RealFFT 16384 0.61 -> 0.59).
+	// 0.53, 13824 0.57 -> 0.65, 16384 0.57 -> 0.59 (leading rows); RealFFT 24576 0.48 / 0.42 ->
+	// 0.54 / 0.50 (forward / inverse; the split and pre-twiddle as separate steps); at 200
+	// threads (10000) 0.46 -> 0.39, and where the plain kernel runs two CTAs per SM (complex 8192
+	// 0.68 -> 0.66, RealFFT 16384 0.61 -> 0.59).
 	auto staged_smem = [&](int gg) { return (((size_t)gg * in_bytes + 127) & ~(size_t)127) + (size_t)gg * per; };
 	const int staging = knobs ? knobs->staging : 0;
 	const bool staged_enabled = staging == 1 || (staging == 0 && debug_knob("staged", 0) == 1);
