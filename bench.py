@@ -49,10 +49,11 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the host-buffer leg (default: steps/10)")
     ap.add_argument("--workload", default="realfft",
-                    choices=["realfft", "fp64", "large", "serve", "uneven", "precision", "sizes", "dropin",
+                    choices=["realfft", "fp64", "large", "serve", "served", "uneven", "precision", "sizes", "dropin",
                              "uneven_class", "uneven_members"],
                     help="realfft: the batched RealFFT<float> line (default); fp64: FFT<double> N=1024 x256; "
                          "large: single FP32 transforms of 2^24, 3^15, 2^12 3^4 5^2; serve: request serving sweep; "
+                         "served: the default line's served block alone; "
                          "sizes: per-size batched FP32 kernel sweep (--sizes, --kinds, --sweep-mb, --plan-options)")
     ap.add_argument("--sizes", default="256,512,1024,2048,4096,8192,16384",
                     help="sizes workload: comma-separated transform lengths")
@@ -72,6 +73,8 @@ def parse():
                     help="uneven_class workload: one queue-class launch or one launch per size")
     ap.add_argument("--members", type=int, default=16, help="uneven_members workload: sizes in the class")
     ap.add_argument("--uneven-reps", type=int, default=0, help="uneven workload: timed submissions (0: auto)")
+    ap.add_argument("--serve-waves", type=int, default=8, help="batched server: waves in flight")
+    ap.add_argument("--serve-wave-requests", type=int, default=256, help="batched server: requests per wave")
     ap.add_argument("--uneven-fp32-only", action="store_true", help="uneven workload: skip the split-BF16 variant")
     ap.add_argument("--frames-total", type=int, default=4000, help="uneven_members workload: transforms in all")
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
@@ -693,7 +696,8 @@ def served_block(args) -> dict:
     (one synchronous copy-in / launch / copy-out per request) on the same GPU."""
     import fft_gb300 as F
     t0 = time.perf_counter()
-    batched = F.Server(hbm_budget_bytes=16 << 30, waves=4, max_requests_per_wave=256, coalesce=True)
+    batched = F.Server(hbm_budget_bytes=16 << 30, waves=args.serve_waves,
+                       max_requests_per_wave=args.serve_wave_requests, coalesce=True)
     plain = F.Server(hbm_budget_bytes=16 << 30, coalesce=False)
     sweep = []
     for i, rate in enumerate(SERVE_LOADS):
@@ -714,6 +718,7 @@ def served_block(args) -> dict:
         "workload": "open-loop Poisson, 1-64 frames/request, N log-uniform over 2^a3^b5^c in [256,65536], "
                     "70% real / 30% complex, 50/50 fwd/inv, FP32, pinned host buffers, 16 GB HBM budget",
         "duration_s_per_load": args.served_duration,
+        "server": {"waves_in_flight": args.serve_waves, "requests_per_wave": args.serve_wave_requests},
         "p99_bound_us": P99_BOUND_US,
         "max_sustained_load": best["offered_transforms_per_s"] if best else None,
         "at_max_sustained_load": ({"GFLOP_s": best["batched"]["GFLOP_s"],
@@ -743,7 +748,8 @@ def run_serve(args):
     import fft_gb300 as F
     loads = [1e4, 1e5, 5e5, 1e6, 2e6]
     sweep = []
-    batched = F.Server(hbm_budget_bytes=16 << 30, waves=4, max_requests_per_wave=256, coalesce=True)
+    batched = F.Server(hbm_budget_bytes=16 << 30, waves=args.serve_waves,
+                       max_requests_per_wave=args.serve_wave_requests, coalesce=True)
     plain = F.Server(hbm_budget_bytes=16 << 30, coalesce=False)
     for i, rate in enumerate(loads):
         row = {"offered_transforms_per_s": rate}
@@ -1085,6 +1091,7 @@ def main():
         fb.build()
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         {"fp64": run_fp64, "large": run_large, "serve": run_serve, "uneven": run_uneven,
+         "served": lambda a: print(json.dumps(served_block(a)), flush=True),
          "precision": run_precision, "sizes": run_sizes, "dropin": run_dropin,
          "uneven_class": run_uneven_class, "uneven_members": run_uneven_members}[args.workload](args)
     else:

@@ -647,7 +647,7 @@ def _declare_server(l):
 class Server:
     """Continuous-batching request server (ssfft_server_* in include/ssfft.h)."""
 
-    def __init__(self, hbm_budget_bytes: int = 1 << 30, waves: int = 4, max_requests_per_wave: int = 256,
+    def __init__(self, hbm_budget_bytes: int = 1 << 30, waves: int = 8, max_requests_per_wave: int = 256,
                  coalesce: bool = True):
         l = _declare_server(lib())
         cfg = ServerConfig(hbm_budget_bytes, waves, max_requests_per_wave, int(bool(coalesce)))

@@ -551,7 +551,9 @@ ssfft_status ssfft_server_create(ssfft_server_t *out, const ssfft_server_config 
 	std::unique_ptr<ServerImpl> s(new ServerImpl());
 	if (cfg) s->cfg = *cfg;
 	if (!s->cfg.hbm_budget_bytes) s->cfg.hbm_budget_bytes = (size_t)1 << 30;
-	if (s->cfg.max_waves_in_flight <= 0) s->cfg.max_waves_in_flight = 4;
+	// default 8 waves in flight: measured on GB300 (the bench's Poisson mix), p99 at 1.5 M
+	// transforms/s offered 2.4 -> 1.6 ms and at 1.75 M/s 10.5 -> 3.8 ms against 4 waves
+	if (s->cfg.max_waves_in_flight <= 0) s->cfg.max_waves_in_flight = 8;
 	if (s->cfg.max_requests_per_wave <= 0) s->cfg.max_requests_per_wave = 256;
 	cudaError_t e = cudaGetDevice(&s->device);
 	if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");

@@ -197,7 +197,7 @@ typedef struct ssfft_server_s *ssfft_server_t;
 
 typedef struct {
 	size_t hbm_budget_bytes;   /* device arena for in-flight request buffers (0: 1 GiB) */
-	int max_waves_in_flight;   /* concurrent waves, one stream each (0: 4) */
+	int max_waves_in_flight;   /* concurrent waves, one stream each (0: 8) */
 	int max_requests_per_wave; /* (0: 256) */
 	int coalesce;              /* 1: batched waves; 0: plain, one request at a time, synchronously */
 } ssfft_server_config;
