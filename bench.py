@@ -160,6 +160,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def parse_cpulist(txt: str) -> set:
+    """CPU numbers of a sysfs CPU list ("0-3,8,10-11")."""
+    cpus = set()
+    for part in txt.strip().split(","):
+        if "-" in part:
+            a, b = part.split("-")
+            cpus.update(range(int(a), int(b) + 1))
+        elif part:
+            cpus.add(int(part))
+    return cpus
+
+
 def gpu_local_cpus(device_index: int):
     """The CPUs of the host node the GPU is attached to (its PCI function's `local_cpulist` in
     sysfs) that this process may run on, or None when that is unknown or every CPU."""
@@ -168,16 +180,9 @@ def gpu_local_cpus(device_index: int):
         pr = torch.cuda.get_device_properties(device_index)
         dev = "%04x:%02x:%02x.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
         with open(f"/sys/bus/pci/devices/{dev}/local_cpulist") as f:
-            txt = f.read().strip()
+            cpus = parse_cpulist(f.read())
     except Exception:
         return None
-    cpus = set()
-    for part in txt.split(","):
-        if "-" in part:
-            a, b = part.split("-")
-            cpus.update(range(int(a), int(b) + 1))
-        elif part:
-            cpus.add(int(part))
     mine = os.sched_getaffinity(0)
     usable = cpus & mine
     return usable if usable and usable != mine else None
