@@ -311,6 +311,42 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+def e2e_leg(F, args, plans, xs, specs, backs, frames: int, world: int, dist) -> dict:
+    """The same work through the C ABI's host-buffer entry point: pinned host frames -> bins ->
+    host frames per size, four host threads (one per size), H2D / kernel / D2H inside the timing."""
+    import torch
+    from concurrent.futures import ThreadPoolExecutor
+    e2e_steps = args.e2e_steps or max(3, args.steps // 10)
+    hin = [torch.from_numpy(x.cpu().numpy()).pin_memory() for x in xs]
+    hspec = [torch.empty(s.shape, dtype=s.dtype).pin_memory() for s in specs]
+    hback = [torch.empty(b.shape, dtype=b.dtype).pin_memory() for b in backs]
+    lib = F.lib()
+
+    def chain(p, a, s, b):
+        # one size: host frames -> bins -> host frames, through the C ABI's host-buffer entry point
+        F.check(lib.ssfft_exec_host(p.handle, 0, a.data_ptr(), s.data_ptr()), "exec_host")
+        F.check(lib.ssfft_exec_host(p.handle, 1, s.data_ptr(), b.data_ptr()), "exec_host")
+
+    with ThreadPoolExecutor(max_workers=len(SIZES)) as pool:
+        def e2e_step():
+            # the sizes are independent jobs: one host thread each (distinct plans are thread-safe)
+            list(pool.map(lambda args: chain(*args), zip(plans, hin, hspec, hback)))
+
+        for _ in range(2):
+            e2e_step()
+        if dist:
+            dist.barrier()
+        te = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        te = max_over_ranks(time.perf_counter() - te, dist, "cuda")
+    h2d = sum(a.numel() * 4 for a in hin) + sum(s.numel() * 8 for s in hspec)
+    d2h = sum(s.numel() * 8 for s in hspec) + sum(b.numel() * 4 for b in hback)
+    return {"value": flops_per_step(frames) * e2e_steps * world / te / 1e9, "unit": "GFLOP/s",
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
+            "path": "ssfft_exec_host (pinned host buffers, 3-stream copy/compute pipeline)"}
+
+
 def run_gpu(args, rank: int, world: int):
     import torch
 
@@ -462,44 +498,10 @@ def run_gpu(args, rank: int, world: int):
         rel_sizes[f"N{n}"] = {"fwd": rf, "inv": ri}
     rel = max(max(v.values()) for v in rel_sizes.values())
 
-    # end to end through the C ABI with pinned host buffers
-    affinity = HostAffinity(local)
-    affinity.__enter__()
-    e2e_steps = args.e2e_steps or max(3, args.steps // 10)
-    hin = [torch.from_numpy(x.cpu().numpy()).pin_memory() for x in xs]
-    hspec = [torch.empty(s.shape, dtype=s.dtype).pin_memory() for s in specs]
-    hback = [torch.empty(b.shape, dtype=b.dtype).pin_memory() for b in backs]
-    lib = F.lib()
-
-    from concurrent.futures import ThreadPoolExecutor
-    pool = ThreadPoolExecutor(max_workers=len(SIZES))
-
-    def chain(p, a, s, b):
-        # one size: host frames -> bins -> host frames, through the C ABI's host-buffer entry point
-        F.check(lib.ssfft_exec_host(p.handle, 0, a.data_ptr(), s.data_ptr()), "exec_host")
-        F.check(lib.ssfft_exec_host(p.handle, 1, s.data_ptr(), b.data_ptr()), "exec_host")
-
-    def e2e_step():
-        # the four sizes are independent jobs: one host thread each (distinct plans are thread-safe)
-        list(pool.map(lambda args: chain(*args), zip(plans, hin, hspec, hback)))
-
-    for _ in range(2):
-        e2e_step()
-    if dist:
-        dist.barrier()
-    te = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_step()
-    te = max_over_ranks(time.perf_counter() - te, dist, "cuda")
-    pool.shutdown()
-    h2d = sum(a.numel() * 4 for a in hin) + sum(s.numel() * 8 for s in hspec)
-    d2h = sum(s.numel() * 8 for s in hspec) + sum(b.numel() * 4 for b in hback)
-    e2e = {"value": flops_per_step(frames) * e2e_steps * world / te / 1e9, "unit": "GFLOP/s",
-           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
-           "path": "ssfft_exec_host (pinned host buffers, 3-stream copy/compute pipeline)",
-           "host_cpus": affinity.note()}
-    del hin, hspec, hback
-    affinity.__exit__(None, None, None)
+    # end to end through the C ABI with pinned host buffers (on the CPUs local to the GPU)
+    with HostAffinity(local) as affinity:
+        e2e = e2e_leg(F, args, plans, xs, specs, backs, frames, world, dist)
+        e2e["host_cpus"] = affinity.note()
 
     cpu = None
     if rank == 0 and not args.no_cpu:
