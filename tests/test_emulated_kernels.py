@@ -42,6 +42,9 @@ CASES = [
     (5120, "f32", "complex", 2, 2), (6000, "f32", "complex", 1, 1), (7680, "f32", "complex", 1, 1),
     (12288, "f32", "real", 1, 1), (10800, "f32", "complex", 2, 2), (9600, "f32", "complex", 1, 1),
     (20480, "f32", "real", 2, 2),
+    # one persistent CTA walking three groups of the leading-row staged kernel (the copies of the
+    # next group's rows issued from the first and the last pass)
+    (16384, "f32", "complex", 3, 3), (15000, "f32", "complex", 3, 3),
     (2, "f64", "real_halfshift", 1, 1), (4, "f64", "real_halfshift", 2, 2), (9, "f64", "real_halfshift", 1, 1),
     (12, "f32", "real_halfshift", 2, 2), (98, "f64", "real_halfshift", 1, 1), (960, "f32", "real_halfshift", 2, 2),
 ]
