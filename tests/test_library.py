@@ -255,3 +255,30 @@ def test_long_staging_in_the_planner():
             F.schedule_options(staging=2)
     finally:
         F.schedule_options()
+
+
+def test_long_schedules_respect_shared_memory_and_thread_bounds():
+    """Every FP32 length of 8192-16384 complex points (and the RealFFT lengths of those halves)
+    gets a schedule within the device's limits: shared memory within 227 KiB, at most 1024
+    threads per CTA; a staged one keeps one transform per CTA and 224-384 threads, and a
+    leading-row staging keeps at least half the first pass's rows and fewer than all."""
+    smooth = []
+    for n in range(8192, 16385):
+        m = n
+        for p in (2, 3, 5):
+            while m % p == 0:
+                m //= p
+        if m == 1:
+            smooth.append(n)
+    for kind, lengths in (("complex", smooth), ("real", [2 * n for n in smooth if n % 2 == 0])):
+        for n in lengths:
+            info = F.schedule_info(n, "f32", kind, 4096)
+            name = F.schedule_name(n, "f32", kind, 4096, 0)
+            assert info["smem_bytes"] <= 227 * 1024, (n, kind, info)
+            assert info["threads"] * info["per_cta"] <= 1024, (n, kind, info)
+            if "batch_staged" in name:
+                args = name[name.index("<") + 1:-1].split(", ")
+                assert info["per_cta"] == 1 and 224 <= info["threads"] <= 384, (n, kind, name)
+                k = int(args[9])
+                r0 = int(args[10])
+                assert k == 0 or (2 * k >= r0 and k < r0), (n, kind, name)
